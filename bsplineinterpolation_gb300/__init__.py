@@ -1,0 +1,404 @@
+"""GB300-native B-spline interpolation (hot path of 12ff54e/BSplineInterpolation).
+
+Python host mirror of the reference's C++ interface (src/include/
+Interpolation.hpp, InterpolationTemplate.hpp, BandLU.hpp) over the CUDA
+library's C-ABI (include/intp_gpu.h). The same interface exists as a
+header-only C++ drop-in under include/intp/.
+
+    f = InterpolationFunction(3, [False, False], mesh, (0.0, 1.0), (0.0, 2.0))
+    f(0.3, 1.1)                      # operator()
+    f.derivative_at((0.3, 1.1), 1, 0)  # range-checked derivative
+    f.evaluate(points, derivs=[[0, 0], [1, 0]])  # batched, device or host
+
+There is no CPU fallback: the CUDA library must be built (build.build()).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import IntpDomainError, IntpError
+
+__all__ = [
+    "InterpolationFunction",
+    "InterpolationFunction1D",
+    "InterpolationFunctionTemplate",
+    "InterpolationFunctionTemplate1D",
+    "BandLU",
+    "IntpError",
+    "IntpDomainError",
+]
+
+_PRECISIONS = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}
+
+
+def _torch():
+    try:
+        import torch
+        return torch
+    except ImportError:
+        return None
+
+
+def _is_cuda_tensor(x):
+    t = _torch()
+    return t is not None and isinstance(x, t.Tensor) and x.is_cuda
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        t = _torch()
+        if t is not None and t.cuda.is_available() and t.cuda.is_initialized():
+            return C.c_void_p(t.cuda.current_stream().cuda_stream)
+        return None
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _is_range(r):
+    return isinstance(r, (tuple, list)) and len(r) == 2 and all(np.isscalar(v) for v in r)
+
+
+class InterpolationFunctionTemplate:
+    """Knots and per-axis band LU factors for a mesh shape; solves for control
+    points of any value mesh of that shape.
+
+    Mirrors InterpolationFunctionTemplate (InterpolationTemplate.hpp:32-581):
+    constructor (:60-79) and interpolate (:118-143). `x_ranges` holds, per
+    axis, either (x_min, x_max) for a uniform axis or a 1-D array of sample
+    coordinates for a non-uniform one (size + 1 entries on a periodic axis).
+    """
+
+    def __init__(self, order, periodicity, mesh_dims, *x_ranges, precision="fp64",
+                 refine_steps=-1):
+        lib = _lib.load()
+        dims = [int(v) for v in np.atleast_1d(mesh_dims)]
+        D = len(dims)
+        if len(x_ranges) != D:
+            raise ValueError("need one x range per dimension")
+        if periodicity is None:
+            periodicity = [False] * D
+        periodicity = [bool(v) for v in np.atleast_1d(periodicity)]
+        if len(periodicity) != D:
+            raise ValueError("need one periodicity flag per dimension")
+        desc = _lib.TableDesc()
+        desc.dim = D
+        desc.order = int(order)
+        desc.precision = _PRECISIONS[precision]
+        desc.refine_steps = int(refine_steps)
+        self._coords = []
+        for d in range(D):
+            desc.periodic[d] = int(periodicity[d])
+            desc.size[d] = dims[d]
+            r = x_ranges[d]
+            if _is_range(r):
+                desc.range_lo[d] = float(r[0])
+                desc.range_hi[d] = float(r[1])
+                desc.coords[d] = None
+            else:
+                c = np.ascontiguousarray(np.asarray(r, np.float64))
+                if c.ndim != 1 or c.size != dims[d] + (1 if periodicity[d] else 0):
+                    raise ValueError("axis %d: expected %d coordinates" %
+                                     (d, dims[d] + (1 if periodicity[d] else 0)))
+                self._coords.append(c)
+                desc.coords[d] = c.ctypes.data
+        h = C.c_void_p()
+        _lib.check(lib.intp_table_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        self.dim = D
+        self.order = int(order)
+        self.dims = dims
+        self.precision = precision
+        self._periodicity = periodicity
+        self._x_ranges = x_ranges
+        self._refine = int(refine_steps)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_table_destroy(h)
+            self._h = None
+
+    def _solve(self, mesh, stream=None):
+        lib = _lib.load()
+        if _is_cuda_tensor(mesh):
+            torch = _torch()
+            m = mesh.to(torch.float64).contiguous()
+            if m.numel() != int(np.prod(self.dims)):
+                raise ValueError("mesh shape mismatch")
+            _lib.check(lib.intp_table_interpolate(self._h, C.c_void_p(m.data_ptr()), 1,
+                                                  _stream_ptr(stream)))
+            self._keep = m
+        else:
+            m = np.ascontiguousarray(np.asarray(mesh, np.float64))
+            if m.size != int(np.prod(self.dims)):
+                raise ValueError("mesh shape mismatch")
+            _lib.check(lib.intp_table_interpolate(self._h, m.ctypes.data, 0, _stream_ptr(stream)))
+            _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
+
+    def interpolate(self, mesh, stream=None):
+        """Solve for control points of `mesh` (InterpolationTemplate.hpp:118-143);
+        returns a new InterpolationFunction with its own device table."""
+        f = InterpolationFunction.__new__(InterpolationFunction)
+        f._template = InterpolationFunctionTemplate(self.order, self._periodicity, self.dims,
+                                                    *self._x_ranges, precision=self.precision,
+                                                    refine_steps=self._refine)
+        f._template._solve(mesh, stream)
+        f._init_from_template()
+        return f
+
+
+class InterpolationFunction:
+    """Tensor-product B-spline interpolant of a value mesh, on the GPU.
+
+    Mirrors InterpolationFunction<T, D, O, U> (Interpolation.hpp:17-507):
+    construction from (periodicity, mesh, x_ranges...) (:92-107), operator()
+    (:132-146), at (:153-169), derivative (:177-205), derivative_at (:213-244),
+    periodicity / uniform / range (:248-258), get_order (:267). Batched
+    evaluation is `evaluate`.
+    """
+
+    def __init__(self, order, periodicity, mesh, *x_ranges, precision="fp64", refine_steps=-1,
+                 stream=None):
+        if _is_cuda_tensor(mesh):
+            dims = list(mesh.shape)
+        else:
+            dims = list(np.shape(mesh))
+        if len(x_ranges) == 1 and len(dims) > 1 and not _is_range(x_ranges[0]):
+            x_ranges = tuple(x_ranges[0])
+        self._template = InterpolationFunctionTemplate(order, periodicity, dims, *x_ranges,
+                                                       precision=precision,
+                                                       refine_steps=refine_steps)
+        self._template._solve(mesh, stream)
+        self._init_from_template()
+
+    def _init_from_template(self):
+        lib = _lib.load()
+        t = self._template
+        self.dim = t.dim
+        self.order = t.order
+        self.precision = t.precision
+        self._h = t._h
+        self._range = []
+        self._uniform = []
+        self._per = []
+        for d in range(self.dim):
+            nk, lo, hi, per, uni = (C.c_int64(), C.c_double(), C.c_double(), C.c_int32(),
+                                    C.c_int32())
+            _lib.check(lib.intp_table_axis_info(self._h, d, C.byref(nk), C.byref(lo), C.byref(hi),
+                                                C.byref(per), C.byref(uni)))
+            self._range.append((lo.value, hi.value))
+            self._uniform.append(bool(uni.value))
+            self._per.append(bool(per.value))
+
+    # -- properties (Interpolation.hpp:248-267) --
+    def periodicity(self, d):
+        return self._per[d]
+
+    def uniform(self, d):
+        return self._uniform[d]
+
+    def range(self, d):
+        return self._range[d]
+
+    def get_order(self):
+        return self.order
+
+    def knots(self, d):
+        lib = _lib.load()
+        nk = C.c_int64()
+        _lib.check(lib.intp_table_axis_info(self._h, d, C.byref(nk), None, None, None, None))
+        out = np.zeros(nk.value)
+        _lib.check(lib.intp_table_knots(self._h, d, out.ctypes.data))
+        return out
+
+    def control_points(self):
+        out = np.zeros(int(np.prod(self._template.dims)))
+        _lib.check(_lib.load().intp_table_get_control_points(self._h, out.ctypes.data))
+        return out.reshape(self._template.dims)
+
+    # -- batched evaluation --
+    def evaluate(self, points, derivs=None, out=None, out_dtype=None, stream=None):
+        """Values (derivs None) or derivatives (derivs: K x D orders) at N
+        points (N x D). CUDA tensors stay on the device (result: N x K CUDA
+        tensor); host arrays take the host path (result: N x K numpy array)."""
+        lib = _lib.load()
+        D = self.dim
+        if out_dtype is None:
+            out_dtype = "f32" if self.precision == "mixed" else "f64"
+        od = _lib.F32 if out_dtype == "f32" else _lib.F64
+        if derivs is None:
+            kp, K = None, 1
+            karr = None
+        else:
+            karr = np.ascontiguousarray(np.asarray(derivs, np.int32).reshape(-1, D))
+            K = karr.shape[0]
+            kp = karr.ctypes.data
+        if _is_cuda_tensor(points):
+            torch = _torch()
+            pts = points.to(torch.float64).contiguous().reshape(-1, D)
+            n = pts.shape[0]
+            if out is None:
+                out = torch.empty((n, K), dtype=torch.float32 if od == _lib.F32 else torch.float64,
+                                  device=pts.device)
+            _lib.check(lib.intp_eval(self._h, C.c_void_p(pts.data_ptr()), n, kp, K,
+                                     C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
+            return out
+        pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, D))
+        n = pts.shape[0]
+        res = np.zeros((n, K), np.float32 if od == _lib.F32 else np.float64)
+        _lib.check(lib.intp_eval_host(self._h, pts.ctypes.data, n, kp, K, res.ctypes.data, od,
+                                      _stream_ptr(stream)))
+        return res
+
+    def locate(self, points, stream=None):
+        """Knot-span indices (N x D int64) and wrapped coordinates, for CUDA
+        tensors of points (BSpline.hpp:125-157)."""
+        torch = _torch()
+        lib = _lib.load()
+        pts = points.to(torch.float64).contiguous().reshape(-1, self.dim)
+        cells = torch.empty(pts.shape, dtype=torch.int64, device=pts.device)
+        wrapped = torch.empty(pts.shape, dtype=torch.float64, device=pts.device)
+        _lib.check(lib.intp_locate(self._h, C.c_void_p(pts.data_ptr()), pts.shape[0],
+                                   C.c_void_p(cells.data_ptr()), C.c_void_p(wrapped.data_ptr()),
+                                   _stream_ptr(stream)))
+        return cells, wrapped
+
+    def check_range(self, points, stream=None):
+        """Index of the first point outside a non-periodic axis range, or -1."""
+        torch = _torch()
+        lib = _lib.load()
+        pts = points.to(torch.float64).contiguous().reshape(-1, self.dim)
+        bad = C.c_int64()
+        _lib.check(lib.intp_check_range(self._h, C.c_void_p(pts.data_ptr()), pts.shape[0],
+                                        C.byref(bad), _stream_ptr(stream)))
+        return bad.value
+
+    # -- single-point API of the reference --
+    def _coord(self, coords):
+        if len(coords) == 1 and np.ndim(coords[0]) == 1:
+            coords = tuple(coords[0])
+        if len(coords) != self.dim:
+            raise ValueError("expected %d coordinates" % self.dim)
+        return np.asarray(coords, np.float64)
+
+    def _boundary_check(self, c):
+        for d in range(self.dim):
+            lo, hi = self._range[d]
+            if not self._per[d] and (c[d] < lo or c[d] > hi):
+                raise IntpDomainError(_lib.ERR_DOMAIN,
+                                      "Given coordinate out of interpolation function range!")
+
+    def __call__(self, *coords):
+        c = self._coord(coords)
+        return float(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
+
+    def at(self, *coords):
+        c = self._coord(coords)
+        self._boundary_check(c)
+        return float(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
+
+    def _derivs(self, coord, orders):
+        if len(orders) == 1 and np.ndim(orders[0]) == 1:
+            orders = tuple(orders[0])
+        if len(orders) != self.dim:
+            raise ValueError("expected %d derivative orders" % self.dim)
+        return np.asarray(coord, np.float64).reshape(1, -1), np.asarray(orders, np.int32)
+
+    def derivative(self, coord, *orders):
+        c, k = self._derivs(coord, orders)
+        return float(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
+
+    def derivative_at(self, coord, *orders):
+        c, k = self._derivs(coord, orders)
+        self._boundary_check(c[0])
+        return float(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
+
+
+class InterpolationFunction1D(InterpolationFunction):
+    """1-D convenience form (Interpolation.hpp:509-540). Without an x range the
+    samples sit at 0, 1, 2, ...: the range is (0, n-1), or (0, n) when periodic
+    (INTP_PERIODIC_NO_DUMMY_POINT)."""
+
+    def __init__(self, order, f, x_range=None, periodic=False, **kw):
+        f = f if _is_cuda_tensor(f) else np.asarray(f, np.float64)
+        n = f.shape[0]
+        if x_range is None:
+            x_range = (0.0, float(n - (0 if periodic else 1)))
+        super().__init__(order, [periodic], f, x_range, **kw)
+
+
+class InterpolationFunctionTemplate1D(InterpolationFunctionTemplate):
+    """InterpolationTemplate.hpp:583-604: range defaults to (0, f_length - 1)."""
+
+    def __init__(self, order, f_length, x_range=None, periodic=False, **kw):
+        if x_range is None:
+            x_range = (0.0, float(f_length - 1))
+        super().__init__(order, [periodic], [f_length], x_range, **kw)
+
+
+class BandLU:
+    """Band LU without pivoting (BandLU.hpp), solved on the GPU.
+
+    `band` is n x (1+p+q) in the reference's storage (A(i,j) =
+    band[j, i+q-j]); cyclic matrices add `right` ((n-q-1) x p) and `bottom`
+    ((n-p-1) x q) corner blocks (ExtendedBandMatrix)."""
+
+    def __init__(self, band, p, q, right=None, bottom=None):
+        lib = _lib.load()
+        band = np.ascontiguousarray(band, np.float64)
+        n = band.shape[0]
+        cyclic = right is not None
+        self._r = None if right is None else np.ascontiguousarray(right, np.float64)
+        self._b = None if bottom is None else np.ascontiguousarray(bottom, np.float64)
+        h = C.c_void_p()
+        _lib.check(lib.intp_bandlu_create(n, p, q, int(cyclic), band.ctypes.data,
+                                          None if self._r is None else self._r.ctypes.data,
+                                          None if self._b is None else self._b.ctypes.data,
+                                          C.byref(h)))
+        self._h = h
+        self.n = n
+
+    @classmethod
+    def from_dense(cls, a, p, q, cyclic=False):
+        """Band storage from a dense matrix (only band / side-band entries read)."""
+        a = np.asarray(a, np.float64)
+        n = a.shape[0]
+        band = np.zeros((n, 1 + p + q))
+        for i in range(n):
+            for j in range(max(0, i - p), min(n, i + q + 1)):
+                band[j, i + q - j] = a[i, j]
+        if not cyclic:
+            return cls(band, p, q)
+        right = np.zeros((max(n - q - 1, 0), p))
+        bottom = np.zeros((max(n - p - 1, 0), q))
+        for i in range(n):
+            for j in range(n):
+                if j >= max(n - p, i + q + 1):
+                    right[i, j + p - n] = a[i, j]
+                elif i >= max(n - q, j + p + 1):
+                    bottom[j, i + q - n] = a[i, j]
+        return cls(band, p, q, right, bottom)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_bandlu_destroy(h)
+            self._h = None
+
+    def solve(self, x, stream=None):
+        """Solves in place along axis 0 of a CUDA tensor (n, ...) of float64;
+        for a host array returns the solution (copied through the device)."""
+        lib = _lib.load()
+        torch = _torch()
+        if _is_cuda_tensor(x):
+            assert x.dtype == torch.float64 and x.is_contiguous() and x.shape[0] == self.n
+            inner = x.numel() // self.n
+            _lib.check(lib.intp_bandlu_solve(self._h, C.c_void_p(x.data_ptr()), 1, inner,
+                                             _stream_ptr(stream)))
+            return x
+        xt = torch.tensor(np.asarray(x, np.float64), device="cuda")
+        self.solve(xt, stream)
+        torch.cuda.synchronize()
+        return xt.cpu().numpy()

@@ -1,0 +1,108 @@
+"""ctypes binding of the CUDA library's C-ABI (include/intp_gpu.h).
+
+The shared library is built in-tree by bsplineinterpolation_gb300/build.py.
+There is no CPU fallback: importing the binding without the built library
+raises, and every call that fails raises with the library's error message.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libintp_gb300.so")
+
+MAX_DIM = 4
+MAX_ORDER = 7
+MAX_DERIV = 16
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_DOMAIN = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_CUDA = 4
+ERR_STATE = 5
+ERR_UNSUPPORTED = 6
+ERR_TIMEOUT = 7
+ERR_BUDGET = 8
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+F64 = 0
+F32 = 1
+
+
+class TableDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("order", C.c_int32),
+        ("precision", C.c_int32),
+        ("refine_steps", C.c_int32),
+        ("periodic", C.c_int32 * MAX_DIM),
+        ("size", C.c_int64 * MAX_DIM),
+        ("range_lo", C.c_double * MAX_DIM),
+        ("range_hi", C.c_double * MAX_DIM),
+        ("coords", C.c_void_p * MAX_DIM),
+    ]
+
+
+class IntpError(RuntimeError):
+    """Failure reported by the CUDA library (status code and message)."""
+
+    def __init__(self, status, msg):
+        super().__init__("intp status %d: %s" % (status, msg))
+        self.status = status
+
+
+class IntpDomainError(IntpError, ValueError):
+    """A coordinate lies outside the range of a non-periodic axis
+    (the reference throws std::domain_error, Interpolation.hpp:482-491)."""
+
+
+# the symbols of include/intp_gpu.h: name -> (restype, argtypes)
+_P = C.c_void_p
+SIGNATURES = {
+    "intp_table_create": (C.c_int, [C.POINTER(TableDesc), C.POINTER(C.c_void_p)]),
+    "intp_table_destroy": (C.c_int, [_P]),
+    "intp_table_interpolate": (C.c_int, [_P, _P, C.c_int32, _P]),
+    "intp_table_set_control_points": (C.c_int, [_P, _P]),
+    "intp_table_get_control_points": (C.c_int, [_P, _P]),
+    "intp_table_axis_info": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, _P]),
+    "intp_table_knots": (C.c_int, [_P, C.c_int32, _P]),
+    "intp_eval": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_eval_host": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_check_range": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
+    "intp_locate": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P]),
+    "intp_stream_synchronize": (C.c_int, [_P]),
+    "intp_last_error": (C.c_char_p, []),
+    "intp_launch_count": (C.c_uint64, []),
+    "intp_bandlu_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P,
+                                     C.POINTER(C.c_void_p)]),
+    "intp_bandlu_solve": (C.c_int, [_P, _P, C.c_int64, C.c_int64, _P]),
+    "intp_bandlu_destroy": (C.c_int, [_P]),
+}
+
+_lib = None
+
+
+def load():
+    """Loads the built library (it must exist; nothing falls back to the CPU)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("CUDA library %s is not built; run bsplineinterpolation_gb300.build.build()"
+                          % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status != OK:
+        msg = load().intp_last_error().decode(errors="replace")
+        if status == ERR_DOMAIN:
+            raise IntpDomainError(status, msg)
+        raise IntpError(status, msg)

@@ -1,0 +1,690 @@
+// C-ABI of the library (include/intp_gpu.h): table lifetime, the control-point
+// solve pipelines and batched evaluation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "intp_gpu.h"
+#include "launch.hpp"
+#include "spline_model.hpp"
+
+using namespace intp_gb300;
+
+namespace {
+
+std::atomic<unsigned long long> g_launches{0};
+
+// binned evaluation: shared-memory tile budget per CTA, queries per chunk
+// (chunk outputs stay L2-resident), smallest batch worth binning
+constexpr int64_t kTileBytes = 48 * 1024;
+constexpr int64_t kDefaultChunk = int64_t{1} << 22;
+constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
+
+// INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
+int eval_mode() {
+    const char* v = std::getenv("INTP_GB300_EVAL");
+    if (!v) return 0;
+    if (std::strcmp(v, "direct") == 0) return 1;
+    if (std::strcmp(v, "binned") == 0) return 2;
+    return 0;
+}
+
+int64_t eval_chunk() {
+    const char* v = std::getenv("INTP_GB300_CHUNK");
+    if (!v) return kDefaultChunk;
+    const long long c = std::atoll(v);
+    return c >= 1024 ? c : kDefaultChunk;
+}
+
+// Keep memory freed by cudaFreeAsync in the device's default pool so
+// per-call scratch of the binned evaluation is reused, not re-mapped.
+void retain_pool_memory() {
+    static std::atomic<bool> done{false};
+    if (done.exchange(true)) return;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = ~uint64_t{0};
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+}
+
+thread_local std::string g_last_error;
+
+intp_status fail(intp_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+intp_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return INTP_ERR_OUT_OF_MEMORY;
+    return INTP_ERR_CUDA;
+}
+
+#define INTP_CUDA(call, what)                            \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// Bump allocator over one host staging buffer mirrored to one device buffer.
+struct Arena {
+    std::vector<unsigned char> host;
+    size_t add(size_t bytes) {
+        const size_t off = (host.size() + 255) & ~size_t(255);
+        host.resize(off + std::max<size_t>(bytes, 1));
+        return off;
+    }
+    template <class T>
+    size_t put(const std::vector<T>& v) {
+        const size_t off = add(v.size() * sizeof(T));
+        if (!v.empty()) std::memcpy(host.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+struct AxisFactorDev {
+    const double *lower, *upper, *dinv, *bottom, *right;
+    const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
+    const int64_t* scol;
+    const double* sval;
+    int width;
+};
+
+std::vector<float> to_f32(const std::vector<double>& v) {
+    std::vector<float> r(v.size());
+    for (size_t i = 0; i < v.size(); ++i) r[i] = static_cast<float>(v[i]);
+    return r;
+}
+
+}  // namespace
+
+struct intp_table {
+    TableModel model;
+    int precision = INTP_PRECISION_FP64;
+    int refine_steps = 0;
+    int device = 0;
+    void* arena = nullptr;
+    void* ctrl = nullptr;
+    bool has_ctrl = false;
+    TableDev dev{};
+    BinGeom bins{};
+    AxisFactorDev fac[kMaxDim]{};
+    void* scratch = nullptr;  // solve scratch (values staging, refinement buffers)
+    size_t scratch_bytes = 0;
+    double lo_user[kMaxDim]{};  // uniform axes: x_range.first
+
+    ~intp_table() {
+        if (arena) cudaFree(arena);
+        if (ctrl) cudaFree(ctrl);
+        if (scratch) cudaFree(scratch);
+    }
+    bool mixed() const { return precision == INTP_PRECISION_MIXED; }
+    size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
+};
+
+struct intp_bandlu {
+    LineFactor f;
+    void* arena = nullptr;
+    const double *lower = nullptr, *upper = nullptr, *dinv = nullptr, *bottom = nullptr,
+                 *right = nullptr;
+    ~intp_bandlu() {
+        if (arena) cudaFree(arena);
+    }
+};
+
+namespace {
+
+// Per-axis tables used by evaluation and the solve, laid out in one arena.
+intp_status upload_table(intp_table* t) {
+    const TableModel& m = t->model;
+    const int O = m.order;
+    Arena ar;
+    struct Offs {
+        size_t knots, keys, rinv, rinvf, kdf, khi, klo;
+        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, scol, sval;
+    } off[kMaxDim];
+    for (int d = 0; d < m.dim; ++d) {
+        const AxisModel& ax = m.axis[d];
+        const std::vector<double>& t0 = ax.knots;
+        const int64_t nk = static_cast<int64_t>(t0.size());
+        std::vector<long long> keys(nk);
+        std::vector<double> rinv(static_cast<size_t>(nk * std::max(O, 1)), 0.0);
+        std::vector<float> kdf(static_cast<size_t>(nk * (2 * O + 2)), 0.0f), khi(nk), klo(nk);
+        for (int64_t a = 0; a < nk; ++a) {
+            unsigned long long b;
+            std::memcpy(&b, &t0[a], 8);
+            keys[a] = knot_key_bits(b);
+            for (int s = 1; s <= O; ++s)
+                if (a + s < nk && t0[a + s] != t0[a]) rinv[a * O + (s - 1)] = 1.0 / (t0[a + s] - t0[a]);
+            for (int j = -O; j <= O + 1; ++j)
+                if (a + j >= 0 && a + j < nk) kdf[a * (2 * O + 2) + (j + O)] = static_cast<float>(t0[a + j] - t0[a]);
+            const uint32_t hb = split_hi_bits(b);
+            float hf;
+            std::memcpy(&hf, &hb, 4);
+            khi[a] = hf;
+            klo[a] = static_cast<float>(t0[a] - static_cast<double>(hf));
+        }
+        Offs& o = off[d];
+        o.knots = ar.put(t0);
+        o.keys = ar.put(keys);
+        o.rinv = ar.put(rinv);
+        o.rinvf = ar.put(to_f32(rinv));
+        o.kdf = ar.put(kdf);
+        o.khi = ar.put(khi);
+        o.klo = ar.put(klo);
+        const LineFactor& f = ax.factor;
+        o.lower = ar.put(f.lower);
+        o.upper = ar.put(f.upper);
+        o.dinv = ar.put(f.dinv);
+        o.bottom = ar.put(f.bottom);
+        o.right = ar.put(f.right);
+        o.lowerf = ar.put(to_f32(f.lower));
+        o.upperf = ar.put(to_f32(f.upper));
+        o.dinvf = ar.put(to_f32(f.dinv));
+        o.bottomf = ar.put(to_f32(f.bottom));
+        o.rightf = ar.put(to_f32(f.right));
+        o.scol = ar.put(ax.stencil.col);
+        o.sval = ar.put(ax.stencil.val);
+    }
+    INTP_CUDA(cudaMalloc(&t->arena, ar.host.size()), "cudaMalloc(table)");
+    INTP_CUDA(cudaMemcpy(t->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice),
+              "cudaMemcpy(table)");
+    unsigned char* base = static_cast<unsigned char*>(t->arena);
+    TableDev& dv = t->dev;
+    dv.dim = m.dim;
+    dv.order = O;
+    int64_t stride = 1;
+    for (int d = m.dim - 1; d >= 0; --d) {
+        const AxisModel& ax = m.axis[d];
+        AxisDev& a = dv.ax[d];
+        const Offs& o = off[d];
+        a.n = ax.n;
+        a.nknots = static_cast<int64_t>(ax.knots.size());
+        a.stride = stride;
+        stride *= ax.n;
+        a.periodic = ax.periodic ? 1 : 0;
+        a.uniform = ax.uniform ? 1 : 0;
+        a.lo = ax.range_lo;
+        a.hi = ax.range_hi;
+        a.period = ax.range_hi - ax.range_lo;
+        a.ncells = a.nknots - 2 * O - 1;  // spans O .. nknots-O-2
+        a.int_lo = 1;
+        a.int_hi = 0;
+        if (ax.uniform) {
+            const int64_t extra = ax.periodic ? 2 * O + (1 - O % 2) : O + 1;
+            a.hint_x0 = static_cast<float>(t->lo_user[d]);
+            a.hint_inv_dx = static_cast<float>(1.0 / ax.dx);
+            a.hint_off = static_cast<float>(0.5 * static_cast<double>(extra));
+            a.inv_dxf = static_cast<float>(1.0 / ax.dx);
+            // the basis at span c reads knots c-O+1 .. c+O; on a periodic axis
+            // all knots are uniform, on a non-periodic one knots O+1 ..
+            // nknots-O-2 are (the ends are clamped)
+            if (ax.periodic) {
+                a.int_lo = O;
+                a.int_hi = a.nknots - O - 2;
+            } else {
+                a.int_lo = 2 * O;
+                a.int_hi = a.nknots - 2 * O - 2;
+            }
+        }
+        a.knots = reinterpret_cast<const double*>(base + o.knots);
+        a.keys = reinterpret_cast<const long long*>(base + o.keys);
+        a.rinv = reinterpret_cast<const double*>(base + o.rinv);
+        a.rinvf = reinterpret_cast<const float*>(base + o.rinvf);
+        a.kdf = reinterpret_cast<const float*>(base + o.kdf);
+        a.khi = reinterpret_cast<const float*>(base + o.khi);
+        a.klo = reinterpret_cast<const float*>(base + o.klo);
+        AxisFactorDev& fd = t->fac[d];
+        fd.lower = reinterpret_cast<const double*>(base + o.lower);
+        fd.upper = reinterpret_cast<const double*>(base + o.upper);
+        fd.dinv = reinterpret_cast<const double*>(base + o.dinv);
+        fd.bottom = reinterpret_cast<const double*>(base + o.bottom);
+        fd.right = reinterpret_cast<const double*>(base + o.right);
+        fd.lowerf = reinterpret_cast<const float*>(base + o.lowerf);
+        fd.upperf = reinterpret_cast<const float*>(base + o.upperf);
+        fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
+        fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
+        fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
+        fd.scol = reinterpret_cast<const int64_t*>(base + o.scol);
+        fd.sval = reinterpret_cast<const double*>(base + o.sval);
+        fd.width = ax.stencil.width;
+    }
+    INTP_CUDA(cudaMalloc(&t->ctrl, static_cast<size_t>(m.total) * t->elem()), "cudaMalloc(control points)");
+    dv.ctrl = t->ctrl;
+    if (t->mixed() && m.dim <= 3) t->bins = make_bin_geom(dv, kTileBytes);
+    return INTP_OK;
+}
+
+intp_status ensure_scratch(intp_table* t, size_t bytes) {
+    if (t->scratch_bytes >= bytes) return INTP_OK;
+    if (t->scratch) cudaFree(t->scratch);
+    t->scratch = nullptr;
+    t->scratch_bytes = 0;
+    INTP_CUDA(cudaMalloc(&t->scratch, bytes), "cudaMalloc(solve scratch)");
+    t->scratch_bytes = bytes;
+    return INTP_OK;
+}
+
+ShiftDesc shift_desc(const intp_table* t) {
+    ShiftDesc sd{};
+    const TableModel& m = t->model;
+    sd.dim = m.dim;
+    sd.total = m.total;
+    for (int d = 0; d < m.dim; ++d) {
+        sd.n[d] = m.axis[d].n;
+        sd.shift[d] = m.axis[d].periodic ? (m.order / 2) % m.axis[d].n : 0;
+        sd.stride[d] = t->dev.ax[d].stride;
+    }
+    return sd;
+}
+
+struct LineGeom {
+    int64_t n, S, nlines;
+};
+
+LineGeom line_geom(const intp_table* t, int axis) {
+    const TableModel& m = t->model;
+    LineGeom g;
+    g.n = m.axis[axis].n;
+    g.S = t->dev.ax[axis].stride;
+    g.nlines = m.total / g.n;
+    return g;
+}
+
+cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
+    for (int a = t->model.dim - 1; a >= 0; --a) {
+        const LineGeom g = line_geom(t, a);
+        const AxisFactorDev& f = t->fac[a];
+        const LineFactor& lf = t->model.axis[a].factor;
+        cudaError_t e = launch_line_solve_f32(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf,
+                                              f.upperf, f.dinvf, f.bottomf, f.rightf, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
+    for (int a = t->model.dim - 1; a >= 0; --a) {
+        const LineGeom g = line_geom(t, a);
+        const AxisFactorDev& f = t->fac[a];
+        const LineFactor& lf = t->model.axis[a].factor;
+        cudaError_t e = launch_line_solve_f64(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lower,
+                                              f.upper, f.dinv, f.bottom, f.right, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+int auto_refine_steps(const TableModel& m) {
+    // one FP64-residual step brings the FP32 solve from ~kappa * 6e-8 to the
+    // FP32 storage limit; periodic axes of order >= 6 need it most
+    (void)m;
+    return 1;
+}
+
+intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_t s) {
+    const TableModel& m = t->model;
+    const int64_t N = m.total;
+    const ShiftDesc sd = shift_desc(t);
+    if (!t->mixed()) {
+        double* c = static_cast<double*>(t->ctrl);
+        INTP_CUDA(launch_shift_copy_f64_f64(values_dev, c, sd, s), "shift copy");
+        INTP_CUDA(solve_f64_all(t, c, s), "line solve (fp64)");
+        t->has_ctrl = true;
+        return INTP_OK;
+    }
+    float* c = static_cast<float*>(t->ctrl);
+    INTP_CUDA(launch_shift_copy_f64_f32(values_dev, c, sd, s), "shift copy");
+    INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
+    const int steps = t->refine_steps < 0 ? auto_refine_steps(m) : t->refine_steps;
+    if (steps > 0) {
+        // scratch: shifted values (f64), two f64 ping-pong buffers, f32 correction
+        const size_t need = static_cast<size_t>(N) * (8 * 3 + 4) + 1024;
+        intp_status st = ensure_scratch(t, need);
+        if (st != INTP_OK) return st;
+        unsigned char* b = static_cast<unsigned char*>(t->scratch);
+        double* fsh = reinterpret_cast<double*>(b);
+        double* ta = reinterpret_cast<double*>(b + N * 8);
+        double* tb = reinterpret_cast<double*>(b + N * 16);
+        float* corr = reinterpret_cast<float*>(b + N * 24);
+        INTP_CUDA(launch_shift_copy_f64_f64(values_dev, fsh, sd, s), "shift copy");
+        for (int it = 0; it < steps; ++it) {
+            // r = F - (A_0 x ... x A_{D-1}) c, applied one axis at a time in FP64
+            const double* in64 = nullptr;
+            double* outb = ta;
+            for (int a = m.dim - 1; a >= 0; --a) {
+                const LineGeom g = line_geom(t, a);
+                const AxisFactorDev& f = t->fac[a];
+                const double* rhs = (a == 0) ? fsh : nullptr;
+                cudaError_t e = (a == m.dim - 1)
+                                    ? launch_stencil_f32in(c, outb, rhs, g.n, g.S, g.nlines, f.width,
+                                                           f.scol, f.sval, s)
+                                    : launch_stencil_f64in(in64, outb, rhs, g.n, g.S, g.nlines,
+                                                           f.width, f.scol, f.sval, s);
+                if (e != cudaSuccess) return cuda_fail(e, "residual");
+                in64 = outb;
+                outb = (outb == ta) ? tb : ta;
+            }
+            INTP_CUDA(launch_convert_f64_f32(in64, corr, N, s), "residual convert");
+            INTP_CUDA(solve_f32_all(t, corr, s), "line solve (correction)");
+            INTP_CUDA(launch_add_f32(c, corr, N, s), "correction");
+        }
+    }
+    t->has_ctrl = true;
+    return INTP_OK;
+}
+
+bool make_plan(const intp_table* t, const int32_t* derivs, int32_t nderiv, DerivPlan& plan,
+               std::string& err) {
+    std::memset(&plan, 0, sizeof plan);
+    if (!derivs) {
+        plan.k = 1;
+        return true;
+    }
+    if (nderiv < 1 || nderiv > kMaxDeriv) {
+        err = "nderiv must be in [1, 16]";
+        return false;
+    }
+    plan.k = nderiv;
+    for (int k = 0; k < nderiv; ++k)
+        for (int d = 0; d < t->model.dim; ++d) {
+            const int32_t v = derivs[k * t->model.dim + d];
+            if (v < 0) {
+                err = "derivative orders must be non-negative";
+                return false;
+            }
+            // any order above the spline order gives 0 (BSpline.hpp:404-407)
+            plan.ord[k][d] = static_cast<int8_t>(std::min<int32_t>(v, t->model.order + 1));
+        }
+    return true;
+}
+
+}  // namespace
+
+namespace intp_gb300 {
+void note_launch(int count) { g_launches.fetch_add(static_cast<unsigned long long>(count)); }
+}  // namespace intp_gb300
+
+extern "C" {
+
+const char* intp_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t intp_launch_count(void) { return g_launches.load(); }
+
+intp_status intp_table_create(const intp_table_desc* desc, intp_table** out) {
+    if (!desc || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (desc->dim < 1 || desc->dim > INTP_GPU_MAX_DIM)
+        return fail(INTP_ERR_UNSUPPORTED, "dimension must be in [1, 4]");
+    if (desc->order < 0 || desc->order > INTP_GPU_MAX_ORDER)
+        return fail(INTP_ERR_UNSUPPORTED, "order must be in [0, 7]");
+    if (desc->precision != INTP_PRECISION_FP64 && desc->precision != INTP_PRECISION_MIXED)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (desc->refine_steps < -1 || desc->refine_steps > 4)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "refine_steps must be in [-1, 4]");
+    TableSpec spec;
+    spec.dim = desc->dim;
+    spec.order = desc->order;
+    for (int d = 0; d < desc->dim; ++d) {
+        spec.periodic[d] = desc->periodic[d] != 0;
+        spec.size[d] = desc->size[d];
+        spec.lo[d] = desc->range_lo[d];
+        spec.hi[d] = desc->range_hi[d];
+        spec.coords[d] = desc->coords[d];
+    }
+    intp_table* t = new (std::nothrow) intp_table();
+    if (!t) return fail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    std::string err;
+    try {
+        err = build_model(spec, t->model);
+    } catch (const std::bad_alloc&) {
+        delete t;
+        return fail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    }
+    if (!err.empty()) {
+        delete t;
+        return fail(INTP_ERR_INVALID_ARGUMENT, err);
+    }
+    t->precision = desc->precision;
+    t->refine_steps = desc->refine_steps;
+    for (int d = 0; d < desc->dim; ++d) t->lo_user[d] = desc->range_lo[d];
+    cudaGetDevice(&t->device);
+    intp_status st = upload_table(t);
+    if (st != INTP_OK) {
+        delete t;
+        return st;
+    }
+    *out = t;
+    return INTP_OK;
+}
+
+intp_status intp_table_destroy(intp_table* table) {
+    delete table;
+    return INTP_OK;
+}
+
+intp_status intp_table_interpolate(intp_table* t, const double* values, int32_t values_on_device,
+                                   void* stream) {
+    if (!t || !values) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t N = t->model.total;
+    if (values_on_device) return run_interpolate(t, values, s);
+    // host values: stage them on the device first
+    void* stage = nullptr;
+    INTP_CUDA(cudaMallocAsync(&stage, static_cast<size_t>(N) * 8, s), "cudaMallocAsync(values)");
+    cudaError_t e = cudaMemcpyAsync(stage, values, static_cast<size_t>(N) * 8, cudaMemcpyHostToDevice, s);
+    intp_status st = e == cudaSuccess ? run_interpolate(t, static_cast<double*>(stage), s)
+                                      : cuda_fail(e, "cudaMemcpyAsync(values)");
+    cudaFreeAsync(stage, s);
+    return st;
+}
+
+intp_status intp_table_set_control_points(intp_table* t, const double* ctrl) {
+    if (!t || !ctrl) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    const int64_t N = t->model.total;
+    if (t->mixed()) {
+        std::vector<float> f(static_cast<size_t>(N));
+        for (int64_t i = 0; i < N; ++i) f[i] = static_cast<float>(ctrl[i]);
+        INTP_CUDA(cudaMemcpy(t->ctrl, f.data(), N * 4, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
+    } else {
+        INTP_CUDA(cudaMemcpy(t->ctrl, ctrl, N * 8, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
+    }
+    t->has_ctrl = true;
+    return INTP_OK;
+}
+
+intp_status intp_table_get_control_points(const intp_table* t, double* out) {
+    if (!t || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (!t->has_ctrl) return fail(INTP_ERR_STATE, "table has no control points yet");
+    const int64_t N = t->model.total;
+    INTP_CUDA(cudaDeviceSynchronize(), "synchronize");
+    if (t->mixed()) {
+        std::vector<float> f(static_cast<size_t>(N));
+        INTP_CUDA(cudaMemcpy(f.data(), t->ctrl, N * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+        for (int64_t i = 0; i < N; ++i) out[i] = f[i];
+    } else {
+        INTP_CUDA(cudaMemcpy(out, t->ctrl, N * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+    }
+    return INTP_OK;
+}
+
+intp_status intp_table_axis_info(const intp_table* t, int32_t axis, int64_t* nknots, double* lo,
+                                 double* hi, int32_t* periodic, int32_t* uniform) {
+    if (!t) return fail(INTP_ERR_INVALID_ARGUMENT, "null table");
+    if (axis < 0 || axis >= t->model.dim) return fail(INTP_ERR_INVALID_ARGUMENT, "axis out of range");
+    const AxisModel& ax = t->model.axis[axis];
+    if (nknots) *nknots = static_cast<int64_t>(ax.knots.size());
+    if (lo) *lo = ax.range_lo;
+    if (hi) *hi = ax.range_hi;
+    if (periodic) *periodic = ax.periodic ? 1 : 0;
+    if (uniform) *uniform = ax.uniform ? 1 : 0;
+    return INTP_OK;
+}
+
+intp_status intp_table_knots(const intp_table* t, int32_t axis, double* out) {
+    if (!t || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (axis < 0 || axis >= t->model.dim) return fail(INTP_ERR_INVALID_ARGUMENT, "axis out of range");
+    const AxisModel& ax = t->model.axis[axis];
+    std::memcpy(out, ax.knots.data(), ax.knots.size() * sizeof(double));
+    return INTP_OK;
+}
+
+intp_status intp_eval(const intp_table* t, const double* coords, int64_t npts, const int32_t* derivs,
+                      int32_t nderiv, void* out, int32_t out_dtype, void* stream) {
+    if (!t) return fail(INTP_ERR_INVALID_ARGUMENT, "null table");
+    if (npts < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "npts must be >= 0");
+    if (npts > 0 && (!coords || !out)) return fail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    if (!t->has_ctrl) return fail(INTP_ERR_STATE, "table has no control points yet");
+    if (out_dtype != INTP_F64 && out_dtype != INTP_F32)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    DerivPlan plan;
+    std::string err;
+    if (!make_plan(t, derivs, nderiv, plan, err)) return fail(INTP_ERR_INVALID_ARGUMENT, err);
+    const int mode = eval_mode();
+    const bool binned = t->mixed() && t->model.dim <= 3 &&
+                        (mode == 2 || (mode == 0 && npts >= kBinnedMinPoints));
+    if (binned) {
+        retain_pool_memory();
+        INTP_CUDA(run_binned_eval(t->dev, t->bins, coords, npts, plan, out, out_dtype == INTP_F32, eval_chunk(),
+                                  static_cast<cudaStream_t>(stream)),
+                  "binned evaluation");
+        return INTP_OK;
+    }
+    INTP_CUDA(launch_eval_direct(t->dev, t->mixed(), coords, npts, plan, out, out_dtype == INTP_F32,
+                                 static_cast<cudaStream_t>(stream)),
+              "evaluation kernel");
+    return INTP_OK;
+}
+
+intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t npts,
+                           const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
+                           void* stream) {
+    if (!t) return fail(INTP_ERR_INVALID_ARGUMENT, "null table");
+    if (npts < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "npts must be >= 0");
+    if (npts == 0) return INTP_OK;
+    if (!coords || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int K = derivs ? nderiv : 1;
+    const size_t cb = static_cast<size_t>(npts) * t->model.dim * 8;
+    const size_t ob = static_cast<size_t>(npts) * K * (out_dtype == INTP_F32 ? 4 : 8);
+    void *dc = nullptr, *dout = nullptr;
+    INTP_CUDA(cudaMallocAsync(&dc, cb, s), "cudaMallocAsync(coords)");
+    cudaError_t e = cudaMallocAsync(&dout, ob, s);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(dc, s);
+        return cuda_fail(e, "cudaMallocAsync(out)");
+    }
+    intp_status st = INTP_OK;
+    e = cudaMemcpyAsync(dc, coords, cb, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(coords)");
+    if (st == INTP_OK) st = intp_eval(t, static_cast<double*>(dc), npts, derivs, nderiv, dout, out_dtype, stream);
+    if (st == INTP_OK) {
+        e = cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(out)");
+    }
+    cudaFreeAsync(dc, s);
+    cudaFreeAsync(dout, s);
+    e = cudaStreamSynchronize(s);
+    if (st == INTP_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
+    return st;
+}
+
+intp_status intp_check_range(const intp_table* t, const double* coords, int64_t npts, int64_t* first_bad,
+                             void* stream) {
+    if (!t || !first_bad) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *first_bad = -1;
+    if (npts <= 0) return INTP_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned long long* d = nullptr;
+    INTP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), 8, s), "cudaMallocAsync");
+    const unsigned long long init = ~0ULL;
+    intp_status st = INTP_OK;
+    cudaError_t e = cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_range_check(t->dev, coords, npts, d, s);
+    unsigned long long h = ~0ULL;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_fail(e, "range check");
+    if (st == INTP_OK && h != ~0ULL) *first_bad = static_cast<int64_t>(h);
+    return st;
+}
+
+intp_status intp_locate(const intp_table* t, const double* coords, int64_t npts, int64_t* cells,
+                        double* wrapped, void* stream) {
+    if (!t || (npts > 0 && (!coords || !cells))) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    INTP_CUDA(launch_locate(t->dev, coords, npts, cells, wrapped, static_cast<cudaStream_t>(stream)),
+              "locate kernel");
+    return INTP_OK;
+}
+
+intp_status intp_stream_synchronize(void* stream) {
+    INTP_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
+    return INTP_OK;
+}
+
+intp_status intp_bandlu_create(int64_t n, int32_t p, int32_t q, int32_t cyclic, const double* band,
+                               const double* right, const double* bottom, intp_bandlu** out) {
+    if (!out || !band) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (p != q || p < 0 || p > (cyclic ? 3 : 6))
+        return fail(INTP_ERR_UNSUPPORTED, "band widths must satisfy p == q <= 6 (<= 3 cyclic)");
+    if (n < 2 * p + 1) return fail(INTP_ERR_INVALID_ARGUMENT, "matrix too small for its bands");
+    if (cyclic && (!right || !bottom) && p > 0)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "cyclic matrices need the side bands");
+    BandStore m;
+    m.reset(n, p, q, cyclic != 0);
+    std::memcpy(m.band.data(), band, static_cast<size_t>(n * (1 + p + q)) * 8);
+    if (cyclic && p > 0) {
+        std::memcpy(m.right.data(), right, static_cast<size_t>((n - q - 1) * p) * 8);
+        std::memcpy(m.bottom.data(), bottom, static_cast<size_t>((n - p - 1) * q) * 8);
+    }
+    m.factorize();
+    intp_bandlu* lu = new (std::nothrow) intp_bandlu();
+    if (!lu) return fail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    lu->f = line_factor_from(m);
+    Arena ar;
+    const size_t ol = ar.put(lu->f.lower), ou = ar.put(lu->f.upper), od = ar.put(lu->f.dinv),
+                 ob = ar.put(lu->f.bottom), orr = ar.put(lu->f.right);
+    cudaError_t e = cudaMalloc(&lu->arena, ar.host.size());
+    if (e == cudaSuccess) e = cudaMemcpy(lu->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete lu;
+        return cuda_fail(e, "band LU upload");
+    }
+    unsigned char* b = static_cast<unsigned char*>(lu->arena);
+    lu->lower = reinterpret_cast<const double*>(b + ol);
+    lu->upper = reinterpret_cast<const double*>(b + ou);
+    lu->dinv = reinterpret_cast<const double*>(b + od);
+    lu->bottom = reinterpret_cast<const double*>(b + ob);
+    lu->right = reinterpret_cast<const double*>(b + orr);
+    *out = lu;
+    return INTP_OK;
+}
+
+intp_status intp_bandlu_solve(const intp_bandlu* lu, double* x, int64_t outer, int64_t inner,
+                              void* stream) {
+    if (!lu || !x) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (outer < 1 || inner < 1) return fail(INTP_ERR_INVALID_ARGUMENT, "empty tensor");
+    INTP_CUDA(launch_line_solve_f64(x, lu->f.n, inner, outer * inner, lu->f.p, lu->f.q, lu->f.cyclic,
+                                    lu->lower, lu->upper, lu->dinv, lu->bottom, lu->right,
+                                    static_cast<cudaStream_t>(stream)),
+              "band solve");
+    return INTP_OK;
+}
+
+intp_status intp_bandlu_destroy(intp_bandlu* lu) {
+    delete lu;
+    return INTP_OK;
+}
+
+}  // extern "C"

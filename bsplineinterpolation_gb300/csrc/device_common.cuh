@@ -1,0 +1,172 @@
+// Device-side shared definitions: table descriptor, exact knot-span location,
+// and the integer double->float split used by the mixed-precision path.
+//
+// GB300 executes FP64 (and f64<->f32 conversions) at roughly 1/70 of its FP32
+// rate, so the mixed path keeps every per-point FP64 instruction off the
+// critical path: knot spans are found by exact comparisons of order-preserving
+// int64 keys, and local offsets are formed from an exact (hi, lo) split of
+// the coordinate computed with integer operations.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace intp_gb300 {
+
+constexpr int kDevMaxDim = 4;
+constexpr int kDevMaxOrder = 7;
+constexpr int kMaxDeriv = 16;
+
+struct AxisDev {
+    int64_t n;        // control points along the axis
+    int64_t nknots;
+    int64_t stride;   // control-point stride (elements)
+    int32_t periodic;
+    int32_t uniform;
+    double lo, hi, period;   // BSpline::range_ and hi - lo
+    float hint_x0;           // uniform axes: knots[i] ~ hint_x0 + (i - hint_off) / hint_inv_dx
+    float hint_inv_dx;
+    float hint_off;
+    float inv_dxf;           // uniform axes: 1 / dx in FP32
+    int64_t int_lo, int_hi;  // spans whose basis knots are all uniformly spaced
+    int64_t ncells;          // spans an evaluation can land in: [O, O + ncells)
+    const double* knots;     // [nknots]
+    const long long* keys;   // [nknots] order-preserving keys of the knots
+    const double* rinv;      // [nknots * O]  1 / (t[a+s] - t[a]), s = 1..O (0 if equal)
+    const float* rinvf;      // FP32 copy of rinv
+    const float* kdf;        // [nknots * (2O+2)]  t[a+j] - t[a], j = -O..O+1 (FP32)
+    const float* khi;        // [nknots] high FP32 part of the knot (truncated)
+    const float* klo;        // [nknots] remainder t - khi rounded to FP32
+};
+
+struct TableDev {
+    int32_t dim;
+    int32_t order;
+    AxisDev ax[kDevMaxDim];
+    const void* ctrl;        // float (mixed) or double (fp64) control points, row-major
+};
+
+// Spatial buckets of the binned evaluation. Local span index l_d = c_d - O
+// of a query; bucket coordinate l_d >> lb[d] (B_d = 2^lb[d] spans per bucket
+// and axis); tile of control points P_d = B_d + O per axis, row-major with
+// strides tstride[d].
+struct BinGeom {
+    int32_t dim;
+    int32_t lb[kDevMaxDim];
+    int32_t nb[kDevMaxDim];
+    int32_t P[kDevMaxDim];
+    int32_t shift[kDevMaxDim];   // bit offset of l_d & (B_d - 1) in the packed span
+    int32_t tstride[kDevMaxDim];
+    int64_t nbuckets;
+    int32_t tile_elems;
+    int32_t smem_buckets;        // buckets counted in shared memory (0: global atomics)
+};
+
+// Derivative orders of up to kMaxDeriv outputs per point.
+struct DerivPlan {
+    int32_t k;                      // number of outputs
+    int8_t ord[kMaxDeriv][kDevMaxDim];
+};
+
+// Order-preserving integer key of a double: a < b  <=>  key(a) < key(b) for
+// all non-NaN values, with -0 mapped onto +0 (IEEE compares them equal).
+__host__ __device__ __forceinline__ long long knot_key_bits(unsigned long long b) {
+    if (b == 0x8000000000000000ULL) b = 0;
+    const long long s = static_cast<long long>(b);
+    return s ^ ((s >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+
+__device__ __forceinline__ long long knot_key(double x) {
+    return knot_key_bits(static_cast<unsigned long long>(__double_as_longlong(x)));
+}
+
+// High part of x as a float: sign, exponent and the top 23 mantissa bits of the
+// double (truncation). Tiny magnitudes map to 0, huge ones to infinity.
+__host__ __device__ __forceinline__ uint32_t split_hi_bits(unsigned long long b) {
+    const uint32_t hi = static_cast<uint32_t>(b >> 32);
+    const uint32_t sign = hi & 0x80000000u;
+    const int e = static_cast<int>((hi >> 20) & 0x7FFu);
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return sign;
+    if (ef >= 255) return sign | 0x7F800000u;
+    const uint32_t mant = ((hi & 0xFFFFFu) << 3) | (static_cast<uint32_t>(b >> 29) & 7u);
+    return sign | (static_cast<uint32_t>(ef) << 23) | mant;
+}
+
+// Exact split x = hi + lo (lo rounded to FP32) without FP64 instructions.
+__device__ __forceinline__ void split_double(double x, float& hi, float& lo) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const uint32_t hb = split_hi_bits(b);
+    hi = __int_as_float(static_cast<int>(hb));
+    const uint32_t top = static_cast<uint32_t>(b >> 32);
+    const int e = static_cast<int>((top >> 20) & 0x7FFu);
+    const int ef = e - 1023 + 127;
+    // remainder: low 29 mantissa bits of the double (their top 23 kept), worth
+    // rem * 2^(e - 1075); only meaningful when hi is a normal float
+    const uint32_t rem = (static_cast<uint32_t>(b) & 0x1FFFFFFFu) >> 6;
+    const int se = e - 1069 + 127;  // exponent field of 2^(e - 1075 + 6)
+    float scale = 0.0f;
+    if (ef > 0 && ef < 255 && se > 0) scale = __int_as_float(se << 23);
+    // rem < 2^23: exact conversion through the 2^23 magic constant
+    const float remf = __int_as_float(static_cast<int>(0x4B000000u | rem)) - 8388608.0f;
+    const float mag = remf * scale;
+    lo = (top & 0x80000000u) ? -mag : mag;
+}
+
+// Approximate float value of a double, from integer operations only.
+__device__ __forceinline__ float double_to_float_trunc(double x) {
+    return __int_as_float(static_cast<int>(split_hi_bits(
+        static_cast<unsigned long long>(__double_as_longlong(x)))));
+}
+
+// Periodic wrap of BSpline::get_knot_iter (BSpline.hpp:130-136), in FP64 with
+// the reference's exact operation order. Returns the wrapped coordinate.
+__device__ __forceinline__ double periodic_wrap(const AxisDev& a, double x) {
+    const double r = __dadd_rn(__dadd_rn(a.lo, fmod(__dsub_rn(x, a.lo), a.period)),
+                               (x < a.lo ? a.period : 0.0));
+    return r;
+}
+
+// Knot span of BSpline::get_knot_iter (BSpline.hpp:125-157): the largest
+// j in [O+1, last] with t[j] <= x, or O if there is none, where
+// last = nknots - O - 2. Comparisons use exact integer keys. `hint` is any
+// guess; it is verified before it is used.
+__device__ __forceinline__ int64_t locate_span(const AxisDev& a, int order, long long kx,
+                                               int64_t hint) {
+    const int64_t lastc = a.nknots - order - 2;
+    int64_t h = hint < order ? order : (hint > lastc ? lastc : hint);
+    // accept h when t[h] <= x < t[h+1], or at the clamped ends
+    const long long k0 = __ldg(a.keys + h), k1 = __ldg(a.keys + h + 1);
+    const bool lo_ok = (h == order) || (k0 <= kx);
+    const bool hi_ok = (h == lastc) || (kx < k1);
+    if (lo_ok && hi_ok) return h;
+    // one step either way covers an off-by-one hint
+    if (!hi_ok && h + 1 <= lastc) {
+        const long long k2 = (h + 1 == lastc) ? 0 : __ldg(a.keys + h + 2);
+        if (h + 1 == lastc || kx < k2) return h + 1;
+    }
+    if (!lo_ok && h - 1 >= order) {
+        const long long km = __ldg(a.keys + h - 1);
+        if (h - 1 == order || km <= kx) return h - 1;
+    }
+    // binary search: count of knots in [O+1, last] that are <= x
+    int64_t lo = order + 1, hi = lastc + 1;  // search [lo, hi)
+    while (lo < hi) {
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        if (__ldg(a.keys + mid) <= kx)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo - 1;
+}
+
+// FP32 hint of the span on a uniform axis (integer-derived float of x).
+__device__ __forceinline__ int64_t uniform_hint(const AxisDev& a, double x) {
+    const float xf = double_to_float_trunc(x);
+    const float v = floorf((xf - a.hint_x0) * a.hint_inv_dx + a.hint_off);
+    if (!(v > -1.0e18f) || !(v < 1.0e18f)) return v > 0.0f ? a.nknots : 0;
+    return static_cast<int64_t>(v);
+}
+
+}  // namespace intp_gb300

@@ -1,0 +1,59 @@
+// Kernel launchers shared between the CUDA translation units and the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+
+namespace intp_gb300 {
+
+// Counts kernel launches made by the library (reported by intp_launch_count).
+void note_launch(int count = 1);
+
+struct ShiftDesc {
+    int dim;
+    int64_t total;
+    int64_t n[4];
+    int64_t shift[4];
+    int64_t stride[4];
+};
+
+// evaluation (eval_kernels.cu)
+cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coords, int64_t npts,
+                               const DerivPlan& plan, void* out, bool out_f32, cudaStream_t s);
+// Binned evaluation of the mixed form (bin_host.cu); `chunk` queries per round.
+cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
+                            const DerivPlan& plan, void* out, bool out_f32, int64_t chunk, cudaStream_t s);
+// Bucket geometry for a table (tile of at most `tile_bytes` FP32 control points).
+BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes);
+
+cudaError_t launch_locate(const TableDev& t, const double* coords, int64_t npts, int64_t* cells,
+                          double* wrapped, cudaStream_t s);
+cudaError_t launch_range_check(const TableDev& t, const double* coords, int64_t npts,
+                               unsigned long long* first_bad, cudaStream_t s);
+
+// solve (solve_kernels.cu)
+cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
+                                  bool cyclic, const double* lower, const double* upper,
+                                  const double* dinv, const double* bottom, const double* right,
+                                  cudaStream_t s);
+cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
+                                  bool cyclic, const float* lower, const float* upper,
+                                  const float* dinv, const float* bottom, const float* right,
+                                  cudaStream_t s);
+cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
+                                      cudaStream_t s);
+cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const ShiftDesc& sd,
+                                      cudaStream_t s);
+cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs, int64_t n, int64_t S,
+                                 int64_t nlines, int width, const int64_t* col, const double* val,
+                                 cudaStream_t s);
+cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
+                                 int64_t S, int64_t nlines, int width, const int64_t* col,
+                                 const double* val, cudaStream_t s);
+cudaError_t launch_convert_f64_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+cudaError_t launch_add_f32(float* x, const float* d, int64_t n, cudaStream_t s);
+
+}  // namespace intp_gb300

@@ -1,0 +1,332 @@
+// Control-point solve: per-axis band / cyclic-band substitution over every
+// mesh line (InterpolationTemplate.hpp:448-580, BandLU.hpp:120-143 and
+// :215-259), plus the FP64 residual used by mixed-precision refinement.
+//
+// A mesh of shape N_0 x ... x N_{D-1} is processed one axis at a time. Along
+// axis a the lines are indexed by (outer o, inner t): element k of a line is
+// at o*N_a*S + k*S + t with S = prod_{d>a} N_d. One thread owns one line;
+// adjacent threads own adjacent t, so for S >= 32 every step of the
+// substitution is a coalesced warp-wide access. The contiguous axis (S = 1)
+// is staged through shared memory so it is read and written coalesced too.
+// The reference instead rotates the whole tensor after each axis pass
+// (:537-543); solving in place along strided lines needs no rotation.
+//
+// Substitution order follows the reference's push loops restated as pulls:
+// row i of the forward sweep subtracts L(i, i-p) .. L(i, i-1) in that order,
+// the cyclic bottom rows first collect their side-band terms in increasing
+// column order, and row i of the back sweep subtracts the right side band
+// (columns n-1 down to n-p) before the main band (columns i+q down to i+1).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "launch.hpp"
+
+namespace intp_gb300 {
+
+namespace {
+
+int grid_for(int64_t n, int block, int max_blocks) {
+    int64_t g = (n + block - 1) / block;
+    if (g > max_blocks) g = max_blocks;
+    if (g < 1) g = 1;
+    return static_cast<int>(g);
+}
+
+template <class R>
+struct FactorView {
+    int64_t n;
+    const R* lower;   // [n*P]
+    const R* upper;   // [n*Q]
+    const R* dinv;    // [n]
+    const R* bottom;  // [Q*n]
+    const R* right;   // [P*n]
+};
+
+// Accessor of one line: element k at base[k*S].
+template <class R>
+struct StridedLine {
+    R* base;
+    int64_t S;
+    __device__ __forceinline__ R load(int64_t k) const { return base[k * S]; }
+    __device__ __forceinline__ void store(int64_t k, R v) const { base[k * S] = v; }
+};
+
+template <class R, int P, int Q, bool CYC, class Line>
+__device__ __forceinline__ void solve_line(const FactorView<R>& f, const Line& line) {
+    const int64_t n = f.n;
+    // ---- forward: y = L^{-1} x ----
+    R win[P > 0 ? P : 1];  // y_{i-P} .. y_{i-1}
+#pragma unroll
+    for (int k = 0; k < P; ++k) win[k] = 0;
+    R acc[Q > 0 ? Q : 1];  // cyclic: rows n-Q .. n-1 collecting side-band terms
+    if (CYC) {
+#pragma unroll
+        for (int r = 0; r < Q; ++r) acc[r] = line.load(n - Q + r);
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        R v;
+        if (CYC && i >= n - Q) {
+            v = acc[0];
+#pragma unroll
+            for (int r = 1; r < Q; ++r)
+                if (i == n - Q + r) v = acc[r];
+        } else {
+            v = line.load(i);
+        }
+#pragma unroll
+        for (int k = 0; k < P; ++k) v -= __ldg(f.lower + i * P + k) * win[k];
+        if (CYC && i < n - P - 1) {
+#pragma unroll
+            for (int r = 0; r < Q; ++r) acc[r] -= __ldg(f.bottom + r * n + i) * v;
+        }
+        line.store(i, v);
+#pragma unroll
+        for (int k = 0; k + 1 < P; ++k) win[k] = win[k + 1];
+        if (P > 0) win[P - 1] = v;
+    }
+    // ---- back: x = U^{-1} y ----
+    R zw[Q > 0 ? Q : 1];  // z_{i+1} .. z_{i+Q}
+#pragma unroll
+    for (int k = 0; k < Q; ++k) zw[k] = 0;
+    R tail[P > 0 ? P : 1];  // cyclic: z_{n-P} .. z_{n-1}
+#pragma unroll
+    for (int k = 0; k < P; ++k) tail[k] = 0;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        R v = line.load(i);
+        if (CYC) {
+#pragma unroll
+            for (int r = P - 1; r >= 0; --r)
+                if (n - P + r > i + Q) v -= __ldg(f.right + r * n + i) * tail[r];
+        }
+#pragma unroll
+        for (int k = Q - 1; k >= 0; --k) v -= __ldg(f.upper + i * Q + k) * zw[k];
+        v *= __ldg(f.dinv + i);
+        line.store(i, v);
+        if (CYC) {
+#pragma unroll
+            for (int r = 0; r < P; ++r)
+                if (i == n - P + r) tail[r] = v;
+        }
+#pragma unroll
+        for (int k = Q - 1; k > 0; --k) zw[k] = zw[k - 1];
+        if (Q > 0) zw[0] = v;
+    }
+}
+
+template <class R, int P, int Q, bool CYC>
+__global__ void __launch_bounds__(128) solve_strided_kernel(R* __restrict__ x, int64_t n, int64_t S,
+                                                            int64_t nlines, FactorView<R> f) {
+    for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
+         l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t o = l / S, t = l - o * S;
+        StridedLine<R> line{x + o * n * S + t, S};
+        solve_line<R, P, Q, CYC>(f, line);
+    }
+}
+
+// Contiguous lines (S = 1): a block stages 32 lines x n into shared memory
+// (row pitch n+1, conflict-free per-lane access), solves, writes back.
+template <class R>
+struct SmemLine {
+    R* base;
+    __device__ __forceinline__ R load(int64_t k) const { return base[k]; }
+    __device__ __forceinline__ void store(int64_t k, R v) const { base[k] = v; }
+};
+
+template <class R, int P, int Q, bool CYC>
+__global__ void __launch_bounds__(32) solve_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
+                                                          FactorView<R> f) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* tile = reinterpret_cast<R*>(smem_raw);
+    const int64_t pitch = n + 1;
+    const int lane = threadIdx.x;
+    for (int64_t l0 = blockIdx.x * 32LL; l0 < nlines; l0 += gridDim.x * 32LL) {
+        const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
+        const R* src = x + l0 * n;
+        for (int r = 0; r < rows; ++r)
+            for (int64_t k = lane; k < n; k += 32) tile[r * pitch + k] = src[r * n + k];
+        __syncwarp();
+        if (lane < rows) solve_line<R, P, Q, CYC>(f, SmemLine<R>{tile + lane * pitch});
+        __syncwarp();
+        R* dst = x + l0 * n;
+        for (int r = 0; r < rows; ++r)
+            for (int64_t k = lane; k < n; k += 32) dst[r * n + k] = tile[r * pitch + k];
+        __syncwarp();
+    }
+}
+
+template <class R, int P, int Q, bool CYC>
+cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
+                            cudaStream_t s) {
+    const size_t smem = static_cast<size_t>(32) * static_cast<size_t>(n + 1) * sizeof(R);
+    if (S == 1 && smem <= 96 * 1024) {
+        auto k = solve_contig_kernel<R, P, Q, CYC>;
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+        const int grid = grid_for(nlines, 32, 152 * 64);
+        k<<<grid, 32, smem, s>>>(x, n, nlines, f);
+        note_launch();
+        return cudaGetLastError();
+    }
+    const int grid = grid_for(nlines, 128, 152 * 64);
+    solve_strided_kernel<R, P, Q, CYC><<<grid, 128, 0, s>>>(x, n, S, nlines, f);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_solve_r(R* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                           const FactorView<R>& f, cudaStream_t s) {
+    if (p != q) return cudaErrorInvalidValue;
+    if (cyclic) {
+        switch (p) {
+            case 0: return launch_solve_pq<R, 0, 0, true>(x, n, S, nlines, f, s);
+            case 1: return launch_solve_pq<R, 1, 1, true>(x, n, S, nlines, f, s);
+            case 2: return launch_solve_pq<R, 2, 2, true>(x, n, S, nlines, f, s);
+            case 3: return launch_solve_pq<R, 3, 3, true>(x, n, S, nlines, f, s);
+        }
+        return cudaErrorInvalidValue;
+    }
+    switch (p) {
+        case 0: return launch_solve_pq<R, 0, 0, false>(x, n, S, nlines, f, s);
+        case 1: return launch_solve_pq<R, 1, 1, false>(x, n, S, nlines, f, s);
+        case 2: return launch_solve_pq<R, 2, 2, false>(x, n, S, nlines, f, s);
+        case 3: return launch_solve_pq<R, 3, 3, false>(x, n, S, nlines, f, s);
+        case 4: return launch_solve_pq<R, 4, 4, false>(x, n, S, nlines, f, s);
+        case 5: return launch_solve_pq<R, 5, 5, false>(x, n, S, nlines, f, s);
+        case 6: return launch_solve_pq<R, 6, 6, false>(x, n, S, nlines, f, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---- data movement and residual kernels ----
+
+// dst[shift(i)] = (To) src[i]: periodic axes move index i to (i + O/2) mod n
+// (InterpolationTemplate.hpp:451-462).
+template <class Ti, class To>
+__global__ void shift_copy_kernel(const Ti* __restrict__ src, To* __restrict__ dst, ShiftDesc sd) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < sd.total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t r = i, o = 0;
+#pragma unroll
+        for (int d = 3; d >= 0; --d) {
+            if (d < sd.dim) {
+                const int64_t n = sd.n[d];
+                const int64_t q = r / n;
+                int64_t idx = r - q * n;
+                r = q;
+                if (sd.shift[d]) {
+                    idx += sd.shift[d];
+                    if (idx >= n) idx -= n;
+                }
+                o += idx * sd.stride[d];
+            }
+        }
+        dst[o] = static_cast<To>(src[i]);
+    }
+}
+
+// out(line) = A_a in(line) along axis a (FP64 arithmetic), optionally
+// out = rhs - A in for the last pass of a residual.
+template <class Ti>
+__global__ void __launch_bounds__(128) stencil_kernel(const Ti* __restrict__ in, double* __restrict__ out,
+                                                      const double* __restrict__ rhs, int64_t n,
+                                                      int64_t S, int64_t nlines, int width,
+                                                      const int64_t* __restrict__ col,
+                                                      const double* __restrict__ val) {
+    for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
+         l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t o = l / S, t = l - o * S;
+        const int64_t base = o * n * S + t;
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int w = 0; w < width; ++w) {
+                const double a = __ldg(val + i * width + w);
+                const int64_t j = __ldg(col + i * width + w);
+                acc = fma(a, static_cast<double>(in[base + j * S]), acc);
+            }
+            out[base + i * S] = rhs ? rhs[base + i * S] - acc : acc;
+        }
+    }
+}
+
+template <class Ti, class To>
+__global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = static_cast<To>(in[i]);
+}
+
+__global__ void add_kernel(float* __restrict__ x, const float* __restrict__ d, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        x[i] += d[i];
+}
+
+}  // namespace
+
+cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
+                                  bool cyclic, const double* lower, const double* upper,
+                                  const double* dinv, const double* bottom, const double* right,
+                                  cudaStream_t s) {
+    FactorView<double> f{n, lower, upper, dinv, bottom, right};
+    return launch_solve_r<double>(x, n, S, nlines, p, q, cyclic, f, s);
+}
+
+cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
+                                  bool cyclic, const float* lower, const float* upper,
+                                  const float* dinv, const float* bottom, const float* right,
+                                  cudaStream_t s) {
+    FactorView<float> f{n, lower, upper, dinv, bottom, right};
+    return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
+}
+
+cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
+                                      cudaStream_t s) {
+    shift_copy_kernel<double, double><<<grid_for(sd.total, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const ShiftDesc& sd,
+                                      cudaStream_t s) {
+    shift_copy_kernel<double, float><<<grid_for(sd.total, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs, int64_t n, int64_t S,
+                                 int64_t nlines, int width, const int64_t* col, const double* val,
+                                 cudaStream_t s) {
+    stencil_kernel<float><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
+                                                                        width, col, val);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
+                                 int64_t S, int64_t nlines, int width, const int64_t* col,
+                                 const double* val, cudaStream_t s) {
+    stencil_kernel<double><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
+                                                                         width, col, val);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_f64_f32(const double* in, float* out, int64_t n, cudaStream_t s) {
+    convert_kernel<double, float><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(in, out, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_f32(float* x, const float* d, int64_t n, cudaStream_t s) {
+    add_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(x, d, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace intp_gb300

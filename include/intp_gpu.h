@@ -1,0 +1,163 @@
+/*
+ * intp_gpu.h -- C ABI of the GB300-native B-spline interpolation library.
+ *
+ * Plain pointers and sizes only. Every call returns an intp_status; on failure
+ * intp_last_error() describes the cause (thread-local). Device pointers are
+ * CUDA global-memory pointers on the table's device; `stream` is a
+ * cudaStream_t passed as void* (NULL = the default stream).
+ *
+ * The entry points replace the hot path of the header-only C++ reference
+ * library 12ff54e/BSplineInterpolation (src/include/). Each declaration names
+ * the reference interface it stands in for. Semantics are those of the
+ * reference built with INTP_PERIODIC_NO_DUMMY_POINT: a periodic axis of n
+ * samples has n control points and one period spans its range.
+ */
+#ifndef INTP_GPU_H
+#define INTP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define INTP_GPU_MAX_DIM 4
+#define INTP_GPU_MAX_ORDER 7
+#define INTP_GPU_MAX_DERIV 16
+
+typedef enum intp_status {
+    INTP_OK = 0,
+    INTP_ERR_INVALID_ARGUMENT = 1, /* reference: INTP_ASSERT -> std::runtime_error */
+    INTP_ERR_DOMAIN = 2,           /* reference: std::domain_error (range check) */
+    INTP_ERR_OUT_OF_MEMORY = 3,    /* reference: std::bad_alloc */
+    INTP_ERR_CUDA = 4,             /* CUDA runtime failure */
+    INTP_ERR_STATE = 5,            /* e.g. evaluation before control points exist */
+    INTP_ERR_UNSUPPORTED = 6,      /* dimension / order outside the compiled set */
+    INTP_ERR_TIMEOUT = 7,          /* a bounded wait ran out */
+    INTP_ERR_BUDGET = 8            /* serving: request exceeds the memory budget */
+} intp_status;
+
+typedef enum intp_precision {
+    INTP_PRECISION_FP64 = 0,  /* FP64 end to end (parity form) */
+    INTP_PRECISION_MIXED = 1  /* FP32 solve + refinement, FP32 basis/contraction */
+} intp_precision;
+
+typedef enum intp_dtype { INTP_F64 = 0, INTP_F32 = 1 } intp_dtype;
+
+typedef struct intp_table intp_table;
+typedef struct intp_bandlu intp_bandlu;
+
+/* Description of one interpolation table (one InterpolationFunction). */
+typedef struct intp_table_desc {
+    int32_t dim;           /* 1..INTP_GPU_MAX_DIM */
+    int32_t order;         /* 0..INTP_GPU_MAX_ORDER */
+    int32_t precision;     /* intp_precision */
+    int32_t refine_steps;  /* mixed only: -1 = automatic, else 0..4 */
+    int32_t periodic[INTP_GPU_MAX_DIM];
+    int64_t size[INTP_GPU_MAX_DIM];     /* samples per axis (mesh dim sizes) */
+    double range_lo[INTP_GPU_MAX_DIM];  /* uniform axis: x_min */
+    double range_hi[INTP_GPU_MAX_DIM];  /* uniform axis: x_max */
+    /* non-uniform axis: host array of size[d] (+1 if periodic) increasing
+     * sample coordinates; NULL for a uniform axis */
+    const double* coords[INTP_GPU_MAX_DIM];
+} intp_table_desc;
+
+/* Knot vectors, collocation matrices and their band LU factors, uploaded to
+ * the current device.
+ * Replaces: InterpolationFunctionTemplate::InterpolationFunctionTemplate
+ * (src/include/InterpolationTemplate.hpp:60-79), which builds the knots
+ * (src/include/Interpolation.hpp:322-464) and factors every axis
+ * (InterpolationTemplate.hpp:254-446). */
+intp_status intp_table_create(const intp_table_desc* desc, intp_table** out);
+
+/* Releases the table and its device memory. Replaces the destructor of
+ * InterpolationFunction / InterpolationFunctionTemplate. */
+intp_status intp_table_destroy(intp_table* table);
+
+/* Solves for control points from a row-major value mesh of prod(size)
+ * doubles (host or device memory).
+ * Replaces: InterpolationFunctionTemplate::interpolate
+ * (InterpolationTemplate.hpp:118-143) -> solve_for_control_points_ (:448-580). */
+intp_status intp_table_interpolate(intp_table* table, const double* values,
+                                   int32_t values_on_device, void* stream);
+
+/* Loads / reads control points (row-major, prod(size) doubles, host memory).
+ * Replaces: BSpline::load_ctrlPts (src/include/BSpline.hpp:230-242) and
+ * BSpline::control_points (BSpline.hpp:575-577, plain layout). */
+intp_status intp_table_set_control_points(intp_table* table, const double* ctrl_host);
+intp_status intp_table_get_control_points(const intp_table* table, double* ctrl_host);
+
+/* Axis properties. Replaces InterpolationFunction::periodicity / uniform /
+ * range (Interpolation.hpp:248-258) and BSpline::knots_num (BSpline.hpp:592). */
+intp_status intp_table_axis_info(const intp_table* table, int32_t axis, int64_t* nknots,
+                                 double* range_lo, double* range_hi, int32_t* periodic,
+                                 int32_t* uniform);
+/* Copies the knot vector of one axis to host memory.
+ * Replaces BSpline::knots_begin/knots_end (BSpline.hpp:560-571). */
+intp_status intp_table_knots(const intp_table* table, int32_t axis, double* knots_host);
+
+/* Batched evaluation at npts points (coords: npts x dim doubles, row-major,
+ * device memory). derivs: nderiv x dim derivative orders (host memory), or
+ * NULL for the value only (nderiv ignored, one output). out: npts x nderiv
+ * values of out_dtype (device memory), row-major.
+ * Replaces: InterpolationFunction::operator() (Interpolation.hpp:132-146) and
+ * InterpolationFunction::derivative (Interpolation.hpp:177-205), i.e.
+ * BSpline::operator() (BSpline.hpp:305-368) and BSpline::derivative_at
+ * (BSpline.hpp:393-532), one call for many points. Out-of-range points on a
+ * non-periodic axis extrapolate, as operator() does. */
+intp_status intp_eval(const intp_table* table, const double* coords, int64_t npts,
+                      const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
+                      void* stream);
+
+/* As intp_eval with host buffers: the coordinates are copied to the device,
+ * evaluated, and the results copied back before the call returns. */
+intp_status intp_eval_host(const intp_table* table, const double* coords_host, int64_t npts,
+                           const int32_t* derivs, int32_t nderiv, void* out_host,
+                           int32_t out_dtype, void* stream);
+
+/* Range check of InterpolationFunction::at / derivative_at
+ * (Interpolation.hpp:153-169, :213-244, boundary_check_ :482-491) for a batch
+ * of device coordinates: *first_bad = index of the first point outside the
+ * range of a non-periodic axis, or -1. */
+intp_status intp_check_range(const intp_table* table, const double* coords, int64_t npts,
+                             int64_t* first_bad, void* stream);
+
+/* Knot-span index per point and axis (npts x dim int64, device memory) and the
+ * periodic-wrapped coordinate (npts x dim doubles, device memory, may be NULL).
+ * Replaces BSpline::get_knot_iter (BSpline.hpp:125-157). */
+intp_status intp_locate(const intp_table* table, const double* coords, int64_t npts,
+                        int64_t* cells, double* wrapped, void* stream);
+
+/* Waits for `stream`. */
+intp_status intp_stream_synchronize(void* stream);
+
+/* Description of the last failure on the calling thread. */
+const char* intp_last_error(void);
+
+/* Number of CUDA kernels the library has launched in this process
+ * (diagnostic; no counterpart in the reference). */
+uint64_t intp_launch_count(void);
+
+/* ---- standalone band LU (BandLU.hpp) ---- */
+
+/* Factors an n x n band matrix given in the reference's storage: band is
+ * n x (1+p+q) with A(i,j) = band[j*(1+p+q) + (i+q-j)]; cyclic matrices add
+ * right ((n-q-1) x p, R(i, j+p-n)) and bottom ((n-p-1) x q, S(j, i+q-n))
+ * corner blocks (NULL when cyclic == 0). Only p == q is supported.
+ * Replaces: BandLU<BandMatrix>::compute (src/include/BandLU.hpp:31-41,
+ * :103-118) and BandLU<ExtendedBandMatrix>::compute (:159-213). */
+intp_status intp_bandlu_create(int64_t n, int32_t p, int32_t q, int32_t cyclic, const double* band,
+                               const double* right, const double* bottom, intp_bandlu** out);
+/* Solves in place along the middle axis of an (outer, n, inner) row-major
+ * tensor of doubles in device memory.
+ * Replaces: BandLU::solve_in_place (BandLU.hpp:51-54, :120-143, :215-259). */
+intp_status intp_bandlu_solve(const intp_bandlu* lu, double* x, int64_t outer, int64_t inner,
+                              void* stream);
+intp_status intp_bandlu_destroy(intp_bandlu* lu);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* INTP_GPU_H */

@@ -1,0 +1,65 @@
+"""The C-ABI library loads without a GPU and exports every function that
+include/intp_gpu.h declares; calls that need no device fail cleanly."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "intp_gpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(intp_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from bsplineinterpolation_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header(lib):
+    from bsplineinterpolation_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_invalid_arguments_fail_cleanly(lib):
+    from bsplineinterpolation_gb300 import _lib
+    h = C.c_void_p()
+    assert lib.intp_table_create(None, C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    d = _lib.TableDesc()
+    d.dim = 5
+    assert lib.intp_table_create(C.byref(d), C.byref(h)) == _lib.ERR_UNSUPPORTED
+    d.dim, d.order = 2, 9
+    assert lib.intp_table_create(C.byref(d), C.byref(h)) == _lib.ERR_UNSUPPORTED
+    d.order = 3
+    d.size[0] = d.size[1] = 8
+    d.range_lo[0], d.range_hi[0] = 1.0, 0.0  # decreasing range
+    d.range_lo[1], d.range_hi[1] = 0.0, 1.0
+    assert lib.intp_table_create(C.byref(d), C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert b"increasing" in lib.intp_last_error()
+    assert lib.intp_eval(None, None, 0, None, 0, None, 0, None) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.intp_launch_count() == 0
+
+
+def test_product_never_loads_the_oracle():
+    """The package imports nothing from oracle/ (it is test infrastructure)."""
+    pkg = os.path.join(REPO, "bsplineinterpolation_gb300")
+    for root, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".hpp", ".h")):
+                text = open(os.path.join(root, f), errors="replace").read()
+                assert "oracle" not in text.lower(), f
