@@ -226,6 +226,22 @@ def profile_traffic():
     return None
 
 
+def make_reduce_max(dist, torch, device):
+    """Max over ranks of a float (all-reduce on `device`)."""
+    def reduce_max(v):
+        t = torch.tensor([float(v)], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return reduce_max
+
+
+def replica_throughput(local_ms, pts_per_rank, steps, world, reduce_max=None):
+    """Whole-job points/s of `world` independent replicas: every rank's points
+    over the slowest rank's time. Returns (value, max_ms)."""
+    t_max = reduce_max(local_ms) if reduce_max else float(local_ms)
+    return pts_per_rank * world * steps / (t_max / 1e3), t_max
+
+
 def run_ours(args, rank, world):
     import torch
     import bsplineinterpolation_gb300 as bi
@@ -281,12 +297,8 @@ def run_ours(args, rank, world):
     clocks.start()
     total_ms, solve_ms, eval_ms, wall, launches = timed_steps(f, args.steps, args.warmup, out)
     clock_info = clocks.stop()
-    t_max = total_ms
-    if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = npts * world * args.steps / (t_max / 1e3)
+    value, t_max = replica_throughput(total_ms, npts, args.steps, world,
+                                      make_reduce_max(dist, torch, "cuda") if dist else None)
     result = {
         "metric": METRIC,
         "value": value,

@@ -9,46 +9,96 @@
 
 namespace intp_gb300 {
 
-cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t*, const uint32_t*,
+cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
                                 const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*,
                                 bool, int, cudaStream_t);
-cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t*, const uint32_t*,
-                                const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*,
-                                bool, int, cudaStream_t);
+cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
+                               const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*,
+                               bool, int, cudaStream_t);
 
 namespace bin_detail {
 
-// Exclusive scan of counts into offsets[0..nb] and cursor[0..nb) (one block).
-__global__ void __launch_bounds__(1024) scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
-                                                    uint32_t* __restrict__ cursor, int64_t nb) {
-    __shared__ uint32_t partial[1024];
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* sh, uint32_t& total) {
     const int tid = threadIdx.x;
-    const int64_t per = (nb + 1023) / 1024;
-    const int64_t b0 = tid * per, b1 = (b0 + per < nb) ? b0 + per : nb;
-    uint32_t s = 0;
-    for (int64_t b = b0; b < b1; ++b) s += counts[b];
-    partial[tid] = s;
+    sh[tid] = v;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t v = tid >= off ? partial[tid - off] : 0u;
+    for (int off = 1; off < kScanThreads; off <<= 1) {
+        const uint32_t a = tid >= off ? sh[tid - off] : 0u;
         __syncthreads();
-        partial[tid] += v;
+        sh[tid] += a;
         __syncthreads();
     }
-    uint32_t run = tid == 0 ? 0u : partial[tid - 1];
-    for (int64_t b = b0; b < b1; ++b) {
-        offsets[b] = run;
-        cursor[b] = run;
-        run += counts[b];
+    total = sh[kScanThreads - 1];
+    const uint32_t r = sh[tid] - v;
+    __syncthreads();
+    return r;
+}
+
+// per-tile sums of x[0..n)
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t* __restrict__ x, int64_t n,
+                                                                   uint32_t* __restrict__ tile_sum) {
+    __shared__ uint32_t sh[kScanThreads];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) s += x[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, sh, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// exclusive scan of the tile sums in place (one block; ntiles <= 4096)
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(uint32_t* __restrict__ tile_sum, int64_t ntiles) {
+    __shared__ uint32_t sh[kScanThreads];
+    const int64_t base = threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < ntiles ? tile_sum[base + k] : 0u;
+        s += v[k];
     }
-    if (tid == 1023) offsets[nb] = partial[1023];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, sh, total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < ntiles) {
+            tile_sum[base + k] = run;
+            run += v[k];
+        }
+}
+
+// exclusive scan of x into y, each tile offset by its scanned tile sum
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t* __restrict__ x, int64_t n,
+                                                                  const uint32_t* __restrict__ tile_sum,
+                                                                  uint32_t* __restrict__ y) {
+    __shared__ uint32_t sh[kScanThreads];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? x[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, sh, total) + tile_sum[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) {
+            y[base + k] = run;
+            run += v[k];
+        }
 }
 
 }  // namespace bin_detail
 
 namespace {
 
-constexpr int32_t kSmemBucketLimit = 6144;
+constexpr int32_t kSmemBucketLimit = 48 * 1024;
 
 int sm_count() {
     static int n = 0;
@@ -61,19 +111,31 @@ int sm_count() {
 }
 
 template <int D>
-cudaError_t launch_hist_scatter(const TableDev& t, const BinGeom& g, const double* coords, int64_t n,
-                                uint32_t* counts, uint32_t* offsets, uint32_t* cursor, uint32_t* ridx,
-                                uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s) {
+cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
+                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* ridx,
+                        uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s) {
     using namespace bin_detail;
-    const int grid = sm_count() * 8;
-    cudaError_t e = cudaMemsetAsync(counts, 0, static_cast<size_t>(g.nbuckets) * 4, s);
-    if (e != cudaSuccess) return e;
-    const size_t sm_h = g.smem_buckets > 0 ? static_cast<size_t>(g.smem_buckets) * 4 : 0;
-    hist_kernel<D><<<grid, kBinThreads, sm_h, s>>>(t, g, coords, n, counts);
+    const int64_t slice = (n + nblk - 1) / nblk;
+    const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
+    auto kc = count_kernel<D>;
+    auto ks = scatter_kernel<D>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    kc<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkcount);
     note_launch();
-    scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, cursor, g.nbuckets);
+    const int64_t m = g.nbuckets * nblk;
+    const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
+    scan_reduce_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum);
     note_launch();
-    scatter_kernel<D><<<grid, kBinThreads, sm_h * 2, s>>>(t, g, coords, n, cursor, ridx, rcell, ru, cap);
+    scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(tile_sum, ntiles);
+    note_launch();
+    scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
+    note_launch();
+    ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, ridx, rcell, ru, cap);
     note_launch();
     return cudaGetLastError();
 }
@@ -81,41 +143,24 @@ cudaError_t launch_hist_scatter(const TableDev& t, const BinGeom& g, const doubl
 }  // namespace
 
 BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
+    (void)tile_bytes;
     BinGeom g{};
     const int D = t.dim, O = t.order;
     g.dim = D;
-    int lb[kDevMaxDim] = {0, 0, 0, 0};
-    auto tile = [&](const int* l) {
-        int64_t e = 1;
-        for (int d = 0; d < D; ++d) e *= (int64_t{1} << l[d]) + O;
-        return e * 4;
-    };
-    for (bool grew = true; grew;) {
-        grew = false;
-        for (int d = D - 1; d >= 0; --d) {
-            if ((int64_t{1} << lb[d]) >= t.ax[d].ncells || lb[d] >= 12) continue;
-            int trial[kDevMaxDim];
-            std::copy(lb, lb + kDevMaxDim, trial);
-            ++trial[d];
-            if (tile(trial) <= tile_bytes) {
-                lb[d] = trial[d];
-                grew = true;
-            }
-        }
-    }
     int shift = 0;
     g.nbuckets = 1;
     int32_t stride = 1;
     for (int d = D - 1; d >= 0; --d) {
-        g.lb[d] = lb[d];
-        g.P[d] = (1 << lb[d]) + O;
-        g.nb[d] = static_cast<int32_t>((t.ax[d].ncells + (int64_t{1} << lb[d]) - 1) >> lb[d]);
+        const int lb = bucket_log2(D, d);
+        g.lb[d] = lb;
+        g.P[d] = (1 << lb) + O;
+        g.nb[d] = static_cast<int32_t>((t.ax[d].ncells + (int64_t{1} << lb) - 1) >> lb);
         g.tstride[d] = stride;
         stride *= g.P[d];
     }
     for (int d = 0; d < D; ++d) {
         g.shift[d] = shift;
-        shift += lb[d];
+        shift += g.lb[d];
         g.nbuckets *= g.nb[d];
     }
     g.tile_elems = stride;
@@ -129,26 +174,28 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
     const int64_t cap = std::min<int64_t>(chunk, npts);
-    const int64_t nb = g.nbuckets;
-    // scratch: counts, cursor [nb], offsets [nb+1], records [cap] x (8 + 4D) bytes
-    const size_t b_cnt = static_cast<size_t>(nb) * 4, b_off = static_cast<size_t>(nb + 1) * 4;
+    const int nblk = sm_count() * 2;  // count/scatter CTAs of kSortThreads
+    const int64_t m = g.nbuckets * nblk;
+    const int64_t ntiles = (m + bin_detail::kScanTile - 1) / bin_detail::kScanTile;
+    if (ntiles > bin_detail::kScanThreads * bin_detail::kScanItems) return cudaErrorInvalidValue;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
-    const size_t total = up(b_cnt) * 2 + up(b_off) + up(static_cast<size_t>(cap) * 4) * 2 +
-                         up(static_cast<size_t>(cap) * 4 * D);
+    const size_t b_m = up(static_cast<size_t>(m) * 4), b_t = up(static_cast<size_t>(ntiles) * 4);
+    const size_t b_r = up(static_cast<size_t>(cap) * 4);
+    const size_t total = b_m * 2 + b_t + b_r * (2 + D);
     void* mem = nullptr;
     cudaError_t e = cudaMallocAsync(&mem, total, s);
     if (e != cudaSuccess) return e;
     unsigned char* p = static_cast<unsigned char*>(mem);
-    uint32_t* counts = reinterpret_cast<uint32_t*>(p);
-    p += up(b_cnt);
-    uint32_t* cursor = reinterpret_cast<uint32_t*>(p);
-    p += up(b_cnt);
-    uint32_t* offsets = reinterpret_cast<uint32_t*>(p);
-    p += up(b_off);
+    uint32_t* blkcount = reinterpret_cast<uint32_t*>(p);
+    p += b_m;
+    uint32_t* blkoffset = reinterpret_cast<uint32_t*>(p);
+    p += b_m;
+    uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
+    p += b_t;
     uint32_t* ridx = reinterpret_cast<uint32_t*>(p);
-    p += up(static_cast<size_t>(cap) * 4);
+    p += b_r;
     uint32_t* rcell = reinterpret_cast<uint32_t*>(p);
-    p += up(static_cast<size_t>(cap) * 4);
+    p += b_r;
     float* ru = reinterpret_cast<float*>(p);
     const int K = plan.k;
     const size_t ob = out_f32 ? 4 : 8;
@@ -157,15 +204,15 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
         const int64_t n = std::min(cap, npts - p0);
         const double* c = coords + p0 * D;
         switch (D) {
-            case 1: e = launch_hist_scatter<1>(t, g, c, n, counts, offsets, cursor, ridx, rcell, ru, cap, s); break;
-            case 2: e = launch_hist_scatter<2>(t, g, c, n, counts, offsets, cursor, ridx, rcell, ru, cap, s); break;
-            case 3: e = launch_hist_scatter<3>(t, g, c, n, counts, offsets, cursor, ridx, rcell, ru, cap, s); break;
+            case 1: e = launch_sort<1>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
+            case 2: e = launch_sort<2>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
+            case 3: e = launch_sort<3>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
             default: e = cudaErrorInvalidValue;
         }
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
-        e = D <= 2 ? launch_bin_eval_d12(t, g, offsets, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s)
-                   : launch_bin_eval_d3(t, g, offsets, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s);
+        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s)
+                   : launch_bin_eval_d3(t, g, blkoffset, nblk, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s);
     }
     cudaError_t e2 = cudaFreeAsync(mem, s);
     return e != cudaSuccess ? e : e2;

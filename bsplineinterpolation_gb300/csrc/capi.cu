@@ -325,10 +325,16 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
 }
 
 int auto_refine_steps(const TableModel& m) {
-    // one FP64-residual step brings the FP32 solve from ~kappa * 6e-8 to the
-    // FP32 storage limit; periodic axes of order >= 6 need it most
-    (void)m;
-    return 1;
+    // The FP32 solve's relative error is about 6e-8 * sum_d kappa_d (kappa ~ 3
+    // per axis for cubic collocation, tens for periodic order >= 6). Each
+    // FP64-residual step squares that relative error, down to FP32 storage.
+    double e = fp32_solve_error_estimate(m);
+    int steps = 0;
+    while (e > 1e-6 && steps < 4) {
+        e = e * e + 6e-8;
+        ++steps;
+    }
+    return steps;
 }
 
 intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_t s) {
@@ -383,11 +389,27 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
     return INTP_OK;
 }
 
+// Groups outputs by their derivative orders on axes 1..D-1.
+void group_plan(DerivPlan& plan, int dim) {
+    plan.ngroups = 0;
+    for (int k = 0; k < plan.k; ++k) {
+        int g = 0;
+        for (; g < plan.ngroups; ++g) {
+            bool same = true;
+            for (int d = 1; d < dim; ++d) same = same && plan.ord[plan.group_rep[g]][d] == plan.ord[k][d];
+            if (same) break;
+        }
+        if (g == plan.ngroups) plan.group_rep[plan.ngroups++] = static_cast<int8_t>(k);
+        plan.out_group[k] = static_cast<int8_t>(g);
+    }
+}
+
 bool make_plan(const intp_table* t, const int32_t* derivs, int32_t nderiv, DerivPlan& plan,
                std::string& err) {
     std::memset(&plan, 0, sizeof plan);
     if (!derivs) {
         plan.k = 1;
+        group_plan(plan, t->model.dim);
         return true;
     }
     if (nderiv < 1 || nderiv > kMaxDeriv) {
@@ -405,6 +427,7 @@ bool make_plan(const intp_table* t, const int32_t* derivs, int32_t nderiv, Deriv
             // any order above the spline order gives 0 (BSpline.hpp:404-407)
             plan.ord[k][d] = static_cast<int8_t>(std::min<int32_t>(v, t->model.order + 1));
         }
+    group_plan(plan, t->model.dim);
     return true;
 }
 
@@ -550,7 +573,8 @@ intp_status intp_eval(const intp_table* t, const double* coords, int64_t npts, c
     std::string err;
     if (!make_plan(t, derivs, nderiv, plan, err)) return fail(INTP_ERR_INVALID_ARGUMENT, err);
     const int mode = eval_mode();
-    const bool binned = t->mixed() && t->model.dim <= 3 &&
+    // binned needs the per-bucket counters to fit in shared memory
+    const bool binned = t->mixed() && t->model.dim <= 3 && t->bins.smem_buckets > 0 &&
                         (mode == 2 || (mode == 0 && npts >= kBinnedMinPoints));
     if (binned) {
         retain_pool_memory();

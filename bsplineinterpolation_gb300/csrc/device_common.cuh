@@ -62,11 +62,22 @@ struct BinGeom {
     int32_t smem_buckets;        // buckets counted in shared memory (0: global atomics)
 };
 
-// Derivative orders of up to kMaxDeriv outputs per point.
+// Derivative orders of up to kMaxDeriv outputs per point. Outputs with the
+// same orders on axes 1..D-1 form a group: they share the contraction over
+// those axes and differ only in their axis-0 weights.
 struct DerivPlan {
     int32_t k;                      // number of outputs
     int8_t ord[kMaxDeriv][kDevMaxDim];
+    int32_t ngroups;
+    int8_t group_rep[kMaxDeriv];    // an output of each group
+    int8_t out_group[kMaxDeriv];    // group of each output
 };
+
+// Spans per bucket (log2, per axis) of the binned evaluation, fixed per
+// dimension so the shared-memory tile has compile-time strides.
+__host__ __device__ constexpr int bucket_log2(int dim, int axis) {
+    return dim == 1 ? 12 : dim == 2 ? 6 : 4;
+}
 
 // Order-preserving integer key of a double: a < b  <=>  key(a) < key(b) for
 // all non-NaN values, with -0 mapped onto +0 (IEEE compares them equal).

@@ -22,6 +22,7 @@
 
 #include "basis32.cuh"
 #include "device_common.cuh"
+#include "mixed_point.cuh"
 #include "launch.hpp"
 
 namespace intp_gb300 {
@@ -137,84 +138,86 @@ __global__ void __launch_bounds__(128) eval_direct_kernel(TableDev t, const doub
 #pragma unroll
             for (int i = 0; i < W; ++i) off[d][i] = wrap_index(c - O + i, a.n, a.periodic) * a.stride;
         }
-        // Mixed form: contract the differences c_i - c_ref against the weights
-        // and add c_ref back to values. The weights of a value sum to 1 and
-        // those of a derivative to 0, so FP32 rounding of the weights only
-        // multiplies the (small) local variation of the control points.
-        R c_ref = 0;
         if constexpr (MIXED) {
-            int64_t o = 0;
+            // same per-query code as the binned kernel (identical results)
+            const float cref = __ldg(cp + bucket_centre_offset<D, O>(t, cell));
+            const int64_t o0 = p * K;
+            mixed_point_outputs<D, O>(
+                t, plan, cell, xr, base, cref,
+                [&](const int (&ix)[D]) {
+                    int64_t o = 0;
 #pragma unroll
-            for (int d = 0; d < D; ++d) o += off[d][W / 2];
-            c_ref = __ldg(cp + o);
-        }
-        for (int k = 0; k < K; ++k) {
-            R w[D][W];
-            bool zero = false;
-            bool value_out = true;
+                    for (int d = 0; d < D; ++d) o += off[d][ix[d]];
+                    return __ldg(cp + o) - cref;
+                },
+                [out, out_f32, o0](int k, float v) {
+                    if (out_f32)
+                        static_cast<float*>(out)[o0 + k] = v;
+                    else
+                        static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
+                });
+        } else {
+            for (int k = 0; k < K; ++k) {
+                R w[D][W];
+                bool zero = false;
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                const int kd = plan.ord[k][d];
-                if (kd != 0) value_out = false;
-                if (kd > O) {
-                    zero = true;
-                } else if (kd == 0) {
+                for (int d = 0; d < D; ++d) {
+                    const int kd = plan.ord[k][d];
+                    if (kd > O) {
+                        zero = true;
+                    } else if (kd == 0) {
 #pragma unroll
-                    for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
-                } else {
-                    if constexpr (MIXED) {
-                        axis_weights32<O>(t.ax[d], cell[d], xr[d], kd, w[d]);
+                        for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
                     } else {
                         Basis64<O>::eval(t.ax[d], cell[d], xr[d], O - kd, w[d]);
                         deriv_transform<O, R>(t.ax[d], cell[d], kd, w[d]);
                     }
                 }
-            }
-            R acc = 0;
-            if (!zero) {
-                if constexpr (ROWS <= 64) {
+                R acc = 0;
+                if (!zero) {
+                    if constexpr (ROWS <= 64) {
 #pragma unroll
-                    for (int r = 0; r < ROWS; ++r) {
-                        int64_t o = 0;
-                        R wr = 1;
-                        int rem = r;
+                        for (int r = 0; r < ROWS; ++r) {
+                            int64_t o = 0;
+                            R wr = 1;
+                            int rem = r;
 #pragma unroll
-                        for (int d = D - 2; d >= 0; --d) {
-                            const int i = rem % W;
-                            rem /= W;
-                            o += off[d][i];
-                            wr *= w[d][i];
+                            for (int d = D - 2; d >= 0; --d) {
+                                const int i = rem % W;
+                                rem /= W;
+                                o += off[d][i];
+                                wr *= w[d][i];
+                            }
+                            R s = 0;
+#pragma unroll
+                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
+                            acc += wr * s;
                         }
-                        R s = 0;
-#pragma unroll
-                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * (__ldg(cp + o + off[D - 1][i]) - c_ref);
-                        acc += wr * s;
-                    }
-                } else {
-                    // large (O+1)^(D-1): runtime row loop, weights from local memory
+                    } else {
+                        // large (O+1)^(D-1): runtime row loop, weights from local memory
 #pragma unroll 1
-                    for (int r = 0; r < ROWS; ++r) {
-                        int64_t o = 0;
-                        R wr = 1;
-                        int rem = r;
-                        for (int d = D - 2; d >= 0; --d) {
-                            const int i = rem % W;
-                            rem /= W;
-                            o += off[d][i];
-                            wr *= w[d][i];
-                        }
-                        R s = 0;
+                        for (int r = 0; r < ROWS; ++r) {
+                            int64_t o = 0;
+                            R wr = 1;
+                            int rem = r;
+                            for (int d = D - 2; d >= 0; --d) {
+                                const int i = rem % W;
+                                rem /= W;
+                                o += off[d][i];
+                                wr *= w[d][i];
+                            }
+                            R s = 0;
 #pragma unroll
-                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * (__ldg(cp + o + off[D - 1][i]) - c_ref);
-                        acc += wr * s;
+                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
+                            acc += wr * s;
+                        }
                     }
                 }
+                if (out_f32)
+                    static_cast<float*>(out)[p * K + k] = static_cast<float>(acc);
+                else
+                    static_cast<double*>(out)[p * K + k] = static_cast<double>(acc);
             }
-            if (MIXED && value_out && !zero) acc += c_ref;
-            if (out_f32)
-                static_cast<float*>(out)[p * K + k] = static_cast<float>(acc);
-            else
-                static_cast<double*>(out)[p * K + k] = static_cast<double>(acc);
         }
     }
 }

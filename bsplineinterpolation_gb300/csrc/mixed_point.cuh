@@ -1,0 +1,115 @@
+// Outputs of one query in the mixed form, shared by the direct and the
+// binned evaluation kernels so both produce identical results.
+//
+// Control points are read relative to a reference value `cref` (the control
+// point at the centre of the query's bucket tile): value weights sum to 1 and
+// derivative weights to 0, so FP32 rounding of the weights multiplies only the
+// local variation of the control points. Outputs sharing their derivative
+// orders on axes 1..D-1 form a group and share the contraction over those
+// axes; each then applies its own axis-0 weights.
+#pragma once
+
+#include "basis32.cuh"
+#include "device_common.cuh"
+
+namespace intp_gb300 {
+
+constexpr int ipow_i(int b, int e) { return e == 0 ? 1 : b * ipow_i(b, e - 1); }
+
+// fetch(idx) returns control point (c_d - O + idx_d)_d minus cref;
+// emit(k, v) stores output k.
+template <int D, int O, class Fetch, class Emit>
+__device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const DerivPlan& plan, const int64_t (&c)[D],
+                                                    const float (&u)[D], const float (&base)[D][O + 1], float cref,
+                                                    const Fetch& fetch, const Emit& emit) {
+    constexpr int W = O + 1;
+    constexpr int ROWS1 = D >= 2 ? ipow_i(W, D - 2) : 1;  // rows over axes 1..D-2
+    const int K = plan.k;
+    for (int grp = 0; grp < plan.ngroups; ++grp) {
+        const int rep = plan.group_rep[grp];
+        float w[D][W];
+        bool zero = false;
+#pragma unroll
+        for (int d = 1; d < D; ++d) {
+            const int kd = plan.ord[rep][d];
+            if (kd > O) {
+                zero = true;
+            } else if (kd == 0) {
+#pragma unroll
+                for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
+            } else {
+                axis_weights32<O>(t.ax[d], c[d], u[d], kd, w[d]);
+            }
+        }
+        float Pz[W];
+#pragma unroll
+        for (int i0 = 0; i0 < W; ++i0) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int rw = 0; rw < ROWS1; ++rw) {
+                int idx[D];
+                idx[0] = i0;
+                float wr = 1.0f;
+                int rem = rw;
+#pragma unroll
+                for (int d = D - 2; d >= 1; --d) {
+                    idx[d] = rem % W;
+                    rem /= W;
+                    wr *= w[d][idx[d]];
+                }
+                if constexpr (D == 1) {
+                    acc = fetch(idx);
+                } else {
+                    float s = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < W; ++i) {
+                        idx[D - 1] = i;
+                        s += w[D - 1][i] * fetch(idx);
+                    }
+                    acc += wr * s;
+                }
+            }
+            Pz[i0] = acc;
+        }
+        for (int k = 0; k < K; ++k) {
+            if (plan.out_group[k] != grp) continue;
+            const int k0 = plan.ord[k][0];
+            float v = 0.0f;
+            if (!zero && k0 <= O) {
+                float wl[W];
+                if (k0 == 0) {
+#pragma unroll
+                    for (int i = 0; i < W; ++i) wl[i] = base[0][i];
+                } else {
+                    axis_weights32<O>(t.ax[0], c[0], u[0], k0, wl);
+                }
+#pragma unroll
+                for (int i = 0; i < W; ++i) v += wl[i] * Pz[i];
+                bool value_out = k0 == 0;
+#pragma unroll
+                for (int d = 1; d < D; ++d) value_out = value_out && plan.ord[k][d] == 0;
+                if (value_out) v += cref;
+            }
+            emit(k, v);
+        }
+    }
+}
+
+// Index of the control point at the centre of the bucket tile holding span
+// c (the reference value of the centred contraction), for each axis.
+template <int D, int O>
+__device__ __forceinline__ int64_t bucket_centre_offset(const TableDev& t, const int64_t (&c)[D]) {
+    int64_t off = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const AxisDev& a = t.ax[d];
+        const int lb = bucket_log2(D, d);
+        const int64_t org = ((c[d] - O) >> lb) << lb;
+        int64_t gi = org + ((1 << lb) + O) / 2;
+        gi = a.periodic ? gi % a.n : (gi < a.n ? gi : a.n - 1);
+        off += gi * a.stride;
+    }
+    return off;
+}
+
+}  // namespace intp_gb300

@@ -128,7 +128,56 @@ LineFactor line_factor_from(const BandStore& lu) {
     return f;
 }
 
+void line_factor_solve(const LineFactor& f, double* x) {
+    const int64_t n = f.n, p = f.p, q = f.q;
+    std::vector<double> acc(static_cast<size_t>(q > 0 ? q : 1), 0.0);
+    if (f.cyclic)
+        for (int64_t r = 0; r < q; ++r) acc[r] = x[n - q + r];
+    for (int64_t i = 0; i < n; ++i) {
+        double v = (f.cyclic && i >= n - q) ? acc[i - (n - q)] : x[i];
+        for (int64_t k = 0; k < p; ++k)
+            if (i - p + k >= 0) v -= f.lower[i * p + k] * x[i - p + k];
+        if (f.cyclic && i < n - p - 1)
+            for (int64_t r = 0; r < q; ++r) acc[r] -= f.bottom[r * n + i] * v;
+        x[i] = v;
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+        double v = x[i];
+        if (f.cyclic)
+            for (int64_t r = p - 1; r >= 0; --r)
+                if (n - p + r > i + q) v -= f.right[r * n + i] * x[n - p + r];
+        for (int64_t k = q - 1; k >= 0; --k)
+            if (i + 1 + k < n) v -= f.upper[i * q + k] * x[i + 1 + k];
+        x[i] = v * f.dinv[i];
+    }
+}
+
+double fp32_solve_error_estimate(const TableModel& m) {
+    double s = 0.0;
+    for (int d = 0; d < m.dim; ++d) s += m.axis[d].cond_est;
+    return 6.0e-8 * s;
+}
+
 namespace {
+
+// Condition estimate of a collocation matrix. B-spline collocation matrices
+// are totally positive, so the inverse has a checkerboard sign pattern and
+// ||A^-1||_inf = ||A^-1 s||_inf for the alternating vector s (one solve);
+// for the cyclic (periodic) matrices the same solve gives the estimate.
+double condition_estimate(const AxisModel& ax) {
+    const int64_t n = ax.n;
+    std::vector<double> x(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) x[i] = (i % 2) ? -1.0 : 1.0;
+    line_factor_solve(ax.factor, x.data());
+    double inv = 0.0, a = 0.0;
+    for (int64_t i = 0; i < n; ++i) inv = std::max(inv, std::fabs(x[i]));
+    for (int64_t i = 0; i < n; ++i) {
+        double row = 0.0;
+        for (int w = 0; w < ax.stencil.width; ++w) row += std::fabs(ax.stencil.val[i * ax.stencil.width + w]);
+        a = std::max(a, row);
+    }
+    return std::isfinite(a * inv) ? a * inv : 1e300;
+}
 
 // Uniform knots, Interpolation.hpp:322-362 (NO_DUMMY: n = size + periodic).
 std::string uniform_knots(AxisModel& ax, int order, double x0, double x1) {
@@ -290,6 +339,7 @@ std::string build_axis_solver(AxisModel& ax, int order) {
             s.val[w] = ax.colloc.at(i, j);
         }
     }
+    ax.cond_est = condition_estimate(ax);
     return {};
 }
 

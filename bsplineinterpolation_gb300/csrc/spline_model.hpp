@@ -93,6 +93,7 @@ struct AxisModel {
     BandStore lu;                       // its factor
     LineFactor factor;                  // factor in GPU row layout
     RowStencil stencil;                 // collocation rows for residuals
+    double cond_est = 1.0;              // estimate of ||A||_inf ||A^-1||_inf
 };
 
 struct TableSpec {
@@ -115,6 +116,13 @@ struct TableModel {
 // Builds knots and factors. Returns an empty string on success, else the
 // reason (invalid sizes, non-monotonic coordinates, ...).
 std::string build_model(const TableSpec& spec, TableModel& out, bool need_solver = true);
+
+// Solves A x = b in place in FP64 with a factor in row layout (host).
+void line_factor_solve(const LineFactor& f, double* x);
+
+// Predicted relative error of an FP32 control-point solve: about FP32
+// epsilon times the sum of the per-axis condition estimates.
+double fp32_solve_error_estimate(const TableModel& m);
 
 // Knot-span hint of the reference (Interpolation.hpp:277-295); the span that
 // evaluation finds does not depend on it, it only seeds the search.

