@@ -13,6 +13,86 @@
 
 namespace intp_gb300 {
 
+// Polynomial form of the uniform basis: on unit-spaced knots the O+1 basis
+// functions of order O on a span are fixed polynomials in t = (x - t_c)/dx,
+// and so are their derivatives. c[k][j][m] is the coefficient of t^m in
+// d^k/dt^k of basis function j; it is built at compile time by running the
+// Cox-de Boor recursion (BSpline.hpp:91-109) on polynomials.
+template <int O>
+struct UniformPoly {
+    double c[O + 1][O + 1][O + 1];
+};
+
+template <int O>
+constexpr UniformPoly<O> make_uniform_poly() {
+    UniformPoly<O> r{};
+    double N[O + 1][O + 1] = {};
+    N[O][0] = 1.0;
+    for (int i = 1; i <= O; ++i) {
+        const int b = O - i;
+        for (int j = 0; j <= i; ++j) {
+            double v[O + 1] = {};
+            if (j > 0)
+                for (int m = 0; m < O; ++m) {
+                    v[m + 1] += N[b + j][m] / i;
+                    v[m] += N[b + j][m] * static_cast<double>(i - j) / i;
+                }
+            if (b + j < O)
+                for (int m = 0; m < O; ++m) {
+                    v[m] += N[b + j + 1][m] * static_cast<double>(j + 1) / i;
+                    v[m + 1] -= N[b + j + 1][m] / i;
+                }
+            for (int m = 0; m <= O; ++m) N[b + j][m] = v[m];
+        }
+    }
+    for (int k = 0; k <= O; ++k)
+        for (int j = 0; j <= O; ++j)
+            for (int m = 0; m + k <= O; ++m) {
+                double f = 1.0;
+                for (int q = m + 1; q <= m + k; ++q) f *= q;
+                r.c[k][j][m] = N[j][m + k] * f;
+            }
+    return r;
+}
+
+// One coefficient as a compile-time scalar (folded into the instructions).
+template <int O, int K, int J, int M>
+struct UPolyCoef {
+    static constexpr float value = static_cast<float>(make_uniform_poly<O>().c[K][J][M]);
+};
+
+// Horner evaluation of d^K B_J / dt^K at t (degree O - K).
+template <int O, int K, int J, int M = 0>
+__device__ __forceinline__ float uniform_poly_horner(float t) {
+    if constexpr (M == O - K)
+        return UPolyCoef<O, K, J, M>::value;
+    else
+        return fmaf(uniform_poly_horner<O, K, J, M + 1>(t), t, UPolyCoef<O, K, J, M>::value);
+}
+
+// Derivative-K weights on a uniform span: Horner in t, times dx^-K.
+template <int O, int K, int J = 0>
+__device__ __forceinline__ void uniform_poly_weights(float t, float scale, float (&w)[O + 1]) {
+    if constexpr (J <= O) {
+        w[J] = uniform_poly_horner<O, K, J>(t) * scale;
+        uniform_poly_weights<O, K, J + 1>(t, scale, w);
+    }
+}
+
+template <int O, int K = 0>
+__device__ __forceinline__ void uniform_poly_dispatch(int k, float t, float inv_dx, float (&w)[O + 1]) {
+    if constexpr (K <= O) {
+        if (k == K) {
+            float scale = 1.0f;
+#pragma unroll
+            for (int q = 0; q < K; ++q) scale *= inv_dx;
+            uniform_poly_weights<O, K>(t, scale, w);
+        } else {
+            uniform_poly_dispatch<O, K + 1>(k, t, inv_dx, w);
+        }
+    }
+}
+
 // Right-aligned basis of spline order s <= O on unit-spaced knots at local
 // coordinate t in [0, 1): knots at integer positions relative to the cell.
 template <int O>
@@ -89,9 +169,7 @@ __device__ __forceinline__ void transpose_difference(int k, float (&w)[O + 1], A
 template <int O>
 __device__ __forceinline__ void axis_weights32(const AxisDev& a, int64_t c, float u, int k, float (&w)[O + 1]) {
     if (a.uniform && c >= a.int_lo && c <= a.int_hi) {
-        uniform_basis<O>(u * a.inv_dxf, O - k, w);
-        const float id = a.inv_dxf;
-        transpose_difference<O>(k, w, [id](int, int) { return id; });
+        uniform_poly_dispatch<O>(k, u * a.inv_dxf, a.inv_dxf, w);
     } else {
         table_basis<O>(a, c, u, O - k, w);
         const float* rv = a.rinvf;

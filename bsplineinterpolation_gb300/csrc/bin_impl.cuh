@@ -121,7 +121,7 @@ struct TileShape {
 };
 
 template <int D, int O>
-__global__ void __launch_bounds__(kBinThreads) eval_kernel(TableDev t, BinGeom g, const uint32_t* __restrict__ blkoffset,
+__global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeom g, const uint32_t* __restrict__ blkoffset,
                                                            int nblk, const uint32_t* __restrict__ ridx,
                                                            const uint32_t* __restrict__ rcell,
                                                            const float* __restrict__ ru, int64_t cap, int64_t nrec,
@@ -129,11 +129,14 @@ __global__ void __launch_bounds__(kBinThreads) eval_kernel(TableDev t, BinGeom g
     using TS = TileShape<D, O>;
     extern __shared__ float tile[];
     __shared__ float sh_cref;
+    __shared__ DerivPlan sh_plan;  // indexed by runtime output / group numbers
     constexpr int W = O + 1;
     const float* __restrict__ cp = static_cast<const float*>(t.ctrl);
     const int K = plan.k;
     const int64_t r0 = nrec * blockIdx.x / gridDim.x, r1 = nrec * (blockIdx.x + 1) / gridDim.x;
     if (r0 >= r1) return;
+    if (threadIdx.x == 0) sh_plan = plan;
+    __syncthreads();
     // first slot of bucket b (bucket g.nbuckets: one past the last record)
     auto bstart = [&](int64_t bb) -> int64_t {
         return bb >= g.nbuckets ? nrec : static_cast<int64_t>(__ldg(blkoffset + bb * nblk));
@@ -193,25 +196,44 @@ __global__ void __launch_bounds__(kBinThreads) eval_kernel(TableDev t, BinGeom g
             tile[e] = __ldg(cp + off) - cref;
         }
         __syncthreads();
-        for (int64_t rr = r + threadIdx.x; rr < end; rr += blockDim.x) {
-            const uint32_t idx = __ldg(ridx + rr);
-            const uint32_t packed = __ldg(rcell + rr);
-            int64_t c[D];
+        // records are software-pipelined: the next one loads while the
+        // current one is evaluated
+        uint32_t n_idx = 0, n_packed = 0;
+        float n_u[D];
+        int64_t rr = r + threadIdx.x;
+        if (rr < end) {
+            n_idx = __ldg(ridx + rr);
+            n_packed = __ldg(rcell + rr);
+#pragma unroll
+            for (int d = 0; d < D; ++d) n_u[d] = __ldg(ru + d * cap + rr);
+        }
+        for (; rr < end; rr += blockDim.x) {
+            const uint32_t idx = n_idx;
+            const uint32_t packed = n_packed;
             float u[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) u[d] = n_u[d];
+            const int64_t nx = rr + blockDim.x;
+            if (nx < end) {
+                n_idx = __ldg(ridx + nx);
+                n_packed = __ldg(rcell + nx);
+#pragma unroll
+                for (int d = 0; d < D; ++d) n_u[d] = __ldg(ru + d * cap + nx);
+            }
+            int64_t c[D];
             float base[D][W];
             int tb = 0;
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const int cl = static_cast<int>((packed >> g.shift[d]) & ((1u << bucket_log2(D, d)) - 1u));
                 c[d] = org[d] + cl + O;
-                u[d] = __ldg(ru + d * cap + rr);
                 tb += cl * TS::S(d);
                 axis_weights32<O>(t.ax[d], c[d], u[d], 0, base[d]);
             }
             const float* tl = tile + tb;
             const int64_t o0 = static_cast<int64_t>(idx) * K;
             mixed_point_outputs<D, O>(
-                t, plan, c, u, base, cref,
+                t, sh_plan, c, u, base, cref,
                 [tl](const int (&ix)[D]) {
                     int off = 0;
 #pragma unroll

@@ -653,6 +653,8 @@ intp_status intp_locate(const intp_table* t, const double* coords, int64_t npts,
 
 intp_status intp_stream_synchronize(void* stream) {
     INTP_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
+    if (take_device_error(static_cast<cudaStream_t>(stream)) != 0)
+        return fail(INTP_ERR_TIMEOUT, "a kernel's bounded wait for an asynchronous copy ran out");
     return INTP_OK;
 }
 

@@ -53,6 +53,9 @@ cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs
 cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
                                  int64_t S, int64_t nlines, int width, const int64_t* col,
                                  const double* val, cudaStream_t s);
+// Reads and clears the device error flag set by a kernel whose bounded wait
+// ran out (0 = none).
+int take_device_error(cudaStream_t s);
 cudaError_t launch_convert_f64_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 cudaError_t launch_add_f32(float* x, const float* d, int64_t n, cudaStream_t s);
 

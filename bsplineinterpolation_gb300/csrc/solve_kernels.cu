@@ -18,8 +18,10 @@
 // (columns n-1 down to n-p) before the main band (columns i+q down to i+1).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
+#include "async_copy.cuh"
 #include "launch.hpp"
 
 namespace intp_gb300 {
@@ -157,8 +159,133 @@ __global__ void __launch_bounds__(32) solve_contig_kernel(R* __restrict__ x, int
 }
 
 template <class R, int P, int Q, bool CYC>
+cudaError_t launch_solve_pq_fallback(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
+                                     cudaStream_t s);
+
+// ---- tiled solves: one warp stages 32 lines in shared memory ----
+
+// Column of a [n][32] tile: element k of lane l at base[k*32 + l].
+template <class R>
+struct TileColumn {
+    R* base;
+    __device__ __forceinline__ R load(int64_t k) const { return base[k * 32]; }
+    __device__ __forceinline__ void store(int64_t k, R v) const { base[k * 32] = v; }
+};
+
+// Strided axis (S % (16/sizeof(R)) == 0): the tile holds 32 adjacent lines
+// (t0 .. t0+31 for one outer index o); row k of the tile is the 32 contiguous
+// elements k*S + t0 .. + 31, moved by one TMA bulk copy each way.
+template <class R, int P, int Q, bool CYC>
+__global__ void __launch_bounds__(32) solve_tile_strided_kernel(R* __restrict__ x, int64_t n, int64_t S,
+                                                                int64_t tiles_per_o, int64_t ntiles,
+                                                                FactorView<R> f) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    R* tile = reinterpret_cast<R*>(smem_raw);
+    const int lane = threadIdx.x;
+    if (lane == 0) mbar_init(&bar, 1);
+    __syncwarp();
+    uint32_t phase = 0;
+    for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
+        const int64_t o = tl / tiles_per_o, t0 = (tl - o * tiles_per_o) * 32;
+        const int w = static_cast<int>(S - t0 < 32 ? S - t0 : 32);
+        const uint32_t row_bytes = static_cast<uint32_t>(w * sizeof(R));
+        R* base = x + o * n * S + t0;
+        if (lane == 0) mbar_expect_tx(&bar, row_bytes * static_cast<uint32_t>(n));
+        __syncwarp();
+        for (int64_t k = lane; k < n; k += 32) bulk_load(tile + k * 32, base + k * S, row_bytes, &bar);
+        if (!mbar_wait(&bar, phase)) {
+            mbar_wait(&bar, phase);  // give the copies in flight a second bounded wait
+            return;
+        }
+        phase ^= 1u;
+        if (lane < w) solve_line<R, P, Q, CYC>(f, TileColumn<R>{tile + lane});
+        __syncwarp();
+        fence_async_smem();
+        __syncwarp();
+        for (int64_t k = lane; k < n; k += 32) bulk_store(base + k * S, tile + k * 32, row_bytes);
+        bulk_store_commit();
+        bulk_store_wait_read();
+        __syncwarp();
+    }
+    bulk_store_wait_all();
+}
+
+// Contiguous axis (S = 1): 32 lines of n elements copied element-wise with
+// cp.async into rows of pitch n+1, so lane l reading element k of line l
+// touches bank (l + k) mod 32: no conflicts.
+template <class R, int P, int Q, bool CYC>
+__global__ void __launch_bounds__(32) solve_tile_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
+                                                               FactorView<R> f) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* tile = reinterpret_cast<R*>(smem_raw);
+    const int64_t pitch = n + 1;
+    const int lane = threadIdx.x;
+    for (int64_t l0 = blockIdx.x * 32LL; l0 < nlines; l0 += gridDim.x * 32LL) {
+        const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
+        const R* src = x + l0 * n;
+        for (int r = 0; r < rows; ++r)
+            for (int64_t k = lane; k < n; k += 32) cp_async<sizeof(R)>(tile + r * pitch + k, src + r * n + k);
+        cp_async_wait_all();
+        __syncwarp();
+        if (lane < rows) solve_line<R, P, Q, CYC>(f, SmemLine<R>{tile + lane * pitch});
+        __syncwarp();
+        R* dst = x + l0 * n;
+        for (int r = 0; r < rows; ++r)
+            for (int64_t k = lane; k < n; k += 32) dst[r * n + k] = tile[r * pitch + k];
+        __syncwarp();
+    }
+}
+
+int sm_count_solve() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+constexpr size_t kTileSmemLimit = 200 * 1024;
+
+template <class R, int P, int Q, bool CYC>
 cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
                             cudaStream_t s) {
+    const size_t tile_bytes = static_cast<size_t>(n) * 32 * sizeof(R);
+    const bool aligned = (S * static_cast<int64_t>(sizeof(R))) % 16 == 0 &&
+                         (reinterpret_cast<uintptr_t>(x) % 16) == 0;
+    if (S >= 32 && aligned && tile_bytes <= kTileSmemLimit) {
+        auto k = solve_tile_strided_kernel<R, P, Q, CYC>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(tile_bytes));
+        if (e != cudaSuccess) return e;
+        const int64_t tiles_per_o = (S + 31) / 32;
+        const int64_t ntiles = (nlines / S) * tiles_per_o;
+        const int per_sm = static_cast<int>(std::max<size_t>(1, 220 * 1024 / (tile_bytes + 1024)));
+        const int grid = static_cast<int>(std::min<int64_t>(ntiles, int64_t{sm_count_solve()} * per_sm));
+        k<<<grid, 32, tile_bytes, s>>>(x, n, S, tiles_per_o, ntiles, f);
+        note_launch();
+        return cudaGetLastError();
+    }
+    const size_t ctile = static_cast<size_t>(32) * static_cast<size_t>(n + 1) * sizeof(R);
+    if (S == 1 && ctile <= kTileSmemLimit) {
+        auto k = solve_tile_contig_kernel<R, P, Q, CYC>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ctile));
+        if (e != cudaSuccess) return e;
+        const int per_sm = static_cast<int>(std::max<size_t>(1, 220 * 1024 / (ctile + 1024)));
+        const int64_t ntiles = (nlines + 31) / 32;
+        const int grid = static_cast<int>(std::min<int64_t>(ntiles, int64_t{sm_count_solve()} * per_sm));
+        k<<<grid, 32, ctile, s>>>(x, n, nlines, f);
+        note_launch();
+        return cudaGetLastError();
+    }
+    return launch_solve_pq_fallback<R, P, Q, CYC>(x, n, S, nlines, f, s);
+}
+
+template <class R, int P, int Q, bool CYC>
+cudaError_t launch_solve_pq_fallback(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
+                                     cudaStream_t s) {
     const size_t smem = static_cast<size_t>(32) * static_cast<size_t>(n + 1) * sizeof(R);
     if (S == 1 && smem <= 96 * 1024) {
         auto k = solve_contig_kernel<R, P, Q, CYC>;
@@ -268,6 +395,15 @@ __global__ void add_kernel(float* __restrict__ x, const float* __restrict__ d, i
 }
 
 }  // namespace
+
+int take_device_error(cudaStream_t s) {
+    int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return 0;
+    cudaMemcpyToSymbolAsync(g_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+    return v;
+}
 
 cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
                                   bool cyclic, const double* lower, const double* upper,
