@@ -69,6 +69,7 @@ SIGNATURES = {
     "intp_table_knots": (C.c_int, [_P, C.c_int32, _P]),
     "intp_eval": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
     "intp_eval_host": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_eval_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
     "intp_check_range": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_locate": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P]),
     "intp_stream_synchronize": (C.c_int, [_P]),

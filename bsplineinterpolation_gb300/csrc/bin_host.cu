@@ -142,6 +142,17 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
 
 }  // namespace
 
+cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* ridx,
+                           uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s) {
+    switch (t.dim) {
+        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
+        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
+        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
     (void)tile_bytes;
     BinGeom g{};

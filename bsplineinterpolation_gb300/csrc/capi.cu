@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -431,6 +432,32 @@ bool make_plan(const intp_table* t, const int32_t* derivs, int32_t nderiv, Deriv
     return true;
 }
 
+// ---- fixed scratch of the allocation-free evaluation (intp_eval_noalloc) ----
+//
+// One file-scope device array, the same on every device that loads this
+// library (held until the process exits). In host code its name is only a
+// host-side stand-in for the symbol, so the device address is looked up with
+// cudaGetSymbolAddress, once per device, with that device current.
+constexpr size_t kNoAllocScratchBytes = size_t{8} << 20;  // 8 MiB
+constexpr int kNoAllocSortBlocks = 32;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+intp_status noalloc_scratch_address(int dev, void** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(INTP_ERR_UNSUPPORTED, "device ordinal out of range");
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return INTP_OK;
+}
+
 }  // namespace
 
 namespace intp_gb300 {
@@ -710,6 +737,80 @@ intp_status intp_bandlu_solve(const intp_bandlu* lu, double* x, int64_t outer, i
 
 intp_status intp_bandlu_destroy(intp_bandlu* lu) {
     delete lu;
+    return INTP_OK;
+}
+
+intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t npts, const int32_t* derivs,
+                              int32_t nderiv, void* out, int32_t out_dtype, void* stream) {
+    if (!t) return fail(INTP_ERR_INVALID_ARGUMENT, "null table");
+    if (npts < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "npts must be >= 0");
+    if (npts > 0 && (!coords || !out)) return fail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    if (!t->has_ctrl) return fail(INTP_ERR_STATE, "table has no control points yet");
+    if (out_dtype != INTP_F64 && out_dtype != INTP_F32)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    DerivPlan plan;
+    std::string err;
+    if (!make_plan(t, derivs, nderiv, plan, err)) return fail(INTP_ERR_INVALID_ARGUMENT, err);
+    int dev = -1;
+    INTP_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev != t->device) return fail(INTP_ERR_INVALID_ARGUMENT, "make the table's device current first");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool out_f32 = out_dtype == INTP_F32;
+    if (!(t->mixed() && t->model.dim <= 3 && t->bins.smem_buckets > 0)) {
+        // tables the binned path does not take evaluate with the direct
+        // kernel, which needs no scratch
+        if (npts == 0) return INTP_OK;
+        INTP_CUDA(launch_eval_direct(t->dev, t->mixed(), coords, npts, plan, out, out_f32, s), "evaluation kernel");
+        return INTP_OK;
+    }
+    void* base = nullptr;
+    const intp_status st = noalloc_scratch_address(dev, &base);
+    if (st != INTP_OK) return st;
+    // carve the fixed area: per-(bucket, CTA) counts and offsets, scan tile
+    // sums, then as many query records as fit
+    const int D = t->model.dim;
+    const BinGeom& g = t->bins;
+    const int64_t m = g.nbuckets * kNoAllocSortBlocks;
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
+    const size_t per_rec = static_cast<size_t>(8 + 4 * D);
+    if (fixed + 1024 * per_rec + 3 * 256 > kNoAllocScratchBytes)
+        return fail(INTP_ERR_INVALID_ARGUMENT,
+                    "table has too many buckets (" + std::to_string(g.nbuckets) +
+                        ") for the 8 MiB scratch of the allocation-free evaluation; use intp_eval");
+    if (npts == 0) return INTP_OK;
+    int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 3 * 256) / per_rec);
+    cap &= ~int64_t{63};
+    unsigned char* p = static_cast<unsigned char*>(base);
+    uint32_t* blkcount = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>(m) * 4);
+    uint32_t* blkoffset = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>(m) * 4);
+    uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>((m + 4095) / 4096) * 4);
+    uint32_t* ridx = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>(cap) * 4);
+    uint32_t* rcell = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>(cap) * 4);
+    float* ru = reinterpret_cast<float*>(p);
+    // every word the kernels read is written earlier in the same chunk (counts
+    // by the count kernel, offsets by the scan, records by the scatter), so
+    // nothing in the area has to be cleared between calls
+    int sms = 1;
+    INTP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    const size_t ob = out_f32 ? 4 : 8;
+    for (int64_t p0 = 0; p0 < npts; p0 += cap) {
+        const int64_t n = std::min(cap, npts - p0);
+        INTP_CUDA(bin_sort_chunk(t->dev, g, coords + p0 * D, n, kNoAllocSortBlocks, blkcount, blkoffset, tile_sum,
+                                 ridx, rcell, ru, cap, s),
+                  "binned sort");
+        void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
+        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, ridx, rcell, ru, cap, n, plan,
+                                               o, out_f32, sms * 6, s)
+                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, ridx, rcell, ru, cap, n, plan,
+                                              o, out_f32, sms * 6, s),
+                  "binned evaluation");
+    }
     return INTP_OK;
 }
 

@@ -59,7 +59,7 @@ struct BinGeom {
     int32_t tstride[kDevMaxDim];
     int64_t nbuckets;
     int32_t tile_elems;
-    int32_t smem_buckets;        // buckets counted in shared memory (0: global atomics)
+    int32_t smem_buckets;        // bucket count, or 0 when too many: the table evaluates directly
 };
 
 // Derivative orders of up to kMaxDeriv outputs per point. Outputs with the

@@ -26,6 +26,18 @@ cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coor
 // Binned evaluation of the mixed form (bin_host.cu); `chunk` queries per round.
 cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
                             const DerivPlan& plan, void* out, bool out_f32, int64_t chunk, cudaStream_t s);
+// One chunk's counting sort by bucket into caller-provided scratch: blkcount
+// and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096), the
+// records cap entries each (ru: D * cap floats).
+cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* ridx,
+                           uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s);
+cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
+                                const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*, bool,
+                                int, cudaStream_t);
+cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
+                               const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*, bool,
+                               int, cudaStream_t);
 // Bucket geometry for a table (tile of at most `tile_bytes` FP32 control points).
 BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes);
 

@@ -116,6 +116,39 @@ intp_status intp_eval_host(const intp_table* table, const double* coords_host, i
                            const int32_t* derivs, int32_t nderiv, void* out_host,
                            int32_t out_dtype, void* stream);
 
+/* Allocation-free form of intp_eval. No counterpart in the reference, whose
+ * evaluation is per point on the host and needs no scratch.
+ *
+ * Same arguments and results as intp_eval, within FP32 rounding of each
+ * output's scale. It allocates nothing on the device or the host: the
+ * bucket-sort scratch of the binned path is one fixed 8 MiB device array
+ * inside this library.
+ *
+ * Intended callers are those that cannot allocate while they evaluate:
+ *  - a serving loop whose per-request latency must not include pool growth,
+ *    or the device-wide synchronisation of cudaMalloc/cudaFree;
+ *  - a process that has handed nearly all device memory to its own pool,
+ *    where a scratch allocation could fail in the middle of a request.
+ *
+ * Requirements and limits:
+ *  - The table's device must be current.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress), which may run the CUDA runtime's module set-up.
+ *    Make that first call (npts = 0 will do) before any stream capture.
+ *  - The array is shared by every call on a device. Calls whose work
+ *    overlaps on the device (several streams or host threads) race on it, so
+ *    issue them on one stream. Its contents between calls do not matter:
+ *    every word a call reads, the same call wrote earlier.
+ *  - A table whose bucket bookkeeping leaves room for fewer than 1024 query
+ *    records in the 8 MiB is rejected with INTP_ERR_INVALID_ARGUMENT (about
+ *    32k buckets, e.g. a 512^3 cubic table); use intp_eval for it.
+ *  - The number of points is not limited: they are taken in chunks that fit.
+ *  - Tables outside the binned path (FP64 precision, dim 4) run the direct
+ *    kernel, which needs no scratch. */
+intp_status intp_eval_noalloc(const intp_table* table, const double* coords, int64_t npts,
+                              const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
+                              void* stream);
+
 /* Range check of InterpolationFunction::at / derivative_at
  * (Interpolation.hpp:153-169, :213-244, boundary_check_ :482-491) for a batch
  * of device coordinates: *first_bad = index of the first point outside the
