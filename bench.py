@@ -215,7 +215,7 @@ def peak_hbm():
 
 def profile_traffic():
     """Per-launch DRAM bytes of the eval kernel from the committed ncu summary."""
-    path = os.path.join(HERE, "profiles", "eval_kernel_3d_cubic.txt")
+    path = os.path.join(HERE, "profiles", "eval_binned_3d_cubic_256.md")
     try:
         with open(path) as fh:
             for line in fh:
