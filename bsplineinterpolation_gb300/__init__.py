@@ -25,6 +25,7 @@ __all__ = [
     "InterpolationFunctionTemplate",
     "InterpolationFunctionTemplate1D",
     "BandLU",
+    "TableBatch",
     "IntpError",
     "IntpDomainError",
 ]
@@ -60,6 +61,42 @@ def _is_range(r):
     return isinstance(r, (tuple, list)) and len(r) == 2 and all(np.isscalar(v) for v in r)
 
 
+def _make_desc(order, periodicity, mesh_dims, x_ranges, precision, refine_steps):
+    """intp_table_desc of one table; returns (desc, arrays to keep alive, dims,
+    periodicity)."""
+    dims = [int(v) for v in np.atleast_1d(mesh_dims)]
+    D = len(dims)
+    if len(x_ranges) != D:
+        raise ValueError("need one x range per dimension")
+    if periodicity is None:
+        periodicity = [False] * D
+    periodicity = [bool(v) for v in np.atleast_1d(periodicity)]
+    if len(periodicity) != D:
+        raise ValueError("need one periodicity flag per dimension")
+    desc = _lib.TableDesc()
+    desc.dim = D
+    desc.order = int(order)
+    desc.precision = _PRECISIONS[precision]
+    desc.refine_steps = int(refine_steps)
+    keep = []
+    for d in range(D):
+        desc.periodic[d] = int(periodicity[d])
+        desc.size[d] = dims[d]
+        r = x_ranges[d]
+        if _is_range(r):
+            desc.range_lo[d] = float(r[0])
+            desc.range_hi[d] = float(r[1])
+            desc.coords[d] = None
+        else:
+            c = np.ascontiguousarray(np.asarray(r, np.float64))
+            if c.ndim != 1 or c.size != dims[d] + (1 if periodicity[d] else 0):
+                raise ValueError("axis %d: expected %d coordinates" %
+                                 (d, dims[d] + (1 if periodicity[d] else 0)))
+            keep.append(c)
+            desc.coords[d] = c.ctypes.data
+    return desc, keep, dims, periodicity
+
+
 class InterpolationFunctionTemplate:
     """Knots and per-axis band LU factors for a mesh shape; solves for control
     points of any value mesh of that shape.
@@ -73,36 +110,9 @@ class InterpolationFunctionTemplate:
     def __init__(self, order, periodicity, mesh_dims, *x_ranges, precision="fp64",
                  refine_steps=-1):
         lib = _lib.load()
-        dims = [int(v) for v in np.atleast_1d(mesh_dims)]
+        desc, self._coords, dims, periodicity = _make_desc(order, periodicity, mesh_dims, x_ranges,
+                                                           precision, refine_steps)
         D = len(dims)
-        if len(x_ranges) != D:
-            raise ValueError("need one x range per dimension")
-        if periodicity is None:
-            periodicity = [False] * D
-        periodicity = [bool(v) for v in np.atleast_1d(periodicity)]
-        if len(periodicity) != D:
-            raise ValueError("need one periodicity flag per dimension")
-        desc = _lib.TableDesc()
-        desc.dim = D
-        desc.order = int(order)
-        desc.precision = _PRECISIONS[precision]
-        desc.refine_steps = int(refine_steps)
-        self._coords = []
-        for d in range(D):
-            desc.periodic[d] = int(periodicity[d])
-            desc.size[d] = dims[d]
-            r = x_ranges[d]
-            if _is_range(r):
-                desc.range_lo[d] = float(r[0])
-                desc.range_hi[d] = float(r[1])
-                desc.coords[d] = None
-            else:
-                c = np.ascontiguousarray(np.asarray(r, np.float64))
-                if c.ndim != 1 or c.size != dims[d] + (1 if periodicity[d] else 0):
-                    raise ValueError("axis %d: expected %d coordinates" %
-                                     (d, dims[d] + (1 if periodicity[d] else 0)))
-                self._coords.append(c)
-                desc.coords[d] = c.ctypes.data
         h = C.c_void_p()
         _lib.check(lib.intp_table_create(C.byref(desc), C.byref(h)))
         self._h = h
@@ -402,3 +412,102 @@ class BandLU:
         self.solve(xt, stream)
         torch.cuda.synchronize()
         return xt.cpu().numpy()
+
+
+class TableBatch:
+    """Many independent tables built and evaluated together (intp_batch_*).
+
+    `tables` is a sequence of (order, periodicity, mesh_dims, x_ranges)
+    tuples, one per table, with the meaning of InterpolationFunctionTemplate's
+    arguments (dimension 1..3). Every table of a batch has one precision.
+    The reference builds such tables one InterpolationFunction at a time
+    (InterpolationTemplate.hpp:60-143); here one launch per axis pass solves
+    all of them, and one launch per (dimension, order) class evaluates them.
+    """
+
+    def __init__(self, tables, precision="mixed", refine_steps=-1):
+        lib = _lib.load()
+        n = len(tables)
+        descs = (_lib.TableDesc * n)()
+        self._keep = []
+        self.dims = []
+        self.orders = []
+        for i, t in enumerate(tables):
+            order, periodicity, mesh_dims, x_ranges = t
+            desc, keep, dims, _ = _make_desc(order, periodicity, mesh_dims, list(x_ranges), precision,
+                                             refine_steps)
+            descs[i] = desc
+            self._keep.extend(keep)
+            self.dims.append(dims)
+            self.orders.append(int(order))
+        h = C.c_void_p()
+        _lib.check(lib.intp_batch_create(descs, n, C.byref(h)))
+        self._h = h
+        self.ntables = n
+        self.precision = precision
+        self.sizes = [int(np.prod(d)) for d in self.dims]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_batch_destroy(h)
+            self._h = None
+
+    def build(self, values, stream=None):
+        """Solves every table's control points. `values`: one flat array of all
+        meshes in table order (a CUDA tensor stays on the device), or a list
+        of per-table meshes."""
+        lib = _lib.load()
+        if isinstance(values, (list, tuple)):
+            values = np.concatenate([np.asarray(v, np.float64).ravel() for v in values])
+        if _is_cuda_tensor(values):
+            torch = _torch()
+            v = values.to(torch.float64).contiguous().reshape(-1)
+            if v.numel() != int(self.offsets[-1]):
+                raise ValueError("expected %d values" % int(self.offsets[-1]))
+            _lib.check(lib.intp_batch_build(self._h, C.c_void_p(v.data_ptr()), 1, _stream_ptr(stream)))
+            self._kept_values = v
+        else:
+            v = np.ascontiguousarray(np.asarray(values, np.float64).ravel())
+            if v.size != int(self.offsets[-1]):
+                raise ValueError("expected %d values" % int(self.offsets[-1]))
+            _lib.check(lib.intp_batch_build(self._h, v.ctypes.data, 0, _stream_ptr(stream)))
+            _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
+
+    def control_points(self, i):
+        out = np.zeros(self.sizes[i])
+        _lib.check(_lib.load().intp_batch_get_control_points(self._h, i, out.ctypes.data))
+        return out.reshape(self.dims[i])
+
+    def evaluate(self, coords, point_offsets, derivs=None, out=None, out_dtype=None, stream=None):
+        """Evaluates table i at its points point_offsets[i] .. point_offsets[i+1]-1.
+        `coords`: CUDA tensor of every table's points in table order (dim_i
+        doubles per point). `derivs`: K rows of up to 4 derivative orders (a
+        table of dimension D uses the first D). Returns a (points x K) CUDA
+        tensor."""
+        torch = _torch()
+        lib = _lib.load()
+        po = np.ascontiguousarray(np.asarray(point_offsets, np.int64))
+        if po.size != self.ntables + 1:
+            raise ValueError("point_offsets needs ntables + 1 entries")
+        if out_dtype is None:
+            out_dtype = "f32" if self.precision == "mixed" else "f64"
+        od = _lib.F32 if out_dtype == "f32" else _lib.F64
+        if derivs is None:
+            kp, K, karr = None, 1, None
+        else:
+            d = np.asarray(derivs, np.int32)
+            d = d.reshape(-1, d.shape[-1])
+            karr = np.zeros((d.shape[0], _lib.MAX_DIM), np.int32)
+            karr[:, :d.shape[1]] = d
+            K = karr.shape[0]
+            kp = karr.ctypes.data
+        x = coords.to(torch.float64).contiguous().reshape(-1)
+        npts = int(po[-1])
+        if out is None:
+            out = torch.empty((npts, K), dtype=torch.float32 if od == _lib.F32 else torch.float64,
+                              device=x.device)
+        _lib.check(lib.intp_batch_eval(self._h, C.c_void_p(x.data_ptr()), po.ctypes.data, kp, K,
+                                       C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
+        return out

@@ -79,6 +79,12 @@ SIGNATURES = {
                                      C.POINTER(C.c_void_p)]),
     "intp_bandlu_solve": (C.c_int, [_P, _P, C.c_int64, C.c_int64, _P]),
     "intp_bandlu_destroy": (C.c_int, [_P]),
+    "intp_batch_create": (C.c_int, [C.POINTER(TableDesc), C.c_int64, C.POINTER(C.c_void_p)]),
+    "intp_batch_destroy": (C.c_int, [_P]),
+    "intp_batch_info": (C.c_int, [_P, _P, _P]),
+    "intp_batch_build": (C.c_int, [_P, _P, C.c_int32, _P]),
+    "intp_batch_get_control_points": (C.c_int, [_P, C.c_int64, _P]),
+    "intp_batch_eval": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P, C.c_int32, _P]),
 }
 
 _lib = None

@@ -1,0 +1,660 @@
+// Batched tables: thousands of independent interpolation tables of uneven
+// size, order, periodicity and dimension (1..3), built and evaluated
+// together.
+//
+// A batch packs the per-axis data of every table into one device arena and
+// the control points of every table into one array (table i at element
+// offset off[i]). The control-point solve of all tables runs as one launch
+// per axis pass: pass j solves axis D_i - 1 - j of every table i that has
+// one, as a work list of line groups (one warp per group of up to 32 lines),
+// longest lines first. The arithmetic per line is solve_line, the same as the
+// single-table solves, so a batched table gets the control points that
+// intp_table_interpolate gives it, bit for bit. Mixed-precision batches
+// refine per table (FP64 residual, FP32 correction) with the same step count
+// a single table would choose.
+//
+// Evaluation takes one list of query runs per (dimension, order) class and
+// evaluates each run with the per-point code of the direct kernel
+// (eval_point), so batched results equal intp_eval's direct path bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "batch.hpp"
+#include "intp_gpu.h"
+#include "launch.hpp"
+#include "solve_line.cuh"
+#include "spline_model.hpp"
+#include "table_pack.hpp"
+
+using namespace intp_gb300;
+
+namespace {
+
+constexpr int kBatchMaxDim = 3;
+constexpr int32_t kChunkElems = 8192;
+constexpr int64_t kEvalRun = 2048;           // query points per evaluation CTA
+constexpr size_t kStageBytes = 34 * 1024;     // shared memory per warp for contiguous lines
+constexpr size_t kStageMaxBytes = 200 * 1024;  // longest contiguous line staged
+
+intp_status bfail(intp_status s, const std::string& msg);
+
+}  // namespace
+
+struct intp_batch {
+    int precision = INTP_PRECISION_MIXED;
+    int device = 0;
+    int64_t ntables = 0;
+    std::vector<TableModel> models;
+    std::vector<int64_t> off;      // ntables + 1 element offsets
+    std::vector<int> refine;       // refinement steps per table (mixed)
+    int max_refine = 0;
+    std::vector<TableDev> h_tables;
+    void* arena = nullptr;         // per-axis data, descriptors, work lists
+    void* ctrl = nullptr;
+    void* scratch = nullptr;       // refinement buffers
+    size_t scratch_bytes = 0;
+    TableDev* d_tables = nullptr;
+    const AxisFactorDev* d_fac = nullptr;  // [ntables * kBatchMaxDim]
+    const int64_t* d_off = nullptr;
+    const int32_t* d_refine = nullptr;
+    const int2* d_bands = nullptr;  // (band width, cyclic) per (table, axis)
+    const ChunkItem* d_chunks = nullptr;
+    int64_t nchunks = 0;
+    struct Pass {
+        const SolveItem* items = nullptr;
+        int64_t nitems = 0;
+        size_t smem_elems = 0;     // staging elements per warp (contiguous pass)
+    } pass[kBatchMaxDim];
+    int npasses = 0;
+    bool has_ctrl = false;
+
+    ~intp_batch() {
+        if (arena) cudaFree(arena);
+        if (ctrl) cudaFree(ctrl);
+        if (scratch) cudaFree(scratch);
+    }
+    bool mixed() const { return precision == INTP_PRECISION_MIXED; }
+    size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
+};
+
+namespace {
+
+intp_status bfail(intp_status s, const std::string& msg) {
+    set_last_error(msg);
+    return s;
+}
+
+intp_status bcuda(cudaError_t e, const char* what) {
+    set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? INTP_ERR_OUT_OF_MEMORY : INTP_ERR_CUDA;
+}
+
+#define BATCH_CUDA(call, what)                           \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return bcuda(e_, what);   \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+template <class R>
+__device__ __forceinline__ FactorView<R> factor_view(const AxisFactorDev& f, int64_t n);
+
+template <>
+__device__ __forceinline__ FactorView<float> factor_view<float>(const AxisFactorDev& f, int64_t n) {
+    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf};
+}
+
+template <>
+__device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFactorDev& f, int64_t n) {
+    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right};
+}
+
+template <class R, class Line>
+__device__ __forceinline__ void solve_dispatch(int p, bool cyc, const FactorView<R>& fv, const Line& line) {
+    if (cyc) {
+        switch (p) {
+            case 0: solve_line<R, 0, 0, true>(fv, line); return;
+            case 1: solve_line<R, 1, 1, true>(fv, line); return;
+            case 2: solve_line<R, 2, 2, true>(fv, line); return;
+            case 3: solve_line<R, 3, 3, true>(fv, line); return;
+        }
+        return;
+    }
+    switch (p) {
+        case 0: solve_line<R, 0, 0, false>(fv, line); return;
+        case 1: solve_line<R, 1, 1, false>(fv, line); return;
+        case 2: solve_line<R, 2, 2, false>(fv, line); return;
+        case 3: solve_line<R, 3, 3, false>(fv, line); return;
+        case 4: solve_line<R, 4, 4, false>(fv, line); return;
+        case 5: solve_line<R, 5, 5, false>(fv, line); return;
+        case 6: solve_line<R, 6, 6, false>(fv, line); return;
+    }
+}
+
+// One warp per item (one CTA = one warp). `bands` holds the band width and
+// cyclic flag of every (table, axis). Items of tables whose refinement count
+// is not above `step` are skipped (step < 0: none skipped).
+template <class R>
+__global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
+                                                         const TableDev* __restrict__ tables,
+                                                         const AxisFactorDev* __restrict__ fac,
+                                                         const int64_t* __restrict__ off,
+                                                         const int32_t* __restrict__ refine, int step,
+                                                         const int2* __restrict__ bands) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* tile = reinterpret_cast<R*>(smem_raw);
+    const SolveItem it = items[blockIdx.x];
+    if (step >= 0 && refine[it.table] <= step) return;
+    const int lane = threadIdx.x;
+    const TableDev& t = tables[it.table];
+    const AxisDev& ax = t.ax[it.axis];
+    const int64_t n = ax.n, S = ax.stride;
+    const int2 band = bands[it.table * kBatchMaxDim + it.axis];
+    const FactorView<R> fv = factor_view<R>(fac[it.table * kBatchMaxDim + it.axis], n);
+    R* base = data + off[it.table];
+    if (it.staged) {
+        // S == 1: lines line0 .. line0+rows-1 are one contiguous run of rows*n
+        const int64_t pitch = n + 1;
+        R* src = base + it.line0 * n;
+        const int64_t total = static_cast<int64_t>(it.rows) * n;
+        for (int64_t e = lane; e < total; e += 32) {
+            const int64_t r = e / n, k = e - r * n;
+            tile[r * pitch + k] = src[e];
+        }
+        __syncwarp();
+        if (lane < it.rows) solve_dispatch<R>(band.x, band.y != 0, fv, SmemLine<R>{tile + lane * pitch});
+        __syncwarp();
+        for (int64_t e = lane; e < total; e += 32) {
+            const int64_t r = e / n, k = e - r * n;
+            src[e] = tile[r * pitch + k];
+        }
+        return;
+    }
+    if (lane < it.rows) {
+        const int64_t l = it.line0 + lane;
+        const int64_t o = l / S, tt = l - o * S;
+        solve_dispatch<R>(band.x, band.y != 0, fv, StridedLine<R>{base + o * n * S + tt, S});
+    }
+}
+
+// Residual pass of the refinement: one lane per line, mid = A_axis in, or
+// res = fsh - A_axis in on the table's last pass (axis 0).
+template <class Ti>
+__global__ void __launch_bounds__(32) batch_stencil_kernel(const Ti* __restrict__ in, double* __restrict__ mid,
+                                                           double* __restrict__ res, const double* __restrict__ fsh,
+                                                           const SolveItem* __restrict__ items,
+                                                           const TableDev* __restrict__ tables,
+                                                           const AxisFactorDev* __restrict__ fac,
+                                                           const int64_t* __restrict__ off,
+                                                           const int32_t* __restrict__ refine, int step) {
+    const SolveItem it = items[blockIdx.x];
+    if (refine[it.table] <= step) return;
+    const int lane = threadIdx.x;
+    if (lane >= it.rows) return;
+    const TableDev& t = tables[it.table];
+    const AxisDev& ax = t.ax[it.axis];
+    const AxisFactorDev& f = fac[it.table * kBatchMaxDim + it.axis];
+    const int64_t n = ax.n, S = ax.stride;
+    const int64_t l = it.line0 + lane;
+    const int64_t o = l / S, tt = l - o * S;
+    const int64_t o0 = off[it.table];
+    double* out = it.last ? res + o0 : mid + o0;
+    const double* rhs = it.last ? fsh + o0 : nullptr;
+    stencil_line<Ti>(in + o0, out, rhs, o * n * S + tt, n, S, f.width, f.scol, f.sval);
+}
+
+// Element-wise passes over chunk items:
+//  op 0: dst[shift(i)] = (R) src[i] (and fsh[shift(i)] = src[i] when fsh)
+//  op 1: corr[i] = (float) res[i]            (refining tables only)
+//  op 2: ctrl[i] += corr[i]                  (refining tables only)
+// The periodic shift moves index i to (i + O/2) mod n along every periodic
+// axis (InterpolationTemplate.hpp:451-462).
+template <class R>
+__global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const double* __restrict__ src,
+                                                                R* __restrict__ dst, double* __restrict__ fsh,
+                                                                const double* __restrict__ res,
+                                                                float* __restrict__ corr,
+                                                                const ChunkItem* __restrict__ chunks,
+                                                                const TableDev* __restrict__ tables,
+                                                                const int64_t* __restrict__ off,
+                                                                const int32_t* __restrict__ refine, int step) {
+    const ChunkItem c = chunks[blockIdx.x];
+    if (op != 0 && refine[c.table] <= step) return;
+    const int64_t o0 = off[c.table];
+    if (op == 0) {
+        const TableDev& t = tables[c.table];
+        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
+            const int64_t i = c.start + e;
+            int64_t r = i, o = 0;
+            for (int d = t.dim - 1; d >= 0; --d) {
+                const AxisDev& a = t.ax[d];
+                const int64_t q = r / a.n;
+                int64_t idx = r - q * a.n;
+                r = q;
+                if (a.periodic) {
+                    idx += (t.order / 2) % a.n;
+                    if (idx >= a.n) idx -= a.n;
+                }
+                o += idx * a.stride;
+            }
+            const double v = src[o0 + i];
+            dst[o0 + o] = static_cast<R>(v);
+            if (fsh) fsh[o0 + o] = v;
+        }
+    } else if (op == 1) {
+        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
+            const int64_t i = o0 + c.start + e;
+            corr[i] = static_cast<float>(res[i]);
+        }
+    } else {
+        float* x = reinterpret_cast<float*>(dst);
+        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
+            const int64_t i = o0 + c.start + e;
+            x[i] += corr[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+
+size_t up256(size_t v) { return (v + 255) & ~size_t(255); }
+
+int sm_count_batch() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+// Work lists of the axis passes and of the element-wise kernels.
+void build_work(const intp_batch& b, std::vector<std::vector<SolveItem>>& passes, std::vector<size_t>& smem_elems,
+                std::vector<ChunkItem>& chunks) {
+    const size_t esz = b.elem();
+    passes.assign(kBatchMaxDim, {});
+    smem_elems.assign(kBatchMaxDim, 0);
+    for (int64_t i = 0; i < b.ntables; ++i) {
+        const TableModel& m = b.models[i];
+        for (int j = 0; j < m.dim; ++j) {
+            const int a = m.dim - 1 - j;
+            const int64_t n = m.axis[a].n;
+            const int64_t nlines = m.total / n;
+            const bool contig = (a == m.dim - 1);
+            int64_t rows_max = 32;
+            bool staged = false;
+            if (contig) {
+                const size_t line_bytes = static_cast<size_t>(n + 1) * esz;
+                if (line_bytes <= kStageMaxBytes) {
+                    staged = true;
+                    rows_max = std::max<int64_t>(1, std::min<int64_t>(32, static_cast<int64_t>(kStageBytes / line_bytes)));
+                }
+            }
+            for (int64_t l0 = 0; l0 < nlines; l0 += rows_max) {
+                SolveItem it{};
+                it.table = static_cast<int32_t>(i);
+                it.axis = static_cast<int16_t>(a);
+                it.staged = staged ? 1 : 0;
+                it.last = (a == 0) ? 1 : 0;
+                it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
+                it.line0 = l0;
+                passes[j].push_back(it);
+                if (staged)
+                    smem_elems[j] = std::max(smem_elems[j], static_cast<size_t>(it.rows) * static_cast<size_t>(n + 1));
+            }
+        }
+        for (int64_t s = 0; s < m.total; s += kChunkElems) {
+            ChunkItem c{};
+            c.table = static_cast<int32_t>(i);
+            c.start = s;
+            c.len = static_cast<int32_t>(std::min<int64_t>(kChunkElems, m.total - s));
+            chunks.push_back(c);
+        }
+    }
+    // longest lines first: the slowest warps start first
+    for (auto& p : passes)
+        std::stable_sort(p.begin(), p.end(), [&](const SolveItem& x, const SolveItem& y) {
+            return b.models[x.table].axis[x.axis].n > b.models[y.table].axis[y.axis].n;
+        });
+}
+
+template <class R>
+cudaError_t run_passes(intp_batch* b, R* data, int step, const int2* bands, cudaStream_t s) {
+    for (int j = 0; j < b->npasses; ++j) {
+        const intp_batch::Pass& p = b->pass[j];
+        if (p.nitems == 0) continue;
+        const size_t smem = p.smem_elems * sizeof(R);
+        auto k = batch_solve_kernel<R>;
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+        k<<<static_cast<unsigned>(p.nitems), 32, smem, s>>>(data, p.items, b->d_tables, b->d_fac, b->d_off, b->d_refine,
+                                                             step, bands);
+        note_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t s) {
+    const int64_t N = b->off[b->ntables];
+    const int2* bands = b->d_bands;
+    const unsigned nch = static_cast<unsigned>(b->nchunks);
+    if (!b->mixed()) {
+        double* c = static_cast<double*>(b->ctrl);
+        batch_elementwise_kernel<double><<<nch, 256, 0, s>>>(0, values, c, nullptr, nullptr, nullptr, b->d_chunks,
+                                                             b->d_tables, b->d_off, b->d_refine, -1);
+        note_launch();
+        BATCH_CUDA(cudaGetLastError(), "batch shift copy");
+        BATCH_CUDA(run_passes<double>(b, c, -1, bands, s), "batch line solve (fp64)");
+        b->has_ctrl = true;
+        return INTP_OK;
+    }
+    float* c = static_cast<float*>(b->ctrl);
+    double* fsh = nullptr;
+    double *tmp = nullptr, *tmp2 = nullptr, *res = nullptr;
+    float* corr = nullptr;
+    if (b->max_refine > 0) {
+        const size_t need = static_cast<size_t>(N) * (8 * 4 + 4) + 1024;
+        if (b->scratch_bytes < need) {
+            if (b->scratch) cudaFree(b->scratch);
+            b->scratch = nullptr;
+            b->scratch_bytes = 0;
+            BATCH_CUDA(cudaMalloc(&b->scratch, need), "cudaMalloc(batch refinement scratch)");
+            b->scratch_bytes = need;
+        }
+        unsigned char* p = static_cast<unsigned char*>(b->scratch);
+        fsh = reinterpret_cast<double*>(p);
+        tmp = reinterpret_cast<double*>(p + N * 8);
+        tmp2 = reinterpret_cast<double*>(p + N * 16);
+        res = reinterpret_cast<double*>(p + N * 24);
+        corr = reinterpret_cast<float*>(p + N * 32);
+    }
+    batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(0, values, c, fsh, nullptr, nullptr, b->d_chunks, b->d_tables,
+                                                        b->d_off, b->d_refine, -1);
+    note_launch();
+    BATCH_CUDA(cudaGetLastError(), "batch shift copy");
+    BATCH_CUDA(run_passes<float>(b, c, -1, bands, s), "batch line solve (fp32)");
+    for (int step = 0; step < b->max_refine; ++step) {
+        // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass, FP64:
+        // c -> tmp -> tmp2 -> ..., each table's last pass writing res
+        for (int j = 0; j < b->npasses; ++j) {
+            const intp_batch::Pass& p = b->pass[j];
+            if (p.nitems == 0) continue;
+            if (j == 0)
+                batch_stencil_kernel<float><<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(
+                    c, tmp, res, fsh, p.items, b->d_tables, b->d_fac, b->d_off, b->d_refine, step);
+            else
+                batch_stencil_kernel<double><<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(
+                    j == 1 ? tmp : tmp2, j == 1 ? tmp2 : tmp, res, fsh, p.items, b->d_tables, b->d_fac, b->d_off,
+                    b->d_refine, step);
+            note_launch();
+            BATCH_CUDA(cudaGetLastError(), "batch residual");
+        }
+        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, nullptr, nullptr, res, corr, b->d_chunks,
+                                                            b->d_tables, b->d_off, b->d_refine, step);
+        note_launch();
+        BATCH_CUDA(run_passes<float>(b, corr, step, bands, s), "batch line solve (correction)");
+        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(2, nullptr, c, nullptr, nullptr, corr, b->d_chunks,
+                                                            b->d_tables, b->d_off, b->d_refine, step);
+        note_launch();
+        BATCH_CUDA(cudaGetLastError(), "batch correction");
+    }
+    b->has_ctrl = true;
+    return INTP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, intp_batch** out) {
+    if (!descs || !out) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (ntables < 1 || ntables > (int64_t{1} << 30)) return bfail(INTP_ERR_INVALID_ARGUMENT, "ntables must be >= 1");
+    const int prec = descs[0].precision;
+    if (prec != INTP_PRECISION_FP64 && prec != INTP_PRECISION_MIXED)
+        return bfail(INTP_ERR_INVALID_ARGUMENT, "unknown precision");
+    intp_batch* b = new (std::nothrow) intp_batch();
+    if (!b) return bfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    b->precision = prec;
+    b->ntables = ntables;
+    b->off.assign(static_cast<size_t>(ntables) + 1, 0);
+    b->refine.assign(static_cast<size_t>(ntables), 0);
+    try {
+        b->models.resize(static_cast<size_t>(ntables));
+        for (int64_t i = 0; i < ntables; ++i) {
+            const intp_table_desc& d = descs[i];
+            const std::string where = "table " + std::to_string(i) + ": ";
+            if (d.precision != prec) {
+                delete b;
+                return bfail(INTP_ERR_INVALID_ARGUMENT, where + "every table of a batch has the same precision");
+            }
+            if (d.dim < 1 || d.dim > kBatchMaxDim) {
+                delete b;
+                return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables have dimension 1..3");
+            }
+            if (d.order < 0 || d.order > INTP_GPU_MAX_ORDER) {
+                delete b;
+                return bfail(INTP_ERR_UNSUPPORTED, where + "order must be in [0, 7]");
+            }
+            if (d.refine_steps < -1 || d.refine_steps > 4) {
+                delete b;
+                return bfail(INTP_ERR_INVALID_ARGUMENT, where + "refine_steps must be in [-1, 4]");
+            }
+            TableSpec spec;
+            spec.dim = d.dim;
+            spec.order = d.order;
+            for (int a = 0; a < d.dim; ++a) {
+                spec.periodic[a] = d.periodic[a] != 0;
+                spec.size[a] = d.size[a];
+                spec.lo[a] = d.range_lo[a];
+                spec.hi[a] = d.range_hi[a];
+                spec.coords[a] = d.coords[a];
+            }
+            const std::string err = build_model(spec, b->models[i]);
+            if (!err.empty()) {
+                delete b;
+                return bfail(INTP_ERR_INVALID_ARGUMENT, where + err);
+            }
+            b->off[i + 1] = b->off[i] + b->models[i].total;
+            if (b->mixed()) {
+                b->refine[i] = d.refine_steps < 0 ? auto_refine_steps(b->models[i]) : d.refine_steps;
+                b->max_refine = std::max(b->max_refine, b->refine[i]);
+            }
+        }
+    } catch (const std::bad_alloc&) {
+        delete b;
+        return bfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    }
+    cudaGetDevice(&b->device);
+
+    // one arena: per-axis data of every table, then descriptors and work lists
+    Arena ar;
+    std::vector<PackedTable> packed(static_cast<size_t>(ntables));
+    for (int64_t i = 0; i < ntables; ++i) pack_table(b->models[i], ar, packed[i]);
+    std::vector<std::vector<SolveItem>> passes;
+    std::vector<size_t> smem_elems;
+    std::vector<ChunkItem> chunks;
+    build_work(*b, passes, smem_elems, chunks);
+    std::vector<int2> bands(static_cast<size_t>(ntables) * kBatchMaxDim, int2{0, 0});
+    for (int64_t i = 0; i < ntables; ++i)
+        for (int a = 0; a < b->models[i].dim; ++a) {
+            const LineFactor& f = b->models[i].axis[a].factor;
+            bands[i * kBatchMaxDim + a] = int2{f.p, f.cyclic ? 1 : 0};
+        }
+    std::vector<int32_t> refine32(b->refine.begin(), b->refine.end());
+    const size_t o_tables = ar.add(sizeof(TableDev) * static_cast<size_t>(ntables));
+    const size_t o_fac = ar.add(sizeof(AxisFactorDev) * static_cast<size_t>(ntables) * kBatchMaxDim);
+    const size_t o_off = ar.put(b->off);
+    const size_t o_ref = ar.put(refine32);
+    const size_t o_bands = ar.put(bands);
+    const size_t o_chunks = ar.put(chunks);
+    size_t o_pass[kBatchMaxDim];
+    for (int j = 0; j < kBatchMaxDim; ++j) o_pass[j] = ar.put(passes[j]);
+    cudaError_t e = cudaMalloc(&b->arena, ar.host.size());
+    if (e != cudaSuccess) {
+        delete b;
+        return bcuda(e, "cudaMalloc(batch arena)");
+    }
+    const size_t N = static_cast<size_t>(b->off[ntables]);
+    e = cudaMalloc(&b->ctrl, std::max<size_t>(N, 1) * b->elem());
+    if (e != cudaSuccess) {
+        delete b;
+        return bcuda(e, "cudaMalloc(batch control points)");
+    }
+    const unsigned char* base = static_cast<const unsigned char*>(b->arena);
+    b->h_tables.resize(static_cast<size_t>(ntables));
+    std::vector<AxisFactorDev> fac(static_cast<size_t>(ntables) * kBatchMaxDim);
+    for (int64_t i = 0; i < ntables; ++i) {
+        double lo_user[kMaxDim] = {};
+        for (int a = 0; a < descs[i].dim; ++a) lo_user[a] = descs[i].range_lo[a];
+        TableDev& dv = b->h_tables[i];
+        std::memset(&dv, 0, sizeof dv);
+        bind_table(b->models[i], lo_user, packed[i], base, dv, &fac[i * kBatchMaxDim]);
+        dv.ctrl = static_cast<const unsigned char*>(b->ctrl) + static_cast<size_t>(b->off[i]) * b->elem();
+    }
+    std::memcpy(ar.host.data() + o_tables, b->h_tables.data(), sizeof(TableDev) * static_cast<size_t>(ntables));
+    std::memcpy(ar.host.data() + o_fac, fac.data(), sizeof(AxisFactorDev) * fac.size());
+    e = cudaMemcpy(b->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete b;
+        return bcuda(e, "cudaMemcpy(batch arena)");
+    }
+    b->d_tables = reinterpret_cast<TableDev*>(static_cast<unsigned char*>(b->arena) + o_tables);
+    b->d_fac = reinterpret_cast<const AxisFactorDev*>(base + o_fac);
+    b->d_off = reinterpret_cast<const int64_t*>(base + o_off);
+    b->d_refine = reinterpret_cast<const int32_t*>(base + o_ref);
+    b->d_bands = reinterpret_cast<const int2*>(base + o_bands);
+    b->d_chunks = reinterpret_cast<const ChunkItem*>(base + o_chunks);
+    b->nchunks = static_cast<int64_t>(chunks.size());
+    b->npasses = 0;
+    for (int j = 0; j < kBatchMaxDim; ++j) {
+        b->pass[j].items = reinterpret_cast<const SolveItem*>(base + o_pass[j]);
+        b->pass[j].nitems = static_cast<int64_t>(passes[j].size());
+        b->pass[j].smem_elems = smem_elems[j];
+        if (!passes[j].empty()) b->npasses = j + 1;
+    }
+    *out = b;
+    return INTP_OK;
+}
+
+intp_status intp_batch_destroy(intp_batch* b) {
+    delete b;
+    return INTP_OK;
+}
+
+intp_status intp_batch_info(const intp_batch* b, int64_t* ntables, int64_t* total_values) {
+    if (!b) return bfail(INTP_ERR_INVALID_ARGUMENT, "null batch");
+    if (ntables) *ntables = b->ntables;
+    if (total_values) *total_values = b->off[b->ntables];
+    return INTP_OK;
+}
+
+intp_status intp_batch_build(intp_batch* b, const double* values, int32_t values_on_device, void* stream) {
+    if (!b || !values) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (values_on_device) return batch_interpolate(b, values, s);
+    const size_t bytes = static_cast<size_t>(b->off[b->ntables]) * 8;
+    void* stage = nullptr;
+    BATCH_CUDA(cudaMallocAsync(&stage, bytes, s), "cudaMallocAsync(batch values)");
+    cudaError_t e = cudaMemcpyAsync(stage, values, bytes, cudaMemcpyHostToDevice, s);
+    intp_status st = e == cudaSuccess ? batch_interpolate(b, static_cast<double*>(stage), s)
+                                      : bcuda(e, "cudaMemcpyAsync(batch values)");
+    cudaFreeAsync(stage, s);
+    return st;
+}
+
+intp_status intp_batch_get_control_points(const intp_batch* b, int64_t table, double* out) {
+    if (!b || !out) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (table < 0 || table >= b->ntables) return bfail(INTP_ERR_INVALID_ARGUMENT, "table index out of range");
+    if (!b->has_ctrl) return bfail(INTP_ERR_STATE, "batch has no control points yet");
+    const int64_t n = b->off[table + 1] - b->off[table];
+    BATCH_CUDA(cudaDeviceSynchronize(), "synchronize");
+    const unsigned char* src = static_cast<const unsigned char*>(b->ctrl) + static_cast<size_t>(b->off[table]) * b->elem();
+    if (b->mixed()) {
+        std::vector<float> f(static_cast<size_t>(n));
+        BATCH_CUDA(cudaMemcpy(f.data(), src, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+        for (int64_t i = 0; i < n; ++i) out[i] = f[i];
+    } else {
+        BATCH_CUDA(cudaMemcpy(out, src, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+    }
+    return INTP_OK;
+}
+
+intp_status intp_batch_eval(const intp_batch* b, const double* coords, const int64_t* point_offsets,
+                            const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype, void* stream) {
+    if (!b || !point_offsets) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (!b->has_ctrl) return bfail(INTP_ERR_STATE, "batch has no control points yet");
+    if (out_dtype != INTP_F64 && out_dtype != INTP_F32) return bfail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    if (point_offsets[0] != 0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets[0] must be 0");
+    if (derivs && (nderiv < 1 || nderiv > INTP_GPU_MAX_DERIV))
+        return bfail(INTP_ERR_INVALID_ARGUMENT, "nderiv must be in [1, 16]");
+    // runs of queries per (dim, order) class
+    std::vector<EvalItem> items[kBatchMaxDim + 1][INTP_GPU_MAX_ORDER + 1];
+    int64_t coff = 0;
+    for (int64_t i = 0; i < b->ntables; ++i) {
+        const int64_t p0 = point_offsets[i], p1 = point_offsets[i + 1];
+        if (p1 < p0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets must not decrease");
+        const TableModel& m = b->models[i];
+        for (int64_t p = p0; p < p1; p += kEvalRun) {
+            EvalItem it{};
+            it.table = static_cast<int32_t>(i);
+            it.count = static_cast<int32_t>(std::min<int64_t>(kEvalRun, p1 - p));
+            it.coord_off = coff + (p - p0) * m.dim;
+            it.out_pt = p;
+            items[m.dim][m.order].push_back(it);
+        }
+        coff += (p1 - p0) * m.dim;
+    }
+    const int64_t npts = point_offsets[b->ntables];
+    if (npts == 0) return INTP_OK;
+    if (!coords || !out) return bfail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    size_t nitems = 0;
+    for (auto& row : items)
+        for (auto& v : row) nitems += v.size();
+    std::vector<EvalItem> flat;
+    flat.reserve(nitems);
+    for (auto& row : items)
+        for (auto& v : row) flat.insert(flat.end(), v.begin(), v.end());
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    EvalItem* d_items = nullptr;
+    BATCH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_items), flat.size() * sizeof(EvalItem), s),
+               "cudaMallocAsync(batch work list)");
+    cudaError_t e = cudaMemcpyAsync(d_items, flat.data(), flat.size() * sizeof(EvalItem), cudaMemcpyHostToDevice, s);
+    size_t pos = 0;
+    intp_status st = INTP_OK;
+    if (e != cudaSuccess) st = bcuda(e, "cudaMemcpyAsync(batch work list)");
+    for (int D = 1; D <= kBatchMaxDim && st == INTP_OK; ++D)
+        for (int O = 0; O <= INTP_GPU_MAX_ORDER && st == INTP_OK; ++O) {
+            const std::vector<EvalItem>& v = items[D][O];
+            if (v.empty()) continue;
+            DerivPlan plan;
+            std::string err;
+            if (!build_deriv_plan(D, O, derivs, nderiv, INTP_GPU_MAX_DIM, plan, err)) {
+                st = bfail(INTP_ERR_INVALID_ARGUMENT, err);
+                break;
+            }
+            e = launch_batch_eval(D, O, b->mixed(), b->d_tables, d_items + pos, static_cast<int64_t>(v.size()), coords,
+                                  plan, out, out_dtype == INTP_F32, s);
+            if (e != cudaSuccess) st = bcuda(e, "batched evaluation");
+            pos += v.size();
+        }
+    cudaFreeAsync(d_items, s);
+    return st;
+}
+
+}  // extern "C"

@@ -9,13 +9,6 @@
 
 namespace intp_gb300 {
 
-cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
-                                const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*,
-                                bool, int, cudaStream_t);
-cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t*, int, const uint32_t*,
-                               const uint32_t*, const float*, int64_t, int64_t, const DerivPlan&, void*,
-                               bool, int, cudaStream_t);
-
 namespace bin_detail {
 
 constexpr int kScanThreads = 1024;
@@ -112,8 +105,7 @@ int sm_count() {
 
 template <int D>
 cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* ridx,
-                        uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s) {
+                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec, cudaStream_t s) {
     using namespace bin_detail;
     const int64_t slice = (n + nblk - 1) / nblk;
     const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
@@ -135,7 +127,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, ridx, rcell, ru, cap);
+    ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }
@@ -143,12 +135,12 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
 }  // namespace
 
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* ridx,
-                           uint32_t* rcell, float* ru, int64_t cap, cudaStream_t s) {
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec,
+                           cudaStream_t s) {
     switch (t.dim) {
-        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
-        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
-        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s);
+        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
+        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
+        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -185,14 +177,14 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
     const int64_t cap = std::min<int64_t>(chunk, npts);
-    const int nblk = sm_count() * 2;  // count/scatter CTAs of kSortThreads
+    const int nblk = sm_count() * 2;  // count/scatter CTAs of kSortThreads (one pair per SM)
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + bin_detail::kScanTile - 1) / bin_detail::kScanTile;
     if (ntiles > bin_detail::kScanThreads * bin_detail::kScanItems) return cudaErrorInvalidValue;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t b_m = up(static_cast<size_t>(m) * 4), b_t = up(static_cast<size_t>(ntiles) * 4);
-    const size_t b_r = up(static_cast<size_t>(cap) * 4);
-    const size_t total = b_m * 2 + b_t + b_r * (2 + D);
+    const size_t b_r = up(static_cast<size_t>(cap) * 4 * (2 + D));
+    const size_t total = b_m * 2 + b_t + b_r;
     void* mem = nullptr;
     cudaError_t e = cudaMallocAsync(&mem, total, s);
     if (e != cudaSuccess) return e;
@@ -203,27 +195,18 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     p += b_m;
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += b_t;
-    uint32_t* ridx = reinterpret_cast<uint32_t*>(p);
-    p += b_r;
-    uint32_t* rcell = reinterpret_cast<uint32_t*>(p);
-    p += b_r;
-    float* ru = reinterpret_cast<float*>(p);
+    uint32_t* rec = reinterpret_cast<uint32_t*>(p);
     const int K = plan.k;
     const size_t ob = out_f32 ? 4 : 8;
-    const int grid_eval = sm_count() * 6;
+    const int grid_eval = sm_count() * 2;
     for (int64_t p0 = 0; p0 < npts && e == cudaSuccess; p0 += cap) {
         const int64_t n = std::min(cap, npts - p0);
         const double* c = coords + p0 * D;
-        switch (D) {
-            case 1: e = launch_sort<1>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
-            case 2: e = launch_sort<2>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
-            case 3: e = launch_sort<3>(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, ridx, rcell, ru, cap, s); break;
-            default: e = cudaErrorInvalidValue;
-        }
+        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
-        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s)
-                   : launch_bin_eval_d3(t, g, blkoffset, nblk, ridx, rcell, ru, cap, n, plan, o, out_f32, grid_eval, s);
+        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, rec, n, plan, o, out_f32, grid_eval, s)
+                   : launch_bin_eval_d3(t, g, blkoffset, nblk, rec, n, plan, o, out_f32, grid_eval, s);
     }
     cudaError_t e2 = cudaFreeAsync(mem, s);
     return e != cudaSuccess ? e : e2;

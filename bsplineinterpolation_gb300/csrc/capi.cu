@@ -15,6 +15,7 @@
 #include "intp_gpu.h"
 #include "launch.hpp"
 #include "spline_model.hpp"
+#include "table_pack.hpp"
 
 using namespace intp_gb300;
 
@@ -25,7 +26,7 @@ std::atomic<unsigned long long> g_launches{0};
 // binned evaluation: shared-memory tile budget per CTA, queries per chunk
 // (chunk outputs stay L2-resident), smallest batch worth binning
 constexpr int64_t kTileBytes = 48 * 1024;
-constexpr int64_t kDefaultChunk = int64_t{1} << 22;
+constexpr int64_t kDefaultChunk = int64_t{1} << 23;
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
 // INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
@@ -76,30 +77,6 @@ intp_status cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-// Bump allocator over one host staging buffer mirrored to one device buffer.
-struct Arena {
-    std::vector<unsigned char> host;
-    size_t add(size_t bytes) {
-        const size_t off = (host.size() + 255) & ~size_t(255);
-        host.resize(off + std::max<size_t>(bytes, 1));
-        return off;
-    }
-    template <class T>
-    size_t put(const std::vector<T>& v) {
-        const size_t off = add(v.size() * sizeof(T));
-        if (!v.empty()) std::memcpy(host.data() + off, v.data(), v.size() * sizeof(T));
-        return off;
-    }
-};
-
-struct AxisFactorDev {
-    const double *lower, *upper, *dinv, *bottom, *right;
-    const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
-    const int64_t* scol;
-    const double* sval;
-    int width;
-};
-
 std::vector<float> to_f32(const std::vector<double>& v) {
     std::vector<float> r(v.size());
     for (size_t i = 0; i < v.size(); ++i) r[i] = static_cast<float>(v[i]);
@@ -122,11 +99,26 @@ struct intp_table {
     void* scratch = nullptr;  // solve scratch (values staging, refinement buffers)
     size_t scratch_bytes = 0;
     double lo_user[kMaxDim]{};  // uniform axes: x_range.first
+    size_t arena_bytes = 0;
+    // Tables of the serving loop take their memory from the stream-ordered
+    // pool on alloc_stream (no device-wide synchronisation on free).
+    bool stream_ordered = false;
+    cudaStream_t alloc_stream = nullptr;
 
+    cudaError_t dmalloc(void** p, size_t bytes) {
+        return stream_ordered ? cudaMallocAsync(p, bytes, alloc_stream) : cudaMalloc(p, bytes);
+    }
+    void dfree(void* p) {
+        if (!p) return;
+        if (stream_ordered)
+            cudaFreeAsync(p, alloc_stream);
+        else
+            cudaFree(p);
+    }
     ~intp_table() {
-        if (arena) cudaFree(arena);
-        if (ctrl) cudaFree(ctrl);
-        if (scratch) cudaFree(scratch);
+        dfree(arena);
+        dfree(ctrl);
+        dfree(scratch);
     }
     bool mixed() const { return precision == INTP_PRECISION_MIXED; }
     size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
@@ -147,130 +139,29 @@ namespace {
 // Per-axis tables used by evaluation and the solve, laid out in one arena.
 intp_status upload_table(intp_table* t) {
     const TableModel& m = t->model;
-    const int O = m.order;
     Arena ar;
-    struct Offs {
-        size_t knots, keys, rinv, rinvf, kdf, khi, klo;
-        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, scol, sval;
-    } off[kMaxDim];
-    for (int d = 0; d < m.dim; ++d) {
-        const AxisModel& ax = m.axis[d];
-        const std::vector<double>& t0 = ax.knots;
-        const int64_t nk = static_cast<int64_t>(t0.size());
-        std::vector<long long> keys(nk);
-        std::vector<double> rinv(static_cast<size_t>(nk * std::max(O, 1)), 0.0);
-        std::vector<float> kdf(static_cast<size_t>(nk * (2 * O + 2)), 0.0f), khi(nk), klo(nk);
-        for (int64_t a = 0; a < nk; ++a) {
-            unsigned long long b;
-            std::memcpy(&b, &t0[a], 8);
-            keys[a] = knot_key_bits(b);
-            for (int s = 1; s <= O; ++s)
-                if (a + s < nk && t0[a + s] != t0[a]) rinv[a * O + (s - 1)] = 1.0 / (t0[a + s] - t0[a]);
-            for (int j = -O; j <= O + 1; ++j)
-                if (a + j >= 0 && a + j < nk) kdf[a * (2 * O + 2) + (j + O)] = static_cast<float>(t0[a + j] - t0[a]);
-            const uint32_t hb = split_hi_bits(b);
-            float hf;
-            std::memcpy(&hf, &hb, 4);
-            khi[a] = hf;
-            klo[a] = static_cast<float>(t0[a] - static_cast<double>(hf));
-        }
-        Offs& o = off[d];
-        o.knots = ar.put(t0);
-        o.keys = ar.put(keys);
-        o.rinv = ar.put(rinv);
-        o.rinvf = ar.put(to_f32(rinv));
-        o.kdf = ar.put(kdf);
-        o.khi = ar.put(khi);
-        o.klo = ar.put(klo);
-        const LineFactor& f = ax.factor;
-        o.lower = ar.put(f.lower);
-        o.upper = ar.put(f.upper);
-        o.dinv = ar.put(f.dinv);
-        o.bottom = ar.put(f.bottom);
-        o.right = ar.put(f.right);
-        o.lowerf = ar.put(to_f32(f.lower));
-        o.upperf = ar.put(to_f32(f.upper));
-        o.dinvf = ar.put(to_f32(f.dinv));
-        o.bottomf = ar.put(to_f32(f.bottom));
-        o.rightf = ar.put(to_f32(f.right));
-        o.scol = ar.put(ax.stencil.col);
-        o.sval = ar.put(ax.stencil.val);
-    }
-    INTP_CUDA(cudaMalloc(&t->arena, ar.host.size()), "cudaMalloc(table)");
-    INTP_CUDA(cudaMemcpy(t->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice),
-              "cudaMemcpy(table)");
-    unsigned char* base = static_cast<unsigned char*>(t->arena);
-    TableDev& dv = t->dev;
-    dv.dim = m.dim;
-    dv.order = O;
-    int64_t stride = 1;
-    for (int d = m.dim - 1; d >= 0; --d) {
-        const AxisModel& ax = m.axis[d];
-        AxisDev& a = dv.ax[d];
-        const Offs& o = off[d];
-        a.n = ax.n;
-        a.nknots = static_cast<int64_t>(ax.knots.size());
-        a.stride = stride;
-        stride *= ax.n;
-        a.periodic = ax.periodic ? 1 : 0;
-        a.uniform = ax.uniform ? 1 : 0;
-        a.lo = ax.range_lo;
-        a.hi = ax.range_hi;
-        a.period = ax.range_hi - ax.range_lo;
-        a.ncells = a.nknots - 2 * O - 1;  // spans O .. nknots-O-2
-        a.int_lo = 1;
-        a.int_hi = 0;
-        if (ax.uniform) {
-            const int64_t extra = ax.periodic ? 2 * O + (1 - O % 2) : O + 1;
-            a.hint_x0 = static_cast<float>(t->lo_user[d]);
-            a.hint_inv_dx = static_cast<float>(1.0 / ax.dx);
-            a.hint_off = static_cast<float>(0.5 * static_cast<double>(extra));
-            a.inv_dxf = static_cast<float>(1.0 / ax.dx);
-            // the basis at span c reads knots c-O+1 .. c+O; on a periodic axis
-            // all knots are uniform, on a non-periodic one knots O+1 ..
-            // nknots-O-2 are (the ends are clamped)
-            if (ax.periodic) {
-                a.int_lo = O;
-                a.int_hi = a.nknots - O - 2;
-            } else {
-                a.int_lo = 2 * O;
-                a.int_hi = a.nknots - 2 * O - 2;
-            }
-        }
-        a.knots = reinterpret_cast<const double*>(base + o.knots);
-        a.keys = reinterpret_cast<const long long*>(base + o.keys);
-        a.rinv = reinterpret_cast<const double*>(base + o.rinv);
-        a.rinvf = reinterpret_cast<const float*>(base + o.rinvf);
-        a.kdf = reinterpret_cast<const float*>(base + o.kdf);
-        a.khi = reinterpret_cast<const float*>(base + o.khi);
-        a.klo = reinterpret_cast<const float*>(base + o.klo);
-        AxisFactorDev& fd = t->fac[d];
-        fd.lower = reinterpret_cast<const double*>(base + o.lower);
-        fd.upper = reinterpret_cast<const double*>(base + o.upper);
-        fd.dinv = reinterpret_cast<const double*>(base + o.dinv);
-        fd.bottom = reinterpret_cast<const double*>(base + o.bottom);
-        fd.right = reinterpret_cast<const double*>(base + o.right);
-        fd.lowerf = reinterpret_cast<const float*>(base + o.lowerf);
-        fd.upperf = reinterpret_cast<const float*>(base + o.upperf);
-        fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
-        fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
-        fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
-        fd.scol = reinterpret_cast<const int64_t*>(base + o.scol);
-        fd.sval = reinterpret_cast<const double*>(base + o.sval);
-        fd.width = ax.stencil.width;
-    }
-    INTP_CUDA(cudaMalloc(&t->ctrl, static_cast<size_t>(m.total) * t->elem()), "cudaMalloc(control points)");
-    dv.ctrl = t->ctrl;
-    if (t->mixed() && m.dim <= 3) t->bins = make_bin_geom(dv, kTileBytes);
+    PackedTable pt;
+    pack_table(m, ar, pt);
+    INTP_CUDA(t->dmalloc(&t->arena, ar.host.size()), "cudaMalloc(table)");
+    t->arena_bytes = ar.host.size();
+    if (t->stream_ordered)
+        INTP_CUDA(cudaMemcpyAsync(t->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice, t->alloc_stream),
+                  "cudaMemcpyAsync(table)");
+    else
+        INTP_CUDA(cudaMemcpy(t->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice), "cudaMemcpy(table)");
+    bind_table(m, t->lo_user, pt, static_cast<const unsigned char*>(t->arena), t->dev, t->fac);
+    INTP_CUDA(t->dmalloc(&t->ctrl, static_cast<size_t>(m.total) * t->elem()), "cudaMalloc(control points)");
+    t->dev.ctrl = t->ctrl;
+    if (t->mixed() && m.dim <= 3) t->bins = make_bin_geom(t->dev, kTileBytes);
     return INTP_OK;
 }
 
 intp_status ensure_scratch(intp_table* t, size_t bytes) {
     if (t->scratch_bytes >= bytes) return INTP_OK;
-    if (t->scratch) cudaFree(t->scratch);
+    t->dfree(t->scratch);
     t->scratch = nullptr;
     t->scratch_bytes = 0;
-    INTP_CUDA(cudaMalloc(&t->scratch, bytes), "cudaMalloc(solve scratch)");
+    INTP_CUDA(t->dmalloc(&t->scratch, bytes), "cudaMalloc(solve scratch)");
     t->scratch_bytes = bytes;
     return INTP_OK;
 }
@@ -325,19 +216,6 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
     return cudaSuccess;
 }
 
-int auto_refine_steps(const TableModel& m) {
-    // The FP32 solve's relative error is about 6e-8 * sum_d kappa_d (kappa ~ 3
-    // per axis for cubic collocation, tens for periodic order >= 6). Each
-    // FP64-residual step squares that relative error, down to FP32 storage.
-    double e = fp32_solve_error_estimate(m);
-    int steps = 0;
-    while (e > 1e-6 && steps < 4) {
-        e = e * e + 6e-8;
-        ++steps;
-    }
-    return steps;
-}
-
 intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_t s) {
     const TableModel& m = t->model;
     const int64_t N = m.total;
@@ -390,46 +268,9 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
     return INTP_OK;
 }
 
-// Groups outputs by their derivative orders on axes 1..D-1.
-void group_plan(DerivPlan& plan, int dim) {
-    plan.ngroups = 0;
-    for (int k = 0; k < plan.k; ++k) {
-        int g = 0;
-        for (; g < plan.ngroups; ++g) {
-            bool same = true;
-            for (int d = 1; d < dim; ++d) same = same && plan.ord[plan.group_rep[g]][d] == plan.ord[k][d];
-            if (same) break;
-        }
-        if (g == plan.ngroups) plan.group_rep[plan.ngroups++] = static_cast<int8_t>(k);
-        plan.out_group[k] = static_cast<int8_t>(g);
-    }
-}
-
 bool make_plan(const intp_table* t, const int32_t* derivs, int32_t nderiv, DerivPlan& plan,
                std::string& err) {
-    std::memset(&plan, 0, sizeof plan);
-    if (!derivs) {
-        plan.k = 1;
-        group_plan(plan, t->model.dim);
-        return true;
-    }
-    if (nderiv < 1 || nderiv > kMaxDeriv) {
-        err = "nderiv must be in [1, 16]";
-        return false;
-    }
-    plan.k = nderiv;
-    for (int k = 0; k < nderiv; ++k)
-        for (int d = 0; d < t->model.dim; ++d) {
-            const int32_t v = derivs[k * t->model.dim + d];
-            if (v < 0) {
-                err = "derivative orders must be non-negative";
-                return false;
-            }
-            // any order above the spline order gives 0 (BSpline.hpp:404-407)
-            plan.ord[k][d] = static_cast<int8_t>(std::min<int32_t>(v, t->model.order + 1));
-        }
-    group_plan(plan, t->model.dim);
-    return true;
+    return build_deriv_plan(t->model.dim, t->model.order, derivs, nderiv, t->model.dim, plan, err);
 }
 
 // ---- fixed scratch of the allocation-free evaluation (intp_eval_noalloc) ----
@@ -461,16 +302,65 @@ intp_status noalloc_scratch_address(int dev, void** out) {
 }  // namespace
 
 namespace intp_gb300 {
-void note_launch(int count) { g_launches.fetch_add(static_cast<unsigned long long>(count)); }
-}  // namespace intp_gb300
 
-extern "C" {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
 
-const char* intp_last_error(void) { return g_last_error.c_str(); }
+// Groups outputs by their derivative orders on axes 1..D-1.
+void group_plan(DerivPlan& plan, int dim) {
+    plan.ngroups = 0;
+    for (int k = 0; k < plan.k; ++k) {
+        int g = 0;
+        for (; g < plan.ngroups; ++g) {
+            bool same = true;
+            for (int d = 1; d < dim; ++d) same = same && plan.ord[plan.group_rep[g]][d] == plan.ord[k][d];
+            if (same) break;
+        }
+        if (g == plan.ngroups) plan.group_rep[plan.ngroups++] = static_cast<int8_t>(k);
+        plan.out_group[k] = static_cast<int8_t>(g);
+    }
+}
 
-uint64_t intp_launch_count(void) { return g_launches.load(); }
+bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv, int row_stride, DerivPlan& plan,
+                      std::string& err) {
+    std::memset(&plan, 0, sizeof plan);
+    if (!derivs) {
+        plan.k = 1;
+        group_plan(plan, dim);
+        return true;
+    }
+    if (nderiv < 1 || nderiv > kMaxDeriv) {
+        err = "nderiv must be in [1, 16]";
+        return false;
+    }
+    plan.k = nderiv;
+    for (int k = 0; k < nderiv; ++k)
+        for (int d = 0; d < dim; ++d) {
+            const int32_t v = derivs[k * row_stride + d];
+            if (v < 0) {
+                err = "derivative orders must be non-negative";
+                return false;
+            }
+            // any order above the spline order gives 0 (BSpline.hpp:404-407)
+            plan.ord[k][d] = static_cast<int8_t>(std::min<int32_t>(v, order + 1));
+        }
+    group_plan(plan, dim);
+    return true;
+}
 
-intp_status intp_table_create(const intp_table_desc* desc, intp_table** out) {
+int auto_refine_steps(const TableModel& m) {
+    // The FP32 solve's relative error is about 6e-8 * sum_d kappa_d (kappa ~ 3
+    // per axis for cubic collocation, tens for periodic order >= 6). Each
+    // FP64-residual step squares that relative error, down to FP32 storage.
+    double e = fp32_solve_error_estimate(m);
+    int steps = 0;
+    while (e > 1e-6 && steps < 4) {
+        e = e * e + 6e-8;
+        ++steps;
+    }
+    return steps;
+}
+
+intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaStream_t stream, intp_table** out) {
     if (!desc || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
     if (desc->dim < 1 || desc->dim > INTP_GPU_MAX_DIM)
@@ -506,6 +396,8 @@ intp_status intp_table_create(const intp_table_desc* desc, intp_table** out) {
     }
     t->precision = desc->precision;
     t->refine_steps = desc->refine_steps;
+    t->stream_ordered = stream_ordered;
+    t->alloc_stream = stream;
     for (int d = 0; d < desc->dim; ++d) t->lo_user[d] = desc->range_lo[d];
     cudaGetDevice(&t->device);
     intp_status st = upload_table(t);
@@ -515,6 +407,150 @@ intp_status intp_table_create(const intp_table_desc* desc, intp_table** out) {
     }
     *out = t;
     return INTP_OK;
+}
+
+size_t table_device_bytes(const intp_table* t) {
+    return t->arena_bytes + static_cast<size_t>(t->model.total) * t->elem() + t->scratch_bytes;
+}
+
+size_t table_build_scratch_bytes(const intp_table_desc* desc) {
+    int64_t total = 1;
+    for (int d = 0; d < desc->dim && d < INTP_GPU_MAX_DIM; ++d) total *= desc->size[d];
+    // values staging (FP64) plus, in the mixed form, the refinement buffers
+    size_t b = static_cast<size_t>(total) * 8;
+    if (desc->precision == INTP_PRECISION_MIXED) b += static_cast<size_t>(total) * (8 * 3 + 4);
+    return b;
+}
+
+void table_release_scratch(intp_table* t) {
+    t->dfree(t->scratch);
+    t->scratch = nullptr;
+    t->scratch_bytes = 0;
+}
+
+int64_t table_values(const intp_table* t) { return t->model.total; }
+
+void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
+    const int O = m.order;
+    for (int d = 0; d < m.dim; ++d) {
+        const AxisModel& ax = m.axis[d];
+        const std::vector<double>& t0 = ax.knots;
+        const int64_t nk = static_cast<int64_t>(t0.size());
+        std::vector<long long> keys(nk);
+        std::vector<double> rinv(static_cast<size_t>(nk * std::max(O, 1)), 0.0);
+        std::vector<float> kdf(static_cast<size_t>(nk * (2 * O + 2)), 0.0f), khi(nk), klo(nk);
+        for (int64_t a = 0; a < nk; ++a) {
+            unsigned long long b;
+            std::memcpy(&b, &t0[a], 8);
+            keys[a] = knot_key_bits(b);
+            for (int s = 1; s <= O; ++s)
+                if (a + s < nk && t0[a + s] != t0[a]) rinv[a * O + (s - 1)] = 1.0 / (t0[a + s] - t0[a]);
+            for (int j = -O; j <= O + 1; ++j)
+                if (a + j >= 0 && a + j < nk) kdf[a * (2 * O + 2) + (j + O)] = static_cast<float>(t0[a + j] - t0[a]);
+            const uint32_t hb = split_hi_bits(b);
+            float hf;
+            std::memcpy(&hf, &hb, 4);
+            khi[a] = hf;
+            klo[a] = static_cast<float>(t0[a] - static_cast<double>(hf));
+        }
+        PackedTable::Axis& o = pt.ax[d];
+        o.knots = ar.put(t0);
+        o.keys = ar.put(keys);
+        o.rinv = ar.put(rinv);
+        o.rinvf = ar.put(to_f32(rinv));
+        o.kdf = ar.put(kdf);
+        o.khi = ar.put(khi);
+        o.klo = ar.put(klo);
+        const LineFactor& f = ax.factor;
+        o.lower = ar.put(f.lower);
+        o.upper = ar.put(f.upper);
+        o.dinv = ar.put(f.dinv);
+        o.bottom = ar.put(f.bottom);
+        o.right = ar.put(f.right);
+        o.lowerf = ar.put(to_f32(f.lower));
+        o.upperf = ar.put(to_f32(f.upper));
+        o.dinvf = ar.put(to_f32(f.dinv));
+        o.bottomf = ar.put(to_f32(f.bottom));
+        o.rightf = ar.put(to_f32(f.right));
+        o.scol = ar.put(ax.stencil.col);
+        o.sval = ar.put(ax.stencil.val);
+    }
+}
+
+void bind_table(const TableModel& m, const double* lo_user, const PackedTable& pt, const unsigned char* base,
+                TableDev& dv, AxisFactorDev* fac) {
+    const int O = m.order;
+    dv.dim = m.dim;
+    dv.order = O;
+    int64_t stride = 1;
+    for (int d = m.dim - 1; d >= 0; --d) {
+        const AxisModel& ax = m.axis[d];
+        AxisDev& a = dv.ax[d];
+        const PackedTable::Axis& o = pt.ax[d];
+        a.n = ax.n;
+        a.nknots = static_cast<int64_t>(ax.knots.size());
+        a.stride = stride;
+        stride *= ax.n;
+        a.periodic = ax.periodic ? 1 : 0;
+        a.uniform = ax.uniform ? 1 : 0;
+        a.lo = ax.range_lo;
+        a.hi = ax.range_hi;
+        a.period = ax.range_hi - ax.range_lo;
+        a.ncells = a.nknots - 2 * O - 1;  // spans O .. nknots-O-2
+        a.int_lo = 1;
+        a.int_hi = 0;
+        if (ax.uniform) {
+            const int64_t extra = ax.periodic ? 2 * O + (1 - O % 2) : O + 1;
+            a.hint_x0 = static_cast<float>(lo_user[d]);
+            a.hint_inv_dx = static_cast<float>(1.0 / ax.dx);
+            a.hint_off = static_cast<float>(0.5 * static_cast<double>(extra));
+            a.inv_dxf = static_cast<float>(1.0 / ax.dx);
+            // the basis at span c reads knots c-O+1 .. c+O; on a periodic axis
+            // all knots are uniform, on a non-periodic one knots O+1 ..
+            // nknots-O-2 are (the ends are clamped)
+            if (ax.periodic) {
+                a.int_lo = O;
+                a.int_hi = a.nknots - O - 2;
+            } else {
+                a.int_lo = 2 * O;
+                a.int_hi = a.nknots - 2 * O - 2;
+            }
+        }
+        a.knots = reinterpret_cast<const double*>(base + o.knots);
+        a.keys = reinterpret_cast<const long long*>(base + o.keys);
+        a.rinv = reinterpret_cast<const double*>(base + o.rinv);
+        a.rinvf = reinterpret_cast<const float*>(base + o.rinvf);
+        a.kdf = reinterpret_cast<const float*>(base + o.kdf);
+        a.khi = reinterpret_cast<const float*>(base + o.khi);
+        a.klo = reinterpret_cast<const float*>(base + o.klo);
+        AxisFactorDev& fd = fac[d];
+        fd.lower = reinterpret_cast<const double*>(base + o.lower);
+        fd.upper = reinterpret_cast<const double*>(base + o.upper);
+        fd.dinv = reinterpret_cast<const double*>(base + o.dinv);
+        fd.bottom = reinterpret_cast<const double*>(base + o.bottom);
+        fd.right = reinterpret_cast<const double*>(base + o.right);
+        fd.lowerf = reinterpret_cast<const float*>(base + o.lowerf);
+        fd.upperf = reinterpret_cast<const float*>(base + o.upperf);
+        fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
+        fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
+        fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
+        fd.scol = reinterpret_cast<const int64_t*>(base + o.scol);
+        fd.sval = reinterpret_cast<const double*>(base + o.sval);
+        fd.width = ax.stencil.width;
+    }
+}
+
+void note_launch(int count) { g_launches.fetch_add(static_cast<unsigned long long>(count)); }
+}  // namespace intp_gb300
+
+extern "C" {
+
+const char* intp_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t intp_launch_count(void) { return g_launches.load(); }
+
+intp_status intp_table_create(const intp_table_desc* desc, intp_table** out) {
+    return create_table(desc, false, nullptr, out);
 }
 
 intp_status intp_table_destroy(intp_table* table) {
@@ -773,13 +809,13 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     const int64_t m = g.nbuckets * kNoAllocSortBlocks;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    const size_t per_rec = static_cast<size_t>(8 + 4 * D);
-    if (fixed + 1024 * per_rec + 3 * 256 > kNoAllocScratchBytes)
+    const size_t per_rec = static_cast<size_t>(4 * (2 + D));
+    if (fixed + 1024 * per_rec + 256 > kNoAllocScratchBytes)
         return fail(INTP_ERR_INVALID_ARGUMENT,
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
                         ") for the 8 MiB scratch of the allocation-free evaluation; use intp_eval");
     if (npts == 0) return INTP_OK;
-    int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 3 * 256) / per_rec);
+    int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 256) / per_rec);
     cap &= ~int64_t{63};
     unsigned char* p = static_cast<unsigned char*>(base);
     uint32_t* blkcount = reinterpret_cast<uint32_t*>(p);
@@ -788,11 +824,7 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     p += up(static_cast<size_t>(m) * 4);
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    uint32_t* ridx = reinterpret_cast<uint32_t*>(p);
-    p += up(static_cast<size_t>(cap) * 4);
-    uint32_t* rcell = reinterpret_cast<uint32_t*>(p);
-    p += up(static_cast<size_t>(cap) * 4);
-    float* ru = reinterpret_cast<float*>(p);
+    uint32_t* rec = reinterpret_cast<uint32_t*>(p);
     // every word the kernels read is written earlier in the same chunk (counts
     // by the count kernel, offsets by the scan, records by the scatter), so
     // nothing in the area has to be cleared between calls
@@ -802,13 +834,13 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     for (int64_t p0 = 0; p0 < npts; p0 += cap) {
         const int64_t n = std::min(cap, npts - p0);
         INTP_CUDA(bin_sort_chunk(t->dev, g, coords + p0 * D, n, kNoAllocSortBlocks, blkcount, blkoffset, tile_sum,
-                                 ridx, rcell, ru, cap, s),
+                                 rec, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
-        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, ridx, rcell, ru, cap, n, plan,
-                                               o, out_f32, sms * 6, s)
-                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, ridx, rcell, ru, cap, n, plan,
-                                              o, out_f32, sms * 6, s),
+        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, rec, n, plan, o, out_f32,
+                                               sms * 2, s)
+                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, rec, n, plan, o, out_f32,
+                                              sms * 2, s),
                   "binned evaluation");
     }
     return INTP_OK;

@@ -102,124 +102,130 @@ __device__ __forceinline__ int64_t wrap_index(int64_t v, int64_t n, bool periodi
 
 constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
 
+// All outputs of one query point: xp holds its D coordinates, output k goes
+// to out[o0 + k]. Shared by the direct kernel and the batched-table kernel.
 template <int D, int O, bool MIXED>
-__global__ void __launch_bounds__(128) eval_direct_kernel(TableDev t, const double* __restrict__ coords,
-                                                          int64_t npts, DerivPlan plan,
-                                                          void* __restrict__ out, int out_f32) {
+__device__ __forceinline__ void eval_point(const TableDev& t, const double* __restrict__ xp, const DerivPlan& plan,
+                                           void* __restrict__ out, int out_f32, int64_t o0) {
     using R = typename std::conditional<MIXED, float, double>::type;
     constexpr int W = O + 1;
     constexpr int ROWS = ipow(W, D - 1);
     const R* __restrict__ cp = static_cast<const R*>(t.ctrl);
     const int K = plan.k;
-    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < npts;
-         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int64_t cell[D];
-        R xr[D];
-        R base[D][W];
-        int64_t off[D][W];
+    int64_t cell[D];
+    R xr[D];
+    R base[D][W];
+    int64_t off[D][W];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const AxisDev& a = t.ax[d];
-            double x = __ldg(coords + p * D + d);
-            if (a.periodic) x = periodic_wrap(a, x);
-            const int64_t h = a.uniform ? uniform_hint(a, x) : static_cast<int64_t>(O);
-            const int64_t c = locate_span(a, O, knot_key(x), h);
-            cell[d] = c;
-            if constexpr (MIXED) {
-                float xh, xl;
-                split_double(x, xh, xl);
-                const float u = (xh - __ldg(a.khi + c)) + (xl - __ldg(a.klo + c));
-                xr[d] = u;
-                axis_weights32<O>(a, c, u, 0, base[d]);
-            } else {
-                xr[d] = x;
-                Basis64<O>::eval(a, c, x, O, base[d]);
-            }
-#pragma unroll
-            for (int i = 0; i < W; ++i) off[d][i] = wrap_index(c - O + i, a.n, a.periodic) * a.stride;
-        }
+    for (int d = 0; d < D; ++d) {
+        const AxisDev& a = t.ax[d];
+        double x = __ldg(xp + d);
+        if (a.periodic) x = periodic_wrap(a, x);
+        const int64_t h = a.uniform ? uniform_hint(a, x) : static_cast<int64_t>(O);
+        const int64_t c = locate_span(a, O, knot_key(x), h);
+        cell[d] = c;
         if constexpr (MIXED) {
-            // same per-query code as the binned kernel (identical results)
-            const float cref = __ldg(cp + bucket_centre_offset<D, O>(t, cell));
-            const int64_t o0 = p * K;
-            mixed_point_outputs<D, O>(
-                t, plan, cell, xr, base, cref,
-                [&](const int (&ix)[D]) {
-                    int64_t o = 0;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) o += off[d][ix[d]];
-                    return __ldg(cp + o) - cref;
-                },
-                [out, out_f32, o0](int k, float v) {
-                    if (out_f32)
-                        static_cast<float*>(out)[o0 + k] = v;
-                    else
-                        static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
-                });
+            float xh, xl;
+            split_double(x, xh, xl);
+            const float u = (xh - __ldg(a.khi + c)) + (xl - __ldg(a.klo + c));
+            xr[d] = u;
+            axis_weights32<O>(a, c, u, 0, base[d]);
         } else {
-            for (int k = 0; k < K; ++k) {
-                R w[D][W];
-                bool zero = false;
+            xr[d] = x;
+            Basis64<O>::eval(a, c, x, O, base[d]);
+        }
 #pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    const int kd = plan.ord[k][d];
-                    if (kd > O) {
-                        zero = true;
-                    } else if (kd == 0) {
+        for (int i = 0; i < W; ++i) off[d][i] = wrap_index(c - O + i, a.n, a.periodic) * a.stride;
+    }
+    if constexpr (MIXED) {
+        // same per-query code as the binned kernel (identical results)
+        const float cref = __ldg(cp + bucket_centre_offset<D, O>(t, cell));
+        mixed_point_outputs<D, O>(
+            t, plan, cell, xr, base, cref,
+            [&](const int (&ix)[D]) {
+                int64_t o = 0;
 #pragma unroll
-                        for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
-                    } else {
-                        Basis64<O>::eval(t.ax[d], cell[d], xr[d], O - kd, w[d]);
-                        deriv_transform<O, R>(t.ax[d], cell[d], kd, w[d]);
-                    }
-                }
-                R acc = 0;
-                if (!zero) {
-                    if constexpr (ROWS <= 64) {
-#pragma unroll
-                        for (int r = 0; r < ROWS; ++r) {
-                            int64_t o = 0;
-                            R wr = 1;
-                            int rem = r;
-#pragma unroll
-                            for (int d = D - 2; d >= 0; --d) {
-                                const int i = rem % W;
-                                rem /= W;
-                                o += off[d][i];
-                                wr *= w[d][i];
-                            }
-                            R s = 0;
-#pragma unroll
-                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
-                            acc += wr * s;
-                        }
-                    } else {
-                        // large (O+1)^(D-1): runtime row loop, weights from local memory
-#pragma unroll 1
-                        for (int r = 0; r < ROWS; ++r) {
-                            int64_t o = 0;
-                            R wr = 1;
-                            int rem = r;
-                            for (int d = D - 2; d >= 0; --d) {
-                                const int i = rem % W;
-                                rem /= W;
-                                o += off[d][i];
-                                wr *= w[d][i];
-                            }
-                            R s = 0;
-#pragma unroll
-                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
-                            acc += wr * s;
-                        }
-                    }
-                }
+                for (int d = 0; d < D; ++d) o += off[d][ix[d]];
+                return __ldg(cp + o) - cref;
+            },
+            [out, out_f32, o0](int k, float v) {
                 if (out_f32)
-                    static_cast<float*>(out)[p * K + k] = static_cast<float>(acc);
+                    static_cast<float*>(out)[o0 + k] = v;
                 else
-                    static_cast<double*>(out)[p * K + k] = static_cast<double>(acc);
+                    static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
+            });
+    } else {
+        for (int k = 0; k < K; ++k) {
+            R w[D][W];
+            bool zero = false;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const int kd = plan.ord[k][d];
+                if (kd > O) {
+                    zero = true;
+                } else if (kd == 0) {
+#pragma unroll
+                    for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
+                } else {
+                    Basis64<O>::eval(t.ax[d], cell[d], xr[d], O - kd, w[d]);
+                    deriv_transform<O, R>(t.ax[d], cell[d], kd, w[d]);
+                }
             }
+            R acc = 0;
+            if (!zero) {
+                if constexpr (ROWS <= 64) {
+#pragma unroll
+                    for (int r = 0; r < ROWS; ++r) {
+                        int64_t o = 0;
+                        R wr = 1;
+                        int rem = r;
+#pragma unroll
+                        for (int d = D - 2; d >= 0; --d) {
+                            const int i = rem % W;
+                            rem /= W;
+                            o += off[d][i];
+                            wr *= w[d][i];
+                        }
+                        R s = 0;
+#pragma unroll
+                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
+                        acc += wr * s;
+                    }
+                } else {
+                    // large (O+1)^(D-1): runtime row loop, weights from local memory
+#pragma unroll 1
+                    for (int r = 0; r < ROWS; ++r) {
+                        int64_t o = 0;
+                        R wr = 1;
+                        int rem = r;
+                        for (int d = D - 2; d >= 0; --d) {
+                            const int i = rem % W;
+                            rem /= W;
+                            o += off[d][i];
+                            wr *= w[d][i];
+                        }
+                        R s = 0;
+#pragma unroll
+                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
+                        acc += wr * s;
+                    }
+                }
+            }
+            if (out_f32)
+                static_cast<float*>(out)[o0 + k] = static_cast<float>(acc);
+            else
+                static_cast<double*>(out)[o0 + k] = static_cast<double>(acc);
         }
     }
+}
+
+template <int D, int O, bool MIXED>
+__global__ void __launch_bounds__(128) eval_direct_kernel(TableDev t, const double* __restrict__ coords,
+                                                          int64_t npts, DerivPlan plan,
+                                                          void* __restrict__ out, int out_f32) {
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < npts;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        eval_point<D, O, MIXED>(t, coords + p * D, plan, out, out_f32, p * plan.k);
 }
 
 }  // namespace eval_detail

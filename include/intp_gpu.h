@@ -172,6 +172,48 @@ const char* intp_last_error(void);
  * (diagnostic; no counterpart in the reference). */
 uint64_t intp_launch_count(void);
 
+/* ---- batched tables ----
+ *
+ * Many independent tables (InterpolationFunction objects of uneven size,
+ * order, periodicity and dimension 1..3) built and evaluated together: one
+ * device arena for all knots and factors, one control-point array, and one
+ * launch per axis pass (solve) or per (dimension, order) class (evaluation)
+ * for the whole batch. The reference builds and evaluates such tables one
+ * object at a time; a batched table's control points and values are those of
+ * the same table built alone with intp_table_create/intp_table_interpolate
+ * and evaluated with intp_eval's direct kernel, bit for bit. */
+typedef struct intp_batch intp_batch;
+
+/* Knots and factors of ntables tables (descs[i], all of one precision) on the
+ * current device. Replaces ntables InterpolationFunctionTemplate
+ * constructions (InterpolationTemplate.hpp:60-79). */
+intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, intp_batch** out);
+intp_status intp_batch_destroy(intp_batch* batch);
+/* Number of tables and total number of mesh values (sum of prod(size)). */
+intp_status intp_batch_info(const intp_batch* batch, int64_t* ntables, int64_t* total_values);
+
+/* Solves the control points of every table. `values` holds each table's
+ * row-major value mesh, in table order (total_values doubles, host or device
+ * memory). Replaces InterpolationFunctionTemplate::interpolate
+ * (InterpolationTemplate.hpp:118-143) once per table. */
+intp_status intp_batch_build(intp_batch* batch, const double* values, int32_t values_on_device, void* stream);
+
+/* Control points of one table (prod(size) doubles, host memory).
+ * Replaces BSpline::control_points (BSpline.hpp:575-577). */
+intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table, double* ctrl_host);
+
+/* Evaluates every table at its own points. point_offsets (host memory,
+ * ntables + 1 entries, point_offsets[0] = 0) gives table i the points
+ * point_offsets[i] .. point_offsets[i+1]-1; coords (device memory) holds
+ * those points table after table, dim_i doubles per point. derivs (host
+ * memory): nderiv rows of INTP_GPU_MAX_DIM orders, of which a table of
+ * dimension D uses the first D, or NULL for the value only. out (device
+ * memory): point_offsets[ntables] x nderiv values of out_dtype.
+ * Replaces InterpolationFunction::operator() / derivative
+ * (Interpolation.hpp:132-146, :177-205) per table and point. */
+intp_status intp_batch_eval(const intp_batch* batch, const double* coords, const int64_t* point_offsets,
+                            const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype, void* stream);
+
 /* ---- standalone band LU (BandLU.hpp) ---- */
 
 /* Factors an n x n band matrix given in the reference's storage: band is

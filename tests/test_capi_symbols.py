@@ -55,6 +55,29 @@ def test_invalid_arguments_fail_cleanly(lib):
     assert lib.intp_launch_count() == 0
 
 
+def test_batch_rejects_invalid_tables_before_any_device_work(lib):
+    """intp_batch_create validates every descriptor on the host first."""
+    from bsplineinterpolation_gb300 import _lib
+    h = C.c_void_p()
+    descs = (_lib.TableDesc * 3)()
+    for d in descs:
+        d.dim, d.order, d.precision = 1, 3, _lib.PRECISION_MIXED
+        d.size[0] = 16
+        d.range_lo[0], d.range_hi[0] = 0.0, 1.0
+    assert lib.intp_batch_create(None, 3, C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.intp_batch_create(descs, 0, C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    descs[1].dim = 4  # batched tables have dimension 1..3
+    assert lib.intp_batch_create(descs, 3, C.byref(h)) == _lib.ERR_UNSUPPORTED
+    assert b"table 1" in lib.intp_last_error()
+    descs[1].dim = 1
+    descs[2].precision = _lib.PRECISION_FP64  # one precision per batch
+    assert lib.intp_batch_create(descs, 3, C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    descs[2].precision = _lib.PRECISION_MIXED
+    descs[0].size[0] = 2  # fewer samples than order + 1
+    assert lib.intp_batch_create(descs, 3, C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.intp_launch_count() == 0
+
+
 def test_product_never_loads_the_oracle():
     """The package imports nothing from oracle/ (it is test infrastructure)."""
     pkg = os.path.join(REPO, "bsplineinterpolation_gb300")
