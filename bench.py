@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-tables workload")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop workload")
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--batched-tables", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -354,6 +358,10 @@ def run_ours(args, rank, world):
 
     if rank == 0 and not args.no_e2e:
         result["e2e"] = e2e(args, f, vals, pts, lib, torch)
+    if rank == 0 and not args.no_batched:
+        result["batched"] = run_batched(args, torch)
+    if rank == 0 and not args.no_serve:
+        result["serving"] = run_serving(args, torch)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(npts, n, min(npts, 20_000_000))
     if dist:
@@ -402,6 +410,172 @@ def e2e(args, f, vals, pts, lib, torch):
 
 def _out_dtype(args):
     return 1 if args.precision == "mixed" else 0
+
+
+# ---------------------------------------------------------------------------
+# batched tables: 4096 independent tables in one batch
+# ---------------------------------------------------------------------------
+def _fourier(rng, n, periodic):
+    L = n if periodic else n - 1
+    x = np.arange(n, dtype=np.float64)
+    f = np.zeros(n)
+    for k in range(1, 9):
+        f += rng.normal(0.0, 1.0 / k) * np.cos(2 * np.pi * k * x / L + rng.uniform(0, 2 * np.pi))
+    return f
+
+
+def make_batched_workload(ntables, seed):
+    """Half 1D tables with N ~ U[16, 4096], half 2D with sides ~ U[16, 256];
+    orders 3 or 5; 30% periodic (all axes); 8-mode random Fourier values with
+    amplitudes ~ N(0, 1/k^2) (a product of two series in 2D); U[1e3, 1e5]
+    uniform query points per table."""
+    rng = np.random.default_rng(seed)
+    specs, values, counts = [], [], []
+    for i in range(ntables):
+        order = int(rng.choice([3, 5]))
+        periodic = bool(rng.random() < 0.3)
+        if i % 2 == 0:
+            dims = [int(rng.integers(16, 4097))]
+            v = _fourier(rng, dims[0], periodic)
+        else:
+            dims = [int(rng.integers(16, 257)), int(rng.integers(16, 257))]
+            v = np.outer(_fourier(rng, dims[0], periodic), _fourier(rng, dims[1], periodic))
+        specs.append((order, [periodic] * len(dims), dims, [(0.0, float(d)) for d in dims]))
+        values.append(v.ravel())
+        counts.append(int(rng.integers(1000, 100001)))
+    return specs, np.concatenate(values), np.asarray(counts, np.int64)
+
+
+def run_batched(args, torch, steps=5, warmup=3):
+    """Batched-tables workload: one build of every table and one evaluation
+    of every table's points per step (FP32 evaluation, FP32 solve with FP64
+    refinement), inputs resident in HBM; CUDA-event timing."""
+    import bsplineinterpolation_gb300 as bi
+    specs, values, counts = make_batched_workload(args.batched_tables, SEED + 2)
+    b = bi.TableBatch(specs, precision="mixed")
+    vals = torch.tensor(values, device="cuda")
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(SEED + 3)
+    dims = [len(sp[2]) for sp in specs]
+    parts = []
+    for i, sp in enumerate(specs):
+        scale = torch.tensor([float(d) for d in sp[2]], device="cuda", dtype=torch.float64)
+        parts.append((torch.rand((int(counts[i]), dims[i]), device="cuda", dtype=torch.float64,
+                                 generator=gen) * scale).reshape(-1))
+    coords = torch.cat(parts)
+    del parts
+    npts = int(offsets[-1])
+    out = torch.empty((npts, 1), device="cuda", dtype=torch.float32)
+    for _ in range(warmup):
+        b.build(vals)
+        b.evaluate(coords, offsets, out=out)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1, e2 in ev:
+        e0.record()
+        b.build(vals)
+        e1.record()
+        b.evaluate(coords, offsets, out=out)
+        e2.record()
+    torch.cuda.synchronize()
+    build_ms = float(np.median([a.elapsed_time(c) for a, c, _ in ev]))
+    eval_ms = float(np.median([c.elapsed_time(d) for _, c, d in ev]))
+    total_ms = ev[0][0].elapsed_time(ev[-1][2]) / steps
+    # accuracy of a sample of tables against the FP64 form of the same batch
+    b64 = bi.TableBatch(specs, precision="fp64")
+    b64.build(vals)
+    ref = b64.evaluate(coords, offsets, out_dtype="f64")
+    err = float(((out[:, 0].double() - ref[:, 0]).abs().max() / ref[:, 0].abs().max()).item())
+    return {"workload": "%d tables (half 1D N~U[16,4096], half 2D sides~U[16,256]; O in {3,5}; 30%% periodic),"
+                        " %d queries" % (len(specs), npts),
+            "points_per_s": npts / (total_ms / 1e3), "build_ms": build_ms, "eval_ms": eval_ms,
+            "eval_points_per_s": npts / (eval_ms / 1e3), "mesh_values": int(values.size),
+            "max_rel_err_vs_fp64": err, "steps": steps, "warmup": warmup}
+
+
+# ---------------------------------------------------------------------------
+# serving loop: Poisson arrivals of builds and evaluations
+# ---------------------------------------------------------------------------
+def run_serving(args, torch, rate=2000.0, seed=SEED + 4):
+    """Serving-loop workload: Poisson arrivals at `rate` requests/s for
+    --serve-seconds; 10% table builds (2D 32^2..1024^2 or 3D 64^3..256^3,
+    order 3 or 5, random periodicity, values exp(-r^2) cos(4x) + noise on
+    [-1, 1]^D), 90% evaluations of 1e3..1e7 log-uniform uniform points against
+    built tables; 150 GB memory budget with LRU eviction. Latency is measured
+    by the server from submission to completion on the device. Inputs come
+    from pinned host pools (a build's values and an evaluation's points are
+    slices of them)."""
+    import bsplineinterpolation_gb300 as bi
+    rng = np.random.default_rng(seed)
+    # pools: value meshes of a few sizes per class, points, outputs
+    def mesh(dims):
+        axes = np.meshgrid(*[np.linspace(-1.0, 1.0, d) for d in dims], indexing="ij")
+        r2 = sum(a * a for a in axes)
+        f = np.exp(-r2) * np.cos(4 * axes[0]) + rng.normal(0.0, 1e-3, dims)
+        return torch.from_numpy(f).pin_memory()
+    pool2 = [mesh([int(v), int(v)]) for v in (32, 128, 256, 512, 768, 1024)]
+    pool3 = [mesh([int(v)] * 3) for v in (64, 96, 128, 192, 256)]
+    max_pts = 10_000_000
+    pts3 = torch.from_numpy(rng.uniform(-1.0, 1.0, (max_pts, 3))).pin_memory()
+    pts2 = torch.from_numpy(np.ascontiguousarray(pts3.numpy()[:, :2])).pin_memory()
+    ring = torch.empty(1 << 28, dtype=torch.float32).pin_memory()  # output ring
+    srv = bi.Server(memory_budget=150 << 30, slots=8)
+    tables = []  # (table id, dim)
+
+    def submit_build():
+        if rng.random() < 0.5:
+            v = pool2[int(rng.integers(len(pool2)))]
+        else:
+            v = pool3[int(rng.integers(len(pool3)))]
+        D = v.dim()
+        per = [bool(rng.random() < 0.5) for _ in range(D)]
+        tid, rid = srv.submit_build(int(rng.choice([3, 5])), per, v, *[(-1.0, 1.0)] * D)
+        tables.append((tid, D))
+        return rid
+
+    ring_pos = [0]
+
+    def submit_eval():
+        tid, D = tables[int(rng.integers(max(0, len(tables) - 64), len(tables)))]
+        n = int(np.exp(rng.uniform(np.log(1e3), np.log(1e7))))
+        o = int(rng.integers(0, max_pts - n + 1))
+        p = (pts3 if D == 3 else pts2)[o:o + n]
+        if ring_pos[0] + n > ring.numel():
+            ring_pos[0] = 0
+        out = ring[ring_pos[0]:ring_pos[0] + n].view(n, 1)
+        ring_pos[0] += n
+        return srv.submit_eval(tid, p, out)
+
+    rids = [submit_build() for _ in range(16)]
+    for r in rids:
+        srv.wait(r, 300.0)
+    srv.reset_stats()
+    rids = []
+    t0 = time.perf_counter()
+    t_next = t0
+    while True:
+        t_next += rng.exponential(1.0 / rate)
+        if t_next - t0 > args.serve_seconds:
+            break
+        now = time.perf_counter()
+        if t_next > now:
+            time.sleep(t_next - now)
+        rids.append(submit_build() if rng.random() < 0.1 else submit_eval())
+    statuses = [srv.wait(r, 600.0) for r in rids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"workload": "Poisson %.0f req/s for %.0f s: 10%% builds (2D 32^2-1024^2 / 3D 64^3-256^3, O 3|5),"
+                        " 90%% evals of 1e3-1e7 points; 150 GB budget, 8 slots" % (rate, args.serve_seconds),
+            "requests": len(rids), "failed": int(sum(1 for x in statuses if x != 0)),
+            "p50_ms": st["all_p50_ms"], "p99_ms": st["all_p99_ms"],
+            "eval_p50_ms": st["eval_p50_ms"], "eval_p99_ms": st["eval_p99_ms"],
+            "build_p50_ms": st["build_p50_ms"], "build_p99_ms": st["build_p99_ms"],
+            "points_per_s": st["points_per_s"], "points": st["points_evaluated"],
+            "merged_units": st["merged_units"], "evictions": st["evictions"],
+            "served_points_per_wall_s": st["points_evaluated"] / max(wall, 1e-9)}
 
 
 def run_reference(args, rank, world):

@@ -26,6 +26,7 @@ __all__ = [
     "InterpolationFunctionTemplate1D",
     "BandLU",
     "TableBatch",
+    "Server",
     "IntpError",
     "IntpDomainError",
 ]
@@ -511,3 +512,95 @@ class TableBatch:
         _lib.check(lib.intp_batch_eval(self._h, C.c_void_p(x.data_ptr()), po.ctypes.data, kp, K,
                                        C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
         return out
+
+
+class Server:
+    """Serving loop (intp_server_*): tables stay resident on the device, build
+    and evaluate requests run with continuous batching under a memory budget.
+
+    Submissions return request ids at once; `wait` blocks for one. Buffers
+    given to a submission (values, points, outputs) must stay alive and
+    unchanged until its wait returns; pinned host tensors or CUDA tensors let
+    the copies overlap. Table states: "queued", "resident", "gone" (evicted or
+    released), "failed".
+    """
+
+    STATES = {0: "queued", 1: "resident", 2: "gone", 3: "failed"}
+
+    def __init__(self, memory_budget=0, slots=0, max_batch_points=0):
+        lib = _lib.load()
+        cfg = _lib.ServerConfig()
+        cfg.memory_budget = int(memory_budget)
+        cfg.slots = int(slots)
+        cfg.max_batch_points = int(max_batch_points)
+        h = C.c_void_p()
+        _lib.check(lib.intp_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_server_destroy(h)
+            self._h = None
+        self._keep = {}
+
+    def __del__(self):
+        self.close()
+
+    @staticmethod
+    def _ptr(x):
+        if _is_cuda_tensor(x) or (_torch() is not None and isinstance(x, _torch().Tensor)):
+            return C.c_void_p(x.data_ptr())
+        return C.c_void_p(x.ctypes.data)
+
+    def submit_build(self, order, periodicity, values, *x_ranges, precision="mixed", refine_steps=-1):
+        """Queues a table build from `values` (mesh, host array or tensor);
+        returns (table_id, request_id)."""
+        dims = list(values.shape)
+        desc, keep, _, _ = _make_desc(order, periodicity, dims, x_ranges, precision, refine_steps)
+        tid, rid = C.c_int64(), C.c_int64()
+        _lib.check(_lib.load().intp_server_submit_build(self._h, C.byref(desc), self._ptr(values),
+                                                       C.byref(tid), C.byref(rid)))
+        self._keep[rid.value] = (values, keep)
+        return tid.value, rid.value
+
+    def submit_eval(self, table_id, points, out, derivs=None, out_dtype="f32"):
+        """Queues an evaluation of `points` (N x D) into `out` (N x K);
+        returns the request id."""
+        od = _lib.F32 if out_dtype == "f32" else _lib.F64
+        if derivs is None:
+            kp, K, karr = None, 1, None
+        else:
+            karr = np.ascontiguousarray(np.asarray(derivs, np.int32))
+            K = karr.shape[0]
+            kp = karr.ctypes.data
+        rid = C.c_int64()
+        _lib.check(_lib.load().intp_server_submit_eval(self._h, int(table_id), self._ptr(points),
+                                                      int(points.shape[0]), kp, K, self._ptr(out), od,
+                                                      C.byref(rid)))
+        self._keep[rid.value] = (points, out, karr)
+        return rid.value
+
+    def wait(self, request_id, timeout=-1.0):
+        """Status of a finished request (0 = OK); raises IntpError on a timeout."""
+        st = C.c_int()
+        _lib.check(_lib.load().intp_server_wait(self._h, int(request_id), float(timeout), C.byref(st)))
+        self._keep.pop(request_id, None)
+        return st.value
+
+    def release(self, table_id):
+        _lib.check(_lib.load().intp_server_release(self._h, int(table_id)))
+
+    def table_state(self, table_id):
+        v = C.c_int32()
+        _lib.check(_lib.load().intp_server_table_state(self._h, int(table_id), C.byref(v)))
+        return self.STATES[v.value]
+
+    def stats(self):
+        st = _lib.ServerStats()
+        _lib.check(_lib.load().intp_server_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def reset_stats(self):
+        _lib.check(_lib.load().intp_server_reset_stats(self._h))

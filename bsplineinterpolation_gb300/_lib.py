@@ -44,6 +44,26 @@ class TableDesc(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("memory_budget", C.c_uint64),
+        ("slots", C.c_int32),
+        ("pad_", C.c_int32),
+        ("max_batch_points", C.c_int64),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("builds_done", "evals_done", "failed", "evictions", "merged_units",
+                                         "resident_tables")] + \
+               [(n, C.c_uint64) for n in ("resident_bytes", "inflight_bytes")] + \
+               [(n, C.c_double) for n in ("points_evaluated", "build_p50_ms", "build_p99_ms", "eval_p50_ms",
+                                          "eval_p99_ms", "all_p50_ms", "all_p99_ms", "points_per_s")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class IntpError(RuntimeError):
     """Failure reported by the CUDA library (status code and message)."""
 
@@ -85,6 +105,17 @@ SIGNATURES = {
     "intp_batch_build": (C.c_int, [_P, _P, C.c_int32, _P]),
     "intp_batch_get_control_points": (C.c_int, [_P, C.c_int64, _P]),
     "intp_batch_eval": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "intp_server_destroy": (C.c_int, [_P]),
+    "intp_server_submit_build": (C.c_int, [_P, C.POINTER(TableDesc), _P, C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int64)]),
+    "intp_server_submit_eval": (C.c_int, [_P, C.c_int64, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32,
+                                          C.POINTER(C.c_int64)]),
+    "intp_server_wait": (C.c_int, [_P, C.c_int64, C.c_double, C.POINTER(C.c_int)]),
+    "intp_server_release": (C.c_int, [_P, C.c_int64]),
+    "intp_server_table_state": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32)]),
+    "intp_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "intp_server_reset_stats": (C.c_int, [_P]),
 }
 
 _lib = None

@@ -105,19 +105,19 @@ int sm_count() {
 
 template <int D>
 cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec, cudaStream_t s) {
+                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec, uint32_t* rec,
+                        int64_t slice, cudaStream_t s) {
     using namespace bin_detail;
-    const int64_t slice = (n + nblk - 1) / nblk;
     const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
-    auto kc = count_kernel<D>;
-    auto ks = scatter_kernel<D>;
+    auto kl = locate_kernel<D>;
+    auto kp = permute_kernel<D>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t e = cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            e = cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    kc<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkcount);
+    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, blkcount);
     note_launch();
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -127,20 +127,26 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, rec);
+    kp<<<nblk, kSortThreads, smem, s>>>(g, n, slice, in_rec, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }
 
 }  // namespace
 
+int bin_record_words(int dim) { return dim == 1 ? bin_detail::rec_words<1>() : bin_detail::rec_words<2>(); }
+
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec,
-                           cudaStream_t s) {
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
+                           uint32_t* rec, int64_t* slice, cudaStream_t s) {
+    if (nblk < 1 || nblk > bin_detail::kMaxSortBlocks) return cudaErrorInvalidValue;
+    const int64_t sl = (n + nblk - 1) / nblk;
+    if (sl >= bin_detail::kMaxSlice) return cudaErrorInvalidValue;
+    *slice = sl;
     switch (t.dim) {
-        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
-        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
-        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
+        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
+        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
+        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -167,7 +173,11 @@ BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
         g.nbuckets *= g.nb[d];
     }
     g.tile_elems = stride;
-    g.smem_buckets = g.nbuckets <= kSmemBucketLimit ? static_cast<int32_t>(g.nbuckets) : 0;
+    // the binned kernels index spans with 32 bits and keep the bucket in the
+    // 20 high bits of a record's tag word
+    bool small = g.nbuckets <= kSmemBucketLimit;
+    for (int d = 0; d < D; ++d) small = small && t.ax[d].nknots < (int64_t{1} << 30);
+    g.smem_buckets = small ? static_cast<int32_t>(g.nbuckets) : 0;
     return g;
 }
 
@@ -183,8 +193,8 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     if (ntiles > bin_detail::kScanThreads * bin_detail::kScanItems) return cudaErrorInvalidValue;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t b_m = up(static_cast<size_t>(m) * 4), b_t = up(static_cast<size_t>(ntiles) * 4);
-    const size_t b_r = up(static_cast<size_t>(cap) * 4 * (2 + D));
-    const size_t total = b_m * 2 + b_t + b_r;
+    const size_t b_r = up(static_cast<size_t>(cap) * 4 * bin_record_words(D));
+    const size_t total = b_m * 2 + b_t + b_r * 2;
     void* mem = nullptr;
     cudaError_t e = cudaMallocAsync(&mem, total, s);
     if (e != cudaSuccess) return e;
@@ -195,6 +205,8 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     p += b_m;
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += b_t;
+    uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
+    p += b_r;
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
     const int K = plan.k;
     const size_t ob = out_f32 ? 4 : 8;
@@ -202,11 +214,12 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
     for (int64_t p0 = 0; p0 < npts && e == cudaSuccess; p0 += cap) {
         const int64_t n = std::min(cap, npts - p0);
         const double* c = coords + p0 * D;
-        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, rec, s);
+        int64_t slice = 0;
+        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, &slice, s);
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
-        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, rec, n, plan, o, out_f32, grid_eval, s)
-                   : launch_bin_eval_d3(t, g, blkoffset, nblk, rec, n, plan, o, out_f32, grid_eval, s);
+        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s)
+                   : launch_bin_eval_d3(t, g, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s);
     }
     cudaError_t e2 = cudaFreeAsync(mem, s);
     return e != cudaSuccess ? e : e2;

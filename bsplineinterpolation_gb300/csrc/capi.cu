@@ -26,7 +26,7 @@ std::atomic<unsigned long long> g_launches{0};
 // binned evaluation: shared-memory tile budget per CTA, queries per chunk
 // (chunk outputs stay L2-resident), smallest batch worth binning
 constexpr int64_t kTileBytes = 48 * 1024;
-constexpr int64_t kDefaultChunk = int64_t{1} << 23;
+constexpr int64_t kDefaultChunk = int64_t{1} << 24;
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
 // INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
@@ -318,6 +318,9 @@ void group_plan(DerivPlan& plan, int dim) {
         if (g == plan.ngroups) plan.group_rep[plan.ngroups++] = static_cast<int8_t>(k);
         plan.out_group[k] = static_cast<int8_t>(g);
     }
+    plan.simple = plan.ngroups == 1 ? 1 : 0;
+    for (int d = 1; d < dim && plan.simple; ++d)
+        if (plan.ord[plan.group_rep[0]][d] != 0) plan.simple = 0;
 }
 
 bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv, int row_stride, DerivPlan& plan,
@@ -660,28 +663,107 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     if (npts == 0) return INTP_OK;
     if (!coords || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int D = t->model.dim;
     const int K = derivs ? nderiv : 1;
-    const size_t cb = static_cast<size_t>(npts) * t->model.dim * 8;
-    const size_t ob = static_cast<size_t>(npts) * K * (out_dtype == INTP_F32 ? 4 : 8);
-    void *dc = nullptr, *dout = nullptr;
-    INTP_CUDA(cudaMallocAsync(&dc, cb, s), "cudaMallocAsync(coords)");
-    cudaError_t e = cudaMallocAsync(&dout, ob, s);
-    if (e != cudaSuccess) {
+    const size_t osz = out_dtype == INTP_F32 ? 4 : 8;
+    const int64_t chunk = eval_chunk();
+    if (npts <= chunk) {
+        const size_t cb = static_cast<size_t>(npts) * D * 8;
+        const size_t ob = static_cast<size_t>(npts) * K * osz;
+        void *dc = nullptr, *dout = nullptr;
+        INTP_CUDA(cudaMallocAsync(&dc, cb, s), "cudaMallocAsync(coords)");
+        cudaError_t e = cudaMallocAsync(&dout, ob, s);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(dc, s);
+            return cuda_fail(e, "cudaMallocAsync(out)");
+        }
+        intp_status st = INTP_OK;
+        e = cudaMemcpyAsync(dc, coords, cb, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(coords)");
+        if (st == INTP_OK) st = intp_eval(t, static_cast<double*>(dc), npts, derivs, nderiv, dout, out_dtype, stream);
+        if (st == INTP_OK) {
+            e = cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(out)");
+        }
         cudaFreeAsync(dc, s);
-        return cuda_fail(e, "cudaMallocAsync(out)");
+        cudaFreeAsync(dout, s);
+        e = cudaStreamSynchronize(s);
+        if (st == INTP_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
+        return st;
     }
-    intp_status st = INTP_OK;
-    e = cudaMemcpyAsync(dc, coords, cb, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(coords)");
-    if (st == INTP_OK) st = intp_eval(t, static_cast<double*>(dc), npts, derivs, nderiv, dout, out_dtype, stream);
+    // Several chunks: the copy of chunk i+1 in and of chunk i-1 out overlap
+    // the evaluation of chunk i (separate copy streams, two device buffers).
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t start = nullptr, in_ready[2] = {}, done[2] = {}, freed[2] = {};
+    void* din[2] = {};
+    void* dout[2] = {};
+    const size_t cb = static_cast<size_t>(chunk) * D * 8, ob = static_cast<size_t>(chunk) * K * osz;
+    cudaError_t e = cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+        e = cudaEventCreateWithFlags(&in_ready[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&freed[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMallocAsync(&din[j], cb, s);
+        if (e == cudaSuccess) e = cudaMallocAsync(&dout[j], ob, s);
+    }
+    intp_status st = e == cudaSuccess ? INTP_OK : cuda_fail(e, "pipelined evaluation set-up");
     if (st == INTP_OK) {
-        e = cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(out)");
+        // the copy streams start after the caller's earlier work (and the buffers' allocation)
+        e = cudaEventRecord(start, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h2d, start, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(d2h, start, 0);
+        if (e != cudaSuccess) st = cuda_fail(e, "pipelined evaluation set-up");
     }
-    cudaFreeAsync(dc, s);
-    cudaFreeAsync(dout, s);
+    int64_t i = 0;
+    for (int64_t p0 = 0; p0 < npts && st == INTP_OK; p0 += chunk, ++i) {
+        const int j = static_cast<int>(i & 1);
+        const int64_t n = std::min(chunk, npts - p0);
+        if (i >= 2) e = cudaStreamWaitEvent(h2d, freed[j], 0);  // chunk i-2 copied out of buffer j
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(din[j], coords + p0 * D, static_cast<size_t>(n) * D * 8, cudaMemcpyHostToDevice, h2d);
+        if (e == cudaSuccess) e = cudaEventRecord(in_ready[j], h2d);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, in_ready[j], 0);
+        if (e != cudaSuccess) {
+            st = cuda_fail(e, "pipelined evaluation (copy in)");
+            break;
+        }
+        st = intp_eval(t, static_cast<double*>(din[j]), n, derivs, nderiv, dout[j], out_dtype, stream);
+        if (st != INTP_OK) break;
+        e = cudaEventRecord(done[j], s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(d2h, done[j], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * osz, dout[j],
+                                static_cast<size_t>(n) * K * osz, cudaMemcpyDeviceToHost, d2h);
+        if (e == cudaSuccess) e = cudaEventRecord(freed[j], d2h);
+        if (e != cudaSuccess) st = cuda_fail(e, "pipelined evaluation (copy out)");
+    }
+    // the caller's stream resumes after the last copy out; then release
+    if (d2h) {
+        cudaEvent_t fin = nullptr;
+        if (cudaEventCreateWithFlags(&fin, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(fin, d2h);
+            cudaStreamWaitEvent(s, fin, 0);
+            cudaEventDestroy(fin);
+        }
+    }
+    for (int j = 0; j < 2; ++j) {
+        if (din[j]) cudaFreeAsync(din[j], s);
+        if (dout[j]) cudaFreeAsync(dout[j], s);
+    }
     e = cudaStreamSynchronize(s);
     if (st == INTP_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
+    if (h2d) cudaStreamSynchronize(h2d);
+    if (d2h) cudaStreamSynchronize(d2h);
+    for (int j = 0; j < 2; ++j) {
+        if (in_ready[j]) cudaEventDestroy(in_ready[j]);
+        if (done[j]) cudaEventDestroy(done[j]);
+        if (freed[j]) cudaEventDestroy(freed[j]);
+    }
+    if (start) cudaEventDestroy(start);
+    if (h2d) cudaStreamDestroy(h2d);
+    if (d2h) cudaStreamDestroy(d2h);
     return st;
 }
 
@@ -809,13 +891,14 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     const int64_t m = g.nbuckets * kNoAllocSortBlocks;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    const size_t per_rec = static_cast<size_t>(4 * (2 + D));
-    if (fixed + 1024 * per_rec + 256 > kNoAllocScratchBytes)
+    // two records per query in flight: in input order and in bucket order
+    const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D)) * 2;
+    if (fixed + 1024 * per_rec + 512 > kNoAllocScratchBytes)
         return fail(INTP_ERR_INVALID_ARGUMENT,
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
                         ") for the 8 MiB scratch of the allocation-free evaluation; use intp_eval");
     if (npts == 0) return INTP_OK;
-    int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 256) / per_rec);
+    int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 512) / per_rec);
     cap &= ~int64_t{63};
     unsigned char* p = static_cast<unsigned char*>(base);
     uint32_t* blkcount = reinterpret_cast<uint32_t*>(p);
@@ -824,23 +907,26 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     p += up(static_cast<size_t>(m) * 4);
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += up(static_cast<size_t>((m + 4095) / 4096) * 4);
+    uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
+    p += up(static_cast<size_t>(cap) * per_rec / 2);
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
     // every word the kernels read is written earlier in the same chunk (counts
-    // by the count kernel, offsets by the scan, records by the scatter), so
-    // nothing in the area has to be cleared between calls
+    // by the locate kernel, offsets by the scan, records by locate and
+    // permute), so nothing in the area has to be cleared between calls
     int sms = 1;
     INTP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     const size_t ob = out_f32 ? 4 : 8;
     for (int64_t p0 = 0; p0 < npts; p0 += cap) {
         const int64_t n = std::min(cap, npts - p0);
+        int64_t slice = 0;
         INTP_CUDA(bin_sort_chunk(t->dev, g, coords + p0 * D, n, kNoAllocSortBlocks, blkcount, blkoffset, tile_sum,
-                                 rec, s),
+                                 in_rec, rec, &slice, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
-        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, rec, n, plan, o, out_f32,
-                                               sms * 2, s)
-                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, rec, n, plan, o, out_f32,
-                                              sms * 2, s),
+        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
+                                               out_f32, sms * 2, s)
+                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
+                                              out_f32, sms * 2, s),
                   "binned evaluation");
     }
     return INTP_OK;

@@ -71,6 +71,7 @@ struct DerivPlan {
     int32_t ngroups;
     int8_t group_rep[kMaxDeriv];    // an output of each group
     int8_t out_group[kMaxDeriv];    // group of each output
+    int32_t simple;                 // one group, all orders on axes 1..D-1 zero
 };
 
 // Spans per bucket (log2, per axis) of the binned evaluation, fixed per
@@ -170,6 +171,41 @@ __device__ __forceinline__ int64_t locate_span(const AxisDev& a, int order, long
             hi = mid;
     }
     return lo - 1;
+}
+
+// locate_span with 32-bit indices (axes of fewer than 2^31 knots): the same
+// verified-hint search, so the same span.
+__device__ __forceinline__ int locate_span32(const AxisDev& a, int order, long long kx, int hint) {
+    const int lastc = static_cast<int>(a.nknots) - order - 2;
+    const int h = hint < order ? order : (hint > lastc ? lastc : hint);
+    const long long k0 = __ldg(a.keys + h), k1 = __ldg(a.keys + h + 1);
+    const bool lo_ok = (h == order) || (k0 <= kx);
+    const bool hi_ok = (h == lastc) || (kx < k1);
+    if (lo_ok && hi_ok) return h;
+    if (!hi_ok && h + 1 <= lastc) {
+        if (h + 1 == lastc || kx < __ldg(a.keys + h + 2)) return h + 1;
+    }
+    if (!lo_ok && h - 1 >= order) {
+        if (h - 1 == order || __ldg(a.keys + h - 1) <= kx) return h - 1;
+    }
+    int lo = order + 1, hi = lastc + 1;
+    while (lo < hi) {
+        const int mid = lo + ((hi - lo) >> 1);
+        if (__ldg(a.keys + mid) <= kx)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo - 1;
+}
+
+// uniform_hint as a 32-bit index, clamped to [-1, nknots].
+__device__ __forceinline__ int uniform_hint32(const AxisDev& a, float xf) {
+    float v = floorf((xf - a.hint_x0) * a.hint_inv_dx + a.hint_off);
+    if (!(v > -1.0f)) v = -1.0f;  // also NaN
+    const float top = static_cast<float>(a.nknots);
+    if (v > top) v = top;
+    return static_cast<int>(v);
 }
 
 // FP32 hint of the span on a uniform axis (integer-derived float of x).

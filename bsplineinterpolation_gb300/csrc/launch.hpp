@@ -27,15 +27,18 @@ cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coor
 cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
                             const DerivPlan& plan, void* out, bool out_f32, int64_t chunk, cudaStream_t s);
 // One chunk's counting sort by bucket into caller-provided scratch: blkcount
-// and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096), rec
-// cap records of D + 2 words ({u_0..u_{D-1}, packed local span, index}).
+// and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096);
+// in_rec and rec hold n records of bin_record_words(D) words each (queries
+// in input order, then in bucket order). Needs n <= nblk * 2^20. Returns the
+// slice of input queries each sort CTA took (for the evaluation).
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec,
-                           cudaStream_t s);
-cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk,
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
+                           uint32_t* rec, int64_t* slice, cudaStream_t s);
+int bin_record_words(int dim);
+cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk, int64_t slice,
                                 const uint32_t* rec, int64_t n, const DerivPlan&, void* out, bool out_f32,
                                 int grid, cudaStream_t);
-cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk,
+cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk, int64_t slice,
                                const uint32_t* rec, int64_t n, const DerivPlan&, void* out, bool out_f32,
                                int grid, cudaStream_t);
 // Bucket geometry for a table (tile of at most `tile_bytes` FP32 control points).

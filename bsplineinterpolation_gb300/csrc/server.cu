@@ -1,0 +1,647 @@
+// Serving loop: one worker thread keeps built tables resident in HBM and runs
+// table-build and evaluate requests of mixed sizes with continuous batching.
+//
+// Requests are submitted from any host thread and return at once with a
+// request id. The worker admits queued requests whenever a slot (a CUDA
+// stream with its completion event) and device memory are free:
+//   - a build creates the table with stream-ordered allocations on the slot's
+//     stream, copies the values in and solves the control points;
+//   - evaluations queued against the same table (same derivative request and
+//     output type) are merged into one work unit: their coordinates are copied
+//     into one device buffer, evaluated by one intp_eval, and each request's
+//     results are copied back to its own host buffer.
+// Work units on different slots overlap on the device; requests that arrive
+// while others run are admitted as soon as a slot and memory free up, without
+// waiting for the running ones to drain.
+//
+// Memory: resident tables plus the transient bytes of the work in flight stay
+// within the configured budget. A unit that does not fit evicts the least
+// recently used resident tables that no queued or running request refers to;
+// when that is not enough it waits for running units to finish, and fails
+// with INTP_ERR_BUDGET when it could never fit.
+//
+// Latency of a request is measured from its submission to the completion of
+// its work unit on the device; the stats report p50/p99 and points per second.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "intp_gpu.h"
+#include "table_internal.hpp"
+#include "table_pack.hpp"
+
+using namespace intp_gb300;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr int kMaxSlots = 64;
+constexpr uint64_t kDefaultBudget = uint64_t{150} << 30;
+constexpr int64_t kDefaultMaxBatchPoints = int64_t{1} << 24;
+// transient bytes of the binned evaluation (batches of at least
+// kBinnedPoints queries): sort records per query plus an allowance for the
+// per-bucket bookkeeping
+constexpr size_t kEvalScratchPerPoint = 20;
+constexpr size_t kEvalScratchFixed = size_t{16} << 20;
+constexpr int64_t kBinnedPoints = int64_t{1} << 18;
+
+size_t eval_reserve(int64_t npts, size_t per_point) {
+    return static_cast<size_t>(npts) * per_point + (npts >= kBinnedPoints ? kEvalScratchFixed : 0);
+}
+
+enum TableState : int32_t { kQueued = 0, kResident = 1, kGone = 2, kFailed = 3 };
+
+struct Request {
+    int64_t id = 0;
+    bool build = false;
+    int64_t table = 0;
+    // build
+    intp_table_desc desc{};
+    std::vector<double> axis_coords[INTP_GPU_MAX_DIM];  // non-uniform axes, copied at submission
+    const double* values = nullptr;
+    // evaluation
+    const double* coords = nullptr;
+    int64_t npts = 0;
+    std::vector<int32_t> derivs;
+    int32_t nderiv = 0;
+    void* out = nullptr;
+    int32_t out_dtype = INTP_F32;
+    // result
+    Clock::time_point t_submit;
+    intp_status status = INTP_OK;
+    std::string error;
+    bool done = false;
+};
+
+struct Table {
+    intp_table* t = nullptr;
+    int32_t state = kQueued;
+    int dim = 0;
+    int refs = 0;           // queued or running requests that use the table
+    bool release = false;   // drop once refs reaches 0
+    size_t bytes = 0;       // device bytes while resident
+    uint64_t last_use = 0;  // LRU clock
+};
+
+struct Unit {
+    bool build = false;
+    std::vector<Request*> reqs;
+    int64_t table = 0;
+    size_t reserve = 0;  // transient device bytes counted while in flight
+    int64_t npts = 0;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    Unit unit;
+};
+
+double ms_since(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+double percentile(std::vector<double> v, double q) {
+    if (v.empty()) return 0.0;
+    const size_t k = static_cast<size_t>(q * static_cast<double>(v.size() - 1) + 0.5);
+    std::nth_element(v.begin(), v.begin() + static_cast<std::ptrdiff_t>(k), v.end());
+    return v[k];
+}
+
+}  // namespace
+
+struct intp_server {
+    int device = 0;
+    uint64_t budget = kDefaultBudget;
+    int64_t max_batch_points = kDefaultMaxBatchPoints;
+    std::vector<Slot> slots;
+
+    std::mutex mu;
+    std::condition_variable cv_work;  // worker: new requests or stop
+    std::condition_variable cv_done;  // waiters: a request completed
+    bool stop = false;
+    std::thread worker;
+
+    int64_t next_request = 1;
+    int64_t next_table = 1;
+    std::list<Request*> pending;                        // submitted, not admitted
+    std::unordered_map<int64_t, Request*> requests;     // every request not yet waited on
+    std::unordered_map<int64_t, Table> tables;
+    uint64_t lru_clock = 0;
+    uint64_t resident_bytes = 0;
+    uint64_t inflight_bytes = 0;
+
+    // statistics since the last reset
+    std::vector<double> lat_build, lat_eval;
+    double points = 0;
+    int64_t failed = 0, evictions = 0, merged_units = 0;
+    Clock::time_point t_reset = Clock::now(), t_last = Clock::now();
+
+    ~intp_server();
+    void run();
+    void finish_slot(Slot& s, cudaError_t e);
+    bool admit(Slot& s, std::unique_lock<std::mutex>& lock);
+    bool make_room(size_t need);
+    void fail_request(Request* r, intp_status st, const std::string& msg);
+    void complete(Request* r, intp_status st, const std::string& msg, Clock::time_point now);
+    void drop_table(int64_t id, Table& tb);
+};
+
+namespace {
+
+bool same_request_shape(const Request* a, const Request* b) {
+    return a->table == b->table && a->out_dtype == b->out_dtype && a->nderiv == b->nderiv && a->derivs == b->derivs;
+}
+
+}  // namespace
+
+void intp_server::complete(Request* r, intp_status st, const std::string& msg, Clock::time_point now) {
+    r->status = st;
+    r->error = msg;
+    r->done = true;
+    cv_done.notify_all();  // waiters re-check under the lock the worker holds
+    if (st == INTP_OK) {
+        (r->build ? lat_build : lat_eval).push_back(ms_since(r->t_submit, now));
+        if (!r->build) points += static_cast<double>(r->npts);
+        t_last = now;
+    } else {
+        ++failed;
+    }
+    if (!r->build) {
+        auto it = tables.find(r->table);
+        if (it != tables.end()) {
+            it->second.refs--;
+            it->second.last_use = ++lru_clock;
+            if (it->second.release && it->second.refs == 0) drop_table(it->first, it->second);
+        }
+    }
+}
+
+void intp_server::fail_request(Request* r, intp_status st, const std::string& msg) {
+    complete(r, st, msg, Clock::now());
+}
+
+void intp_server::drop_table(int64_t id, Table& tb) {
+    (void)id;
+    if (tb.t) {
+        intp_table_destroy(tb.t);  // stream-ordered frees on the table's build stream
+        tb.t = nullptr;
+    }
+    if (tb.state == kResident) resident_bytes -= tb.bytes;
+    tb.bytes = 0;
+    tb.state = kGone;
+}
+
+// Evicts least recently used idle tables until `need` more bytes fit.
+bool intp_server::make_room(size_t need) {
+    while (resident_bytes + inflight_bytes + need > budget) {
+        int64_t victim = -1;
+        uint64_t oldest = ~uint64_t{0};
+        for (auto& kv : tables) {
+            const Table& tb = kv.second;
+            if (tb.state == kResident && tb.refs == 0 && tb.last_use < oldest) {
+                oldest = tb.last_use;
+                victim = kv.first;
+            }
+        }
+        if (victim < 0) return false;
+        drop_table(victim, tables[victim]);
+        ++evictions;
+    }
+    return true;
+}
+
+void intp_server::finish_slot(Slot& s, cudaError_t e) {
+    const Clock::time_point now = Clock::now();
+    Unit& u = s.unit;
+    inflight_bytes -= u.reserve;
+    if (u.build) {
+        Request* r = u.reqs[0];
+        Table& tb = tables[u.table];
+        if (e == cudaSuccess && tb.t) {
+            table_release_scratch(tb.t);
+            tb.bytes = table_device_bytes(tb.t);
+            tb.state = kResident;
+            tb.last_use = ++lru_clock;
+            resident_bytes += tb.bytes;
+            complete(r, INTP_OK, "", now);
+            if (tb.release && tb.refs == 0) drop_table(u.table, tb);
+        } else {
+            if (tb.t) intp_table_destroy(tb.t);
+            tb.t = nullptr;
+            tb.state = kFailed;
+            complete(r, INTP_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e), now);
+        }
+    } else {
+        for (Request* r : u.reqs)
+            complete(r, e == cudaSuccess ? INTP_OK : INTP_ERR_CUDA,
+                     e == cudaSuccess ? "" : std::string("evaluation: ") + cudaGetErrorString(e), now);
+        if (u.reqs.size() > 1) ++merged_units;
+    }
+    s.busy = false;
+    s.unit = Unit{};
+    cv_done.notify_all();
+}
+
+// Admits the first admissible pending request (with the evaluations that
+// merge into it) onto slot s. Returns false when nothing could be admitted.
+bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
+    (void)lock;
+    for (auto it = pending.begin(); it != pending.end(); ++it) {
+        Request* r = *it;
+        if (r->build) {
+            const size_t need = table_build_scratch_bytes(&r->desc) +
+                                [&] {
+                                    int64_t n = 1;
+                                    for (int d = 0; d < r->desc.dim; ++d) n *= r->desc.size[d];
+                                    return static_cast<size_t>(n) * 8 + (size_t{1} << 20);
+                                }();
+            if (need > budget) {
+                pending.erase(it);
+                tables[r->table].state = kFailed;
+                fail_request(r, INTP_ERR_BUDGET, "table build exceeds the memory budget");
+                return true;
+            }
+            if (!make_room(need)) continue;
+            pending.erase(it);
+            Unit u;
+            u.build = true;
+            u.reqs.push_back(r);
+            u.table = r->table;
+            u.reserve = need;
+            intp_table* t = nullptr;
+            intp_status st = create_table(&r->desc, true, s.stream, &t);
+            if (st == INTP_OK) {
+                tables[r->table].t = t;
+                st = intp_table_interpolate(t, r->values, is_device_pointer(r->values) ? 1 : 0, s.stream);
+            }
+            if (st != INTP_OK) {
+                const std::string msg = intp_last_error();
+                if (t) intp_table_destroy(t);
+                tables[r->table].t = nullptr;
+                tables[r->table].state = kFailed;
+                fail_request(r, st, msg);
+                return true;
+            }
+            inflight_bytes += need;
+            cudaEventRecord(s.done, s.stream);
+            s.unit = std::move(u);
+            s.busy = true;
+            return true;
+        }
+        // evaluation
+        auto tt = tables.find(r->table);
+        if (tt == tables.end() || tt->second.state == kGone || tt->second.state == kFailed) {
+            pending.erase(it);
+            fail_request(r, INTP_ERR_STATE, "table is not resident (evicted, released or failed)");
+            return true;
+        }
+        if (tt->second.state != kResident) continue;  // its build has not finished
+        Table& tb = tt->second;
+        // merge the queued evaluations of the same shape, in submission order
+        Unit u;
+        u.table = r->table;
+        const int K = r->derivs.empty() ? 1 : r->nderiv;
+        const size_t ob = r->out_dtype == INTP_F32 ? 4 : 8;
+        const size_t per_pt = static_cast<size_t>(tb.dim) * 8 + static_cast<size_t>(K) * ob + kEvalScratchPerPoint;
+        for (auto jt = it; jt != pending.end(); ++jt) {
+            Request* q = *jt;
+            if (q->build || !same_request_shape(r, q)) continue;
+            if (!u.reqs.empty() && u.npts + q->npts > max_batch_points) break;
+            u.reqs.push_back(q);
+            u.npts += q->npts;
+        }
+        u.reserve = eval_reserve(u.npts, per_pt);
+        if (u.reserve > budget) {
+            // a single request too large for the budget on its own
+            pending.erase(it);
+            fail_request(r, INTP_ERR_BUDGET, "evaluation exceeds the memory budget");
+            return true;
+        }
+        if (!make_room(u.reserve)) {
+            // take the first request alone if the merged unit does not fit
+            if (u.reqs.size() == 1) continue;
+            u.reqs.resize(1);
+            u.npts = r->npts;
+            u.reserve = eval_reserve(u.npts, per_pt);
+            if (!make_room(u.reserve)) continue;
+        }
+        for (Request* q : u.reqs) pending.remove(q);
+        const int D = tb.dim;
+        cudaStream_t st = s.stream;
+        double* dc = nullptr;
+        void* dout = nullptr;
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dc), static_cast<size_t>(u.npts) * D * 8 + 16, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&dout, static_cast<size_t>(u.npts) * K * ob + 16, st);
+        int64_t off = 0;
+        for (Request* q : u.reqs) {
+            if (e != cudaSuccess) break;
+            if (q->npts > 0)
+                e = cudaMemcpyAsync(dc + off * D, q->coords, static_cast<size_t>(q->npts) * D * 8, cudaMemcpyDefault,
+                                    st);
+            off += q->npts;
+        }
+        intp_status ist = INTP_OK;
+        std::string msg;
+        if (e == cudaSuccess) {
+            ist = intp_eval(tb.t, dc, u.npts, r->derivs.empty() ? nullptr : r->derivs.data(), r->nderiv, dout,
+                            r->out_dtype, st);
+            if (ist != INTP_OK) msg = intp_last_error();
+        }
+        off = 0;
+        for (Request* q : u.reqs) {
+            if (e != cudaSuccess || ist != INTP_OK) break;
+            if (q->npts > 0)
+                e = cudaMemcpyAsync(q->out, static_cast<unsigned char*>(dout) + static_cast<size_t>(off) * K * ob,
+                                    static_cast<size_t>(q->npts) * K * ob, cudaMemcpyDefault, st);
+            off += q->npts;
+        }
+        if (dc) cudaFreeAsync(dc, st);
+        if (dout) cudaFreeAsync(dout, st);
+        if (e != cudaSuccess || ist != INTP_OK) {
+            if (ist == INTP_OK) {
+                ist = e == cudaErrorMemoryAllocation ? INTP_ERR_OUT_OF_MEMORY : INTP_ERR_CUDA;
+                msg = std::string("evaluation: ") + cudaGetErrorString(e);
+            }
+            for (Request* q : u.reqs) fail_request(q, ist, msg);
+            return true;
+        }
+        tb.last_use = ++lru_clock;
+        inflight_bytes += u.reserve;
+        cudaEventRecord(s.done, st);
+        s.unit = std::move(u);
+        s.busy = true;
+        return true;
+    }
+    return false;
+}
+
+void intp_server::run() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lock(mu);
+    for (;;) {
+        bool any_busy = false;
+        for (Slot& s : slots) {
+            if (!s.busy) continue;
+            const cudaError_t q = cudaEventQuery(s.done);
+            if (q != cudaErrorNotReady) finish_slot(s, q);
+            any_busy = any_busy || s.busy;
+        }
+        bool admitted = false;
+        for (Slot& s : slots) {
+            if (s.busy || pending.empty()) continue;
+            if (admit(s, lock)) admitted = true;
+            any_busy = any_busy || s.busy;
+        }
+        if (stop && pending.empty() && !any_busy) break;
+        if (stop && !any_busy && !admitted) {
+            // shutting down with requests that can no longer be admitted
+            // (waiting on memory or on a table that will not come)
+            while (!pending.empty()) {
+                Request* r = pending.front();
+                pending.pop_front();
+                if (r->build) tables[r->table].state = kFailed;
+                fail_request(r, INTP_ERR_STATE, "server shut down before the request could run");
+            }
+            continue;
+        }
+        if (admitted) continue;
+        if (any_busy) {
+            // poll the running units' events
+            lock.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            lock.lock();
+        } else {
+            cv_work.wait_for(lock, std::chrono::milliseconds(2));
+        }
+    }
+}
+
+intp_server::~intp_server() {
+    {
+        std::lock_guard<std::mutex> g(mu);
+        stop = true;
+    }
+    cv_work.notify_all();
+    if (worker.joinable()) worker.join();
+    cudaSetDevice(device);
+    for (auto& kv : tables)
+        if (kv.second.t) intp_table_destroy(kv.second.t);
+    for (Slot& s : slots) {
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.stream) cudaStreamDestroy(s.stream);
+    }
+    for (auto& kv : requests) delete kv.second;  // includes any never waited on
+}
+
+namespace {
+
+intp_status sfail(intp_status s, const std::string& msg) {
+    set_last_error(msg);
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+intp_status intp_server_create(const intp_server_config* cfg, intp_server** out) {
+    if (!out) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    intp_server_config c{};
+    if (cfg) c = *cfg;
+    const int nslots = c.slots > 0 ? c.slots : 4;
+    if (nslots > kMaxSlots) return sfail(INTP_ERR_INVALID_ARGUMENT, "slots must be in [1, 64]");
+    intp_server* s = new (std::nothrow) intp_server();
+    if (!s) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    if (c.memory_budget > 0) s->budget = c.memory_budget;
+    if (c.max_batch_points > 0) s->max_batch_points = c.max_batch_points;
+    cudaGetDevice(&s->device);
+    s->slots.resize(static_cast<size_t>(nslots));
+    for (Slot& sl : s->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            delete s;
+            return sfail(INTP_ERR_CUDA, std::string("server streams: ") + cudaGetErrorString(e));
+        }
+    }
+    s->worker = std::thread([s] { s->run(); });
+    *out = s;
+    return INTP_OK;
+}
+
+intp_status intp_server_destroy(intp_server* s) {
+    delete s;
+    return INTP_OK;
+}
+
+intp_status intp_server_submit_build(intp_server* s, const intp_table_desc* desc, const double* values,
+                                     int64_t* table_id, int64_t* request_id) {
+    if (!s || !desc || !values || !table_id || !request_id) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (desc->dim < 1 || desc->dim > INTP_GPU_MAX_DIM) return sfail(INTP_ERR_UNSUPPORTED, "dimension must be in [1, 4]");
+    Request* r = new (std::nothrow) Request();
+    if (!r) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    r->build = true;
+    r->desc = *desc;
+    for (int d = 0; d < desc->dim; ++d)
+        if (desc->coords[d]) {
+            const size_t n = static_cast<size_t>(desc->size[d] + (desc->periodic[d] ? 1 : 0));
+            r->axis_coords[d].assign(desc->coords[d], desc->coords[d] + n);
+            r->desc.coords[d] = r->axis_coords[d].data();
+        }
+    r->values = values;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        r->id = s->next_request++;
+        r->table = s->next_table++;
+        Table& tb = s->tables[r->table];
+        tb.state = kQueued;
+        tb.dim = desc->dim;
+        s->requests[r->id] = r;
+        s->pending.push_back(r);
+        *table_id = r->table;
+        *request_id = r->id;
+    }
+    s->cv_work.notify_one();
+    return INTP_OK;
+}
+
+intp_status intp_server_submit_eval(intp_server* s, int64_t table_id, const double* coords, int64_t npts,
+                                    const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
+                                    int64_t* request_id) {
+    if (!s || !request_id) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (npts < 0 || (npts > 0 && (!coords || !out))) return sfail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    if (out_dtype != INTP_F32 && out_dtype != INTP_F64) return sfail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    if (derivs && (nderiv < 1 || nderiv > INTP_GPU_MAX_DERIV))
+        return sfail(INTP_ERR_INVALID_ARGUMENT, "nderiv must be in [1, 16]");
+    Request* r = new (std::nothrow) Request();
+    if (!r) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    r->table = table_id;
+    r->coords = coords;
+    r->npts = npts;
+    r->out = out;
+    r->out_dtype = out_dtype;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        auto it = s->tables.find(table_id);
+        if (it == s->tables.end()) {
+            delete r;
+            return sfail(INTP_ERR_INVALID_ARGUMENT, "unknown table id");
+        }
+        if (derivs) {
+            r->derivs.assign(derivs, derivs + static_cast<size_t>(nderiv) * it->second.dim);
+            r->nderiv = nderiv;
+        }
+        it->second.refs++;
+        r->id = s->next_request++;
+        s->requests[r->id] = r;
+        s->pending.push_back(r);
+        *request_id = r->id;
+    }
+    s->cv_work.notify_one();
+    return INTP_OK;
+}
+
+intp_status intp_server_wait(intp_server* s, int64_t request_id, double timeout_s, intp_status* result) {
+    if (!s || !result) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    std::unique_lock<std::mutex> lock(s->mu);
+    auto it = s->requests.find(request_id);
+    if (it == s->requests.end()) return sfail(INTP_ERR_INVALID_ARGUMENT, "unknown or already completed request id");
+    Request* r = it->second;
+    const auto pred = [r] { return r->done; };
+    if (timeout_s < 0) {
+        s->cv_done.wait(lock, pred);
+    } else if (!s->cv_done.wait_for(lock, std::chrono::duration<double>(timeout_s), pred)) {
+        return sfail(INTP_ERR_TIMEOUT, "request still running");
+    }
+    *result = r->status;
+    if (r->status != INTP_OK) set_last_error(r->error);
+    s->requests.erase(it);
+    delete r;
+    return INTP_OK;
+}
+
+intp_status intp_server_release(intp_server* s, int64_t table_id) {
+    if (!s) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->tables.find(table_id);
+    if (it == s->tables.end()) return sfail(INTP_ERR_INVALID_ARGUMENT, "unknown table id");
+    Table& tb = it->second;
+    tb.release = true;
+    if (tb.refs == 0 && tb.state == kResident) s->drop_table(table_id, tb);
+    return INTP_OK;
+}
+
+intp_status intp_server_table_state(intp_server* s, int64_t table_id, int32_t* state) {
+    if (!s || !state) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->tables.find(table_id);
+    if (it == s->tables.end()) return sfail(INTP_ERR_INVALID_ARGUMENT, "unknown table id");
+    *state = it->second.state;
+    return INTP_OK;
+}
+
+intp_status intp_server_get_stats(intp_server* s, intp_server_stats* out) {
+    if (!s || !out) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> g(s->mu);
+    std::memset(out, 0, sizeof *out);
+    out->builds_done = static_cast<int64_t>(s->lat_build.size());
+    out->evals_done = static_cast<int64_t>(s->lat_eval.size());
+    out->failed = s->failed;
+    out->evictions = s->evictions;
+    out->merged_units = s->merged_units;
+    for (auto& kv : s->tables) out->resident_tables += kv.second.state == kResident ? 1 : 0;
+    out->resident_bytes = s->resident_bytes;
+    out->inflight_bytes = s->inflight_bytes;
+    out->points_evaluated = s->points;
+    out->build_p50_ms = percentile(s->lat_build, 0.50);
+    out->build_p99_ms = percentile(s->lat_build, 0.99);
+    out->eval_p50_ms = percentile(s->lat_eval, 0.50);
+    out->eval_p99_ms = percentile(s->lat_eval, 0.99);
+    std::vector<double> all(s->lat_build);
+    all.insert(all.end(), s->lat_eval.begin(), s->lat_eval.end());
+    out->all_p50_ms = percentile(all, 0.50);
+    out->all_p99_ms = percentile(all, 0.99);
+    const double span = ms_since(s->t_reset, s->t_last) / 1e3;
+    out->points_per_s = span > 0 ? s->points / span : 0.0;
+    return INTP_OK;
+}
+
+intp_status intp_server_reset_stats(intp_server* s) {
+    if (!s) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> g(s->mu);
+    s->lat_build.clear();
+    s->lat_eval.clear();
+    s->points = 0;
+    s->failed = s->evictions = s->merged_units = 0;
+    s->t_reset = s->t_last = Clock::now();
+    return INTP_OK;
+}
+
+}  // extern "C"

@@ -214,6 +214,76 @@ intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table
 intp_status intp_batch_eval(const intp_batch* batch, const double* coords, const int64_t* point_offsets,
                             const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype, void* stream);
 
+/* ---- serving loop ----
+ *
+ * A worker thread that keeps built tables resident in device memory and
+ * runs table-build and evaluate requests with continuous batching: requests
+ * submitted while others run are admitted as soon as a slot (a CUDA stream)
+ * and memory free up, their work overlaps on the device, and evaluations
+ * queued against the same table are merged into one launch. Resident tables
+ * plus in-flight work stay within a memory budget; least recently used idle
+ * tables are evicted to make room. The reference has no server: a request
+ * stands for constructing an InterpolationFunction (Interpolation.hpp:92-107)
+ * or calling its operator() / derivative (:132-146, :177-205) on many points.
+ *
+ * Host buffers passed to the submit calls (values, coordinates, outputs) must
+ * stay valid until intp_server_wait reports the request done; page-locked
+ * host memory (or device memory) lets the copies run asynchronously. */
+typedef struct intp_server intp_server;
+
+typedef struct intp_server_config {
+    uint64_t memory_budget;    /* device bytes for tables + work in flight; 0 = 150 GiB */
+    int32_t slots;             /* work units in flight (CUDA streams), 1..64; 0 = 4 */
+    int32_t pad_;
+    int64_t max_batch_points;  /* merged evaluation size limit; 0 = 2^24 points */
+} intp_server_config;
+
+typedef struct intp_server_stats {
+    int64_t builds_done, evals_done, failed, evictions, merged_units, resident_tables;
+    uint64_t resident_bytes, inflight_bytes;
+    double points_evaluated;
+    double build_p50_ms, build_p99_ms, eval_p50_ms, eval_p99_ms, all_p50_ms, all_p99_ms;
+    double points_per_s;  /* points evaluated since the last reset / time to the last completion */
+} intp_server_stats;
+
+/* Table states reported by intp_server_table_state. */
+#define INTP_SERVER_TABLE_QUEUED 0
+#define INTP_SERVER_TABLE_RESIDENT 1
+#define INTP_SERVER_TABLE_GONE 2   /* evicted or released */
+#define INTP_SERVER_TABLE_FAILED 3
+
+/* Starts the worker on the current device (cfg may be NULL for defaults). */
+intp_status intp_server_create(const intp_server_config* cfg, intp_server** out);
+/* Finishes every submitted request, then frees the tables and the worker. */
+intp_status intp_server_destroy(intp_server* server);
+
+/* Queues the build of one table from its value mesh (prod(size) doubles,
+ * host or device memory): a new table id, usable by evaluations at once
+ * (they run after the build). Replaces constructing an InterpolationFunction
+ * (Interpolation.hpp:92-107). */
+intp_status intp_server_submit_build(intp_server* server, const intp_table_desc* desc, const double* values,
+                                     int64_t* table_id, int64_t* request_id);
+/* Queues an evaluation of npts points (npts x dim doubles) of a table, with
+ * the derivs / nderiv / out_dtype meaning of intp_eval; out receives
+ * npts x nderiv values (host or device memory). Replaces
+ * InterpolationFunction::operator() / derivative (Interpolation.hpp:132-146,
+ * :177-205) on each point. */
+intp_status intp_server_submit_eval(intp_server* server, int64_t table_id, const double* coords, int64_t npts,
+                                    const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
+                                    int64_t* request_id);
+/* Waits up to timeout_s seconds (< 0: no limit) for a request; *result is
+ * its status (INTP_ERR_BUDGET: it can never fit the budget; INTP_ERR_STATE:
+ * its table was evicted, released or failed to build). Each request is
+ * waited on once. INTP_ERR_TIMEOUT: still running. */
+intp_status intp_server_wait(intp_server* server, int64_t request_id, double timeout_s, intp_status* result);
+/* Drops a table once the requests that use it are done. */
+intp_status intp_server_release(intp_server* server, int64_t table_id);
+/* One of INTP_SERVER_TABLE_*. */
+intp_status intp_server_table_state(intp_server* server, int64_t table_id, int32_t* state);
+/* Latency percentiles and throughput since the last reset. */
+intp_status intp_server_get_stats(intp_server* server, intp_server_stats* out);
+intp_status intp_server_reset_stats(intp_server* server);
+
 /* ---- standalone band LU (BandLU.hpp) ---- */
 
 /* Factors an n x n band matrix given in the reference's storage: band is

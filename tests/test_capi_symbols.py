@@ -78,6 +78,23 @@ def test_batch_rejects_invalid_tables_before_any_device_work(lib):
     assert lib.intp_launch_count() == 0
 
 
+def test_server_without_a_device_fails_cleanly(lib):
+    """Creating the serving loop needs CUDA streams: without a GPU it reports
+    a CUDA error and leaks no worker thread."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from bsplineinterpolation_gb300 import _lib
+    h = C.c_void_p()
+    cfg = _lib.ServerConfig()
+    cfg.slots = 65
+    assert lib.intp_server_create(C.byref(cfg), C.byref(h)) == _lib.ERR_INVALID_ARGUMENT
+    cfg.slots = 2
+    assert lib.intp_server_create(C.byref(cfg), C.byref(h)) == _lib.ERR_CUDA
+    assert not h.value
+    assert lib.intp_server_destroy(None) == _lib.OK
+
+
 def test_product_never_loads_the_oracle():
     """The package imports nothing from oracle/ (it is test infrastructure)."""
     pkg = os.path.join(REPO, "bsplineinterpolation_gb300")

@@ -122,3 +122,21 @@ def test_binned_single_bucket_and_empty():
     assert _close(a, np.repeat(b, 300_000, axis=0))
     empty = torch.empty((0, 3), dtype=torch.float64, device="cuda")
     assert _eval(f, empty, None, "binned").shape == (0, 1)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_host_buffer_pipeline_equals_device_path(precision):
+    """intp_eval_host with many chunks (copies in and out on their own
+    streams, overlapping the evaluation of the neighbouring chunks) returns
+    exactly what one device-buffer evaluation returns."""
+    n = 40
+    g = np.linspace(-1, 1, n)
+    v = np.sin(3 * g)[:, None, None] * np.cos(2 * g)[None, :, None] * np.exp(g)[None, None, :]
+    f = bi.InterpolationFunction(3, [False] * 3, torch.tensor(v, device="cuda"), (-1, 1), (-1, 1), (-1, 1),
+                                 precision=precision)
+    pts = np.random.default_rng(4).uniform(-1, 1, (50_003, 3))
+    derivs = [[0, 0, 0], [0, 1, 0]]
+    with _Env(INTP_GB300_CHUNK=4096, INTP_GB300_EVAL="direct"):
+        host = f.evaluate(pts, derivs=derivs)
+        dev = f.evaluate(torch.tensor(pts, device="cuda"), derivs=derivs).cpu().numpy()
+    assert np.array_equal(host, dev)
