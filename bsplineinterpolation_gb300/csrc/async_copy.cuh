@@ -56,6 +56,25 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint3
         : "memory");
 }
 
+// TMA tiled tensor loads global -> shared of one box (the map's box sizes),
+// completing on `bar`. Coordinates are in elements, innermost first; the
+// innermost coordinate times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* tmap, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst_smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst_smem, const void* tmap, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst_smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // TMA bulk copy shared -> global, tracked by the bulk async-group
 __device__ __forceinline__ void bulk_store(void* dst, const void* src_smem, uint32_t bytes) {
     asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src_smem)),
@@ -88,5 +107,17 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;" ::: "memory");
     asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
+
+// Defines `int NAME(cudaStream_t)`: reads and clears this translation unit's
+// copy of g_device_error (each unit that waits on a barrier has its own).
+#define INTP_DEFINE_DEVICE_ERROR_READER(NAME)                                                                 \
+    int NAME(cudaStream_t s) {                                                                                \
+        int v = 0, zero = 0;                                                                                  \
+        if (cudaMemcpyFromSymbolAsync(&v, g_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess) \
+            return 0;                                                                                         \
+        cudaMemcpyToSymbolAsync(g_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);            \
+        cudaStreamSynchronize(s);                                                                             \
+        return v;                                                                                             \
+    }
 
 }  // namespace intp_gb300

@@ -6,45 +6,51 @@ namespace intp_gb300 {
 namespace {
 
 template <int D, int O>
-cudaError_t launch_do(const TableDev& t, const BinGeom& g, const uint32_t* offsets, int nblk, int64_t slice, const uint32_t* rec,
+cudaError_t launch_do(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const uint32_t* offsets, int nblk,
+                      int64_t slice, const uint32_t* rec,
                       int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid, cudaStream_t s) {
     auto k = bin_detail::eval_kernel<D, O>;
-    const size_t smem = static_cast<size_t>(g.tile_elems) * 4;
+    const size_t smem = static_cast<size_t>(g.tile_elems) * 4 + 128;  // + alignment of the TMA destination
     // static + dynamic shared memory may pass 48 KB even when the tile alone
     // does not, so the opt-in limit is set on every launch
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32 ? 1 : 0);
+    CUtensorMap none{};
+    k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32 ? 1 : 0,
+                                                  tmap ? *tmap : none, tmap ? 1 : 0);
     note_launch();
     return cudaGetLastError();
 }
 
 template <int D>
-cudaError_t launch_d(const TableDev& t, const BinGeom& g, const uint32_t* offsets, int nblk, int64_t slice, const uint32_t* rec,
+cudaError_t launch_d(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const uint32_t* offsets, int nblk,
+                     int64_t slice, const uint32_t* rec,
                      int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid, cudaStream_t s) {
     switch (t.order) {
-        case 0: return launch_do<D, 0>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 1: return launch_do<D, 1>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 2: return launch_do<D, 2>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 3: return launch_do<D, 3>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 4: return launch_do<D, 4>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 5: return launch_do<D, 5>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 6: return launch_do<D, 6>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 7: return launch_do<D, 7>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 0: return launch_do<D, 0>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 1: return launch_do<D, 1>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 2: return launch_do<D, 2>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 3: return launch_do<D, 3>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 4: return launch_do<D, 4>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 5: return launch_do<D, 5>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 6: return launch_do<D, 6>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 7: return launch_do<D, 7>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
     }
     return cudaErrorInvalidValue;
 }
 
 }  // namespace
 
-cudaError_t launch_bin_eval_d12(const TableDev& t, const BinGeom& g, const uint32_t* offsets, int nblk,
-                                 int64_t slice, const uint32_t* rec, int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid,
+cudaError_t launch_bin_eval_d12(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const uint32_t* offsets,
+                               int nblk, int64_t slice, const uint32_t* rec, int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid,
                                  cudaStream_t s) {
     switch (t.dim) {
-        case 1: return launch_d<1>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
-        case 2: return launch_d<2>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 1: return launch_d<1>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
+        case 2: return launch_d<2>(t, g, tmap, offsets, nblk, slice, rec, n, plan, out, out_f32, grid, s);
     }
     return cudaErrorInvalidValue;
 }
+
+INTP_DEFINE_DEVICE_ERROR_READER(take_device_error_bin_d12)
 
 }  // namespace intp_gb300

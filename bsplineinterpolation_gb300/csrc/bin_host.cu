@@ -165,7 +165,8 @@ BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
         g.P[d] = (1 << lb) + O;
         g.nb[d] = static_cast<int32_t>((t.ax[d].ncells + (int64_t{1} << lb) - 1) >> lb);
         g.tstride[d] = stride;
-        stride *= g.P[d];
+        // rows of the last axis are padded to a multiple of 4 floats
+        stride *= d == D - 1 ? ((g.P[d] + 3) & ~3) : g.P[d];
     }
     for (int d = 0; d < D; ++d) {
         g.shift[d] = shift;
@@ -181,8 +182,9 @@ BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
     return g;
 }
 
-cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
-                            const DerivPlan& plan, void* out, bool out_f32, int64_t chunk, cudaStream_t s) {
+cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const double* coords,
+                            int64_t npts, const DerivPlan& plan, void* out, bool out_f32, int64_t chunk,
+                            cudaStream_t s) {
     if (npts <= 0) return cudaSuccess;
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
@@ -218,8 +220,8 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* c
         e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, &slice, s);
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
-        e = D <= 2 ? launch_bin_eval_d12(t, g, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s)
-                   : launch_bin_eval_d3(t, g, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s);
+        e = D <= 2 ? launch_bin_eval_d12(t, g, tmap, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s)
+                   : launch_bin_eval_d3(t, g, tmap, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s);
     }
     cudaError_t e2 = cudaFreeAsync(mem, s);
     return e != cudaSuccess ? e : e2;

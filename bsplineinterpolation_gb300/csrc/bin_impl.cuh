@@ -27,6 +27,8 @@
 // sectors are complete.
 #pragma once
 
+#include <cuda.h>
+
 #include <cstdint>
 
 #include "async_copy.cuh"
@@ -202,13 +204,15 @@ __global__ void __launch_bounds__(kSortThreads) permute_kernel(BinGeom g, int64_
 
 constexpr int ipow_c(int b, int e) { return e == 0 ? 1 : b * ipow_c(b, e - 1); }
 
-// Compile-time tile shape: P_d = 2^bucket_log2 + O per axis, row-major.
+// Compile-time tile shape: P_d = 2^bucket_log2 + O positions per axis,
+// row-major, rows of the last axis padded to a multiple of 4 floats (the
+// 16-byte inner extent of a TMA box).
 template <int D, int O>
 struct TileShape {
     static constexpr int P(int d) { return (1 << bucket_log2(D, d)) + O; }
-    static constexpr int S(int d) { return d >= D - 1 ? 1 : P(d + 1) * S(d + 1); }
-    static constexpr int elems() { return P(0) * S(0); }
-    static constexpr int rows() { return elems() / P(D - 1); }
+    static constexpr int PL() { return (P(D - 1) + 3) & ~3; }
+    static constexpr int S(int d) { return d >= D - 1 ? 1 : (d == D - 2 ? PL() : P(d + 1) * S(d + 1)); }
+    static constexpr int elems() { return D == 1 ? PL() : P(0) * S(0); }
 };
 
 // Control-point index along axis a of tile position org + i (periodic wrap,
@@ -375,9 +379,14 @@ template <int D, int O>
 __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeom g, const uint32_t* __restrict__ blkoffset,
                                                            int nblk, int64_t slice, const uint32_t* __restrict__ rec,
                                                            int64_t nrec, DerivPlan plan, void* __restrict__ out,
-                                                           int out_f32) {
+                                                           int out_f32, const __grid_constant__ CUtensorMap tmap,
+                                                           int use_tma) {
     using TS = TileShape<D, O>;
-    extern __shared__ float tile[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // 128-byte aligned tile (the TMA destination)
+    float* tile = reinterpret_cast<float*>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
+    __shared__ __align__(8) uint64_t sh_bar;
+    __shared__ float sh_cref;
     __shared__ DerivPlan sh_plan;  // indexed by runtime output / group numbers
     __shared__ TableDev sh_t;      // passed by reference to the out-of-line path
     __shared__ int sh_last[TS::P(D - 1)];                          // last-axis control-point indices
@@ -389,8 +398,10 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
     if (threadIdx.x == 0) {
         sh_plan = plan;
         sh_t = t;
+        mbar_init(&sh_bar, 1);
     }
     __syncthreads();
+    uint32_t bar_phase = 0;
     // first slot of bucket b (bucket g.nbuckets: one past the last record)
     auto bstart = [&](int64_t bb) -> int64_t {
         return bb >= g.nbuckets ? nrec : static_cast<int64_t>(__ldg(blkoffset + bb * nblk));
@@ -406,6 +417,7 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
     int64_t b = lo;
     int64_t r = r0;
     constexpr int PL = TS::P(D - 1);  // tile row length (last axis)
+    constexpr int PLP = TS::PL();      // its padded pitch
     while (r < r1) {
         while (bstart(b + 1) <= r) ++b;
         const int64_t bend = bstart(b + 1);
@@ -420,43 +432,68 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
             }
         }
         __syncthreads();
-        // per-axis global offsets of the tile positions (periodic wrap, clamp
-        // at the end of a non-periodic axis)
-        for (int i = threadIdx.x; i < PL; i += kBinThreads) sh_last[i] = tile_index(t.ax[D - 1], org[D - 1] + i);
         for (int j = threadIdx.x; j < nblk; j += kBinThreads) sh_seg[j] = __ldg(blkoffset + b * nblk + j);
-        if constexpr (D >= 2) {
-            for (int i = threadIdx.x; i < TS::P(0); i += kBinThreads)
-                sh_outer[0][i] = static_cast<int64_t>(tile_index(t.ax[0], org[0] + i)) * t.ax[0].stride;
-        }
-        if constexpr (D >= 3) {
-            for (int i = threadIdx.x; i < TS::P(1); i += kBinThreads)
-                sh_outer[1][i] = static_cast<int64_t>(tile_index(t.ax[1], org[1] + i)) * t.ax[1].stride;
-        }
-        __syncthreads();
-        // stage the whole tile with asynchronous copies, all in flight at once
-        for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) {
-            int rem = e;
-            const int il = rem % PL;
-            rem /= PL;
-            int64_t off = sh_last[il];
+        if (threadIdx.x == 0) {
+            int64_t off = 0;
 #pragma unroll
-            for (int d = D - 2; d >= 0; --d) {
-                const int i = rem % TS::P(d);
-                rem /= TS::P(d);
-                off += sh_outer[d][i];
-            }
-            cp_async<4>(tile + e, cp + off);
+            for (int d = 0; d < D; ++d)
+                off += static_cast<int64_t>(tile_index(t.ax[d], org[d] + TS::P(d) / 2)) * t.ax[d].stride;
+            sh_cref = __ldg(cp + off);
         }
-        cp_async_wait_all();
+        // one TMA box unless the tile wraps around a periodic axis
+        bool tma = use_tma != 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            if (t.ax[d].periodic && org[d] + TS::P(d) > t.ax[d].n) tma = false;
+        if (tma) {
+            if (threadIdx.x == 0) {
+                fence_async_smem();  // the tile's earlier generic-proxy accesses before the async write
+                mbar_expect_tx(&sh_bar, static_cast<uint32_t>(TS::elems() * 4));
+                if constexpr (D == 3) tma_load_3d(tile, &tmap, org[2], org[1], org[0], &sh_bar);
+                if constexpr (D == 2) tma_load_2d(tile, &tmap, org[1], org[0], &sh_bar);
+            }
+            const bool ok = mbar_wait(&sh_bar, bar_phase);
+            if (!__syncthreads_and(ok)) {
+                if (!ok) mbar_wait(&sh_bar, bar_phase);  // bounded: let the copy in flight land
+                return;
+            }
+            bar_phase ^= 1u;
+        } else {
+            // per-axis global offsets of the tile positions (periodic wrap,
+            // clamp at the end of a non-periodic axis)
+            for (int i = threadIdx.x; i < PL; i += kBinThreads) sh_last[i] = tile_index(t.ax[D - 1], org[D - 1] + i);
+            if constexpr (D >= 2) {
+                for (int i = threadIdx.x; i < TS::P(0); i += kBinThreads)
+                    sh_outer[0][i] = static_cast<int64_t>(tile_index(t.ax[0], org[0] + i)) * t.ax[0].stride;
+            }
+            if constexpr (D >= 3) {
+                for (int i = threadIdx.x; i < TS::P(1); i += kBinThreads)
+                    sh_outer[1][i] = static_cast<int64_t>(tile_index(t.ax[1], org[1] + i)) * t.ax[1].stride;
+            }
+            __syncthreads();
+            // asynchronous element copies, all in flight at once
+            for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) {
+                int rem = e;
+                const int il = rem % PLP;
+                rem /= PLP;
+                if (il >= PL) continue;  // row padding
+                int64_t off = sh_last[il];
+#pragma unroll
+                for (int d = D - 2; d >= 0; --d) {
+                    const int i = rem % TS::P(d);
+                    rem /= TS::P(d);
+                    off += sh_outer[d][i];
+                }
+                cp_async<4>(tile + e, cp + off);
+            }
+            cp_async_wait_all();
+        }
         __syncthreads();
         // The tile is stored relative to a reference control point near its
-        // centre: value weights sum to 1 and derivative weights to 0, so the
+        // centre (clamped at the end of a non-periodic axis, as in the direct
+        // kernel): value weights sum to 1 and derivative weights to 0, so the
         // FP32 rounding of the weights only multiplies the local variation.
-        int centre = 0;
-#pragma unroll
-        for (int d = 0; d < D; ++d) centre += (TS::P(d) / 2) * TS::S(d);
-        const float cref = tile[centre];
-        __syncthreads();
+        const float cref = sh_cref;
         for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) tile[e] -= cref;
         __syncthreads();
         if (sh_plan.simple)

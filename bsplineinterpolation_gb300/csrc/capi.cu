@@ -1,5 +1,7 @@
 // C-ABI of the library (include/intp_gpu.h): table lifetime, the control-point
 // solve pipelines and batched evaluation.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,6 +102,10 @@ struct intp_table {
     size_t scratch_bytes = 0;
     double lo_user[kMaxDim]{};  // uniform axes: x_range.first
     size_t arena_bytes = 0;
+    // TMA map of the FP32 control points whose box is one bucket tile of the
+    // binned evaluation (D = 2, 3 with 16-byte aligned row strides)
+    CUtensorMap tile_map{};
+    bool has_tile_map = false;
     // Tables of the serving loop take their memory from the stream-ordered
     // pool on alloc_stream (no device-wide synchronisation on free).
     bool stream_ordered = false;
@@ -136,6 +142,52 @@ struct intp_bandlu {
 
 namespace {
 
+// cuTensorMapEncodeTiled from the driver, looked up through the runtime (the
+// library links no driver library).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// A TMA map of the control points whose box is one bucket tile: extents P_d
+// per axis, the last padded to a multiple of 4 floats. Positions past the end
+// of a non-periodic axis read zeros (no query reads them). Needs row strides
+// that are multiples of 16 bytes and boxes of at most 256 per axis.
+bool make_tile_map(intp_table* t) {
+    const TableModel& m = t->model;
+    const BinGeom& g = t->bins;
+    const int D = m.dim;
+    if (D < 2 || D > 3) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[3] = {}, strides[2] = {};
+    cuuint32_t box[3] = {}, estr[3] = {1, 1, 1};
+    for (int i = 0; i < D; ++i) {
+        const int d = D - 1 - i;  // innermost first
+        dims[i] = static_cast<cuuint64_t>(m.axis[d].n);
+        box[i] = static_cast<cuuint32_t>(i == 0 ? ((g.P[d] + 3) & ~3) : g.P[d]);
+        if (box[i] > 256) return false;
+    }
+    strides[0] = static_cast<cuuint64_t>(m.axis[D - 1].n) * 4;
+    if (D == 3) strides[1] = strides[0] * static_cast<cuuint64_t>(m.axis[1].n);
+    for (int i = 0; i < D - 1; ++i)
+        if (strides[i] % 16 != 0) return false;
+    const CUresult r = enc(&t->tile_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, static_cast<cuuint32_t>(D), t->ctrl, dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // Per-axis tables used by evaluation and the solve, laid out in one arena.
 intp_status upload_table(intp_table* t) {
     const TableModel& m = t->model;
@@ -152,7 +204,10 @@ intp_status upload_table(intp_table* t) {
     bind_table(m, t->lo_user, pt, static_cast<const unsigned char*>(t->arena), t->dev, t->fac);
     INTP_CUDA(t->dmalloc(&t->ctrl, static_cast<size_t>(m.total) * t->elem()), "cudaMalloc(control points)");
     t->dev.ctrl = t->ctrl;
-    if (t->mixed() && m.dim <= 3) t->bins = make_bin_geom(t->dev, kTileBytes);
+    if (t->mixed() && m.dim <= 3) {
+        t->bins = make_bin_geom(t->dev, kTileBytes);
+        if (t->bins.smem_buckets > 0) t->has_tile_map = make_tile_map(t);
+    }
     return INTP_OK;
 }
 
@@ -644,8 +699,8 @@ intp_status intp_eval(const intp_table* t, const double* coords, int64_t npts, c
                         (mode == 2 || (mode == 0 && npts >= kBinnedMinPoints));
     if (binned) {
         retain_pool_memory();
-        INTP_CUDA(run_binned_eval(t->dev, t->bins, coords, npts, plan, out, out_dtype == INTP_F32, eval_chunk(),
-                                  static_cast<cudaStream_t>(stream)),
+        INTP_CUDA(run_binned_eval(t->dev, t->bins, t->has_tile_map ? &t->tile_map : nullptr, coords, npts, plan, out,
+                                  out_dtype == INTP_F32, eval_chunk(), static_cast<cudaStream_t>(stream)),
                   "binned evaluation");
         return INTP_OK;
     }
@@ -798,7 +853,9 @@ intp_status intp_locate(const intp_table* t, const double* coords, int64_t npts,
 
 intp_status intp_stream_synchronize(void* stream) {
     INTP_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
-    if (take_device_error(static_cast<cudaStream_t>(stream)) != 0)
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int err = take_device_error(s) | take_device_error_bin_d12(s) | take_device_error_bin_d3(s);
+    if (err != 0)
         return fail(INTP_ERR_TIMEOUT, "a kernel's bounded wait for an asynchronous copy ran out");
     return INTP_OK;
 }
@@ -923,9 +980,10 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
                                  in_rec, rec, &slice, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
-        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
+        const CUtensorMap* tm = t->has_tile_map ? &t->tile_map : nullptr;
+        INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
                                                out_f32, sms * 2, s)
-                         : launch_bin_eval_d3(t->dev, g, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
+                         : launch_bin_eval_d3(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
                                               out_f32, sms * 2, s),
                   "binned evaluation");
     }

@@ -1,6 +1,7 @@
 // Kernel launchers shared between the CUDA translation units and the C-ABI.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -24,8 +25,11 @@ struct ShiftDesc {
 cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coords, int64_t npts,
                                const DerivPlan& plan, void* out, bool out_f32, cudaStream_t s);
 // Binned evaluation of the mixed form (bin_host.cu); `chunk` queries per round.
-cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
-                            const DerivPlan& plan, void* out, bool out_f32, int64_t chunk, cudaStream_t s);
+// tmap: TMA map of the control points with the tile as its box (NULL: the
+// tiles are staged with element copies).
+cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const double* coords,
+                            int64_t npts, const DerivPlan& plan, void* out, bool out_f32, int64_t chunk,
+                            cudaStream_t s);
 // One chunk's counting sort by bucket into caller-provided scratch: blkcount
 // and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096);
 // in_rec and rec hold n records of bin_record_words(D) words each (queries
@@ -35,12 +39,15 @@ cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* co
                            uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
                            uint32_t* rec, int64_t* slice, cudaStream_t s);
 int bin_record_words(int dim);
-cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk, int64_t slice,
-                                const uint32_t* rec, int64_t n, const DerivPlan&, void* out, bool out_f32,
-                                int grid, cudaStream_t);
-cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const uint32_t* blkoffset, int nblk, int64_t slice,
-                               const uint32_t* rec, int64_t n, const DerivPlan&, void* out, bool out_f32,
-                               int grid, cudaStream_t);
+cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const CUtensorMap* tmap, const uint32_t* blkoffset,
+                                int nblk, int64_t slice, const uint32_t* rec, int64_t n, const DerivPlan&, void* out,
+                                bool out_f32, int grid, cudaStream_t);
+cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const CUtensorMap* tmap, const uint32_t* blkoffset,
+                               int nblk, int64_t slice, const uint32_t* rec, int64_t n, const DerivPlan&, void* out,
+                               bool out_f32, int grid, cudaStream_t);
+// Read and clear the device error flag of the binned evaluation units.
+int take_device_error_bin_d12(cudaStream_t s);
+int take_device_error_bin_d3(cudaStream_t s);
 // Bucket geometry for a table (tile of at most `tile_bytes` FP32 control points).
 BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes);
 
