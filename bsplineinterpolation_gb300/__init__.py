@@ -62,7 +62,7 @@ def _is_range(r):
     return isinstance(r, (tuple, list)) and len(r) == 2 and all(np.isscalar(v) for v in r)
 
 
-def _make_desc(order, periodicity, mesh_dims, x_ranges, precision, refine_steps):
+def _make_desc(order, periodicity, mesh_dims, x_ranges, precision, refine_steps, channels=1):
     """intp_table_desc of one table; returns (desc, arrays to keep alive, dims,
     periodicity)."""
     dims = [int(v) for v in np.atleast_1d(mesh_dims)]
@@ -79,6 +79,7 @@ def _make_desc(order, periodicity, mesh_dims, x_ranges, precision, refine_steps)
     desc.order = int(order)
     desc.precision = _PRECISIONS[precision]
     desc.refine_steps = int(refine_steps)
+    desc.channels = int(channels)
     keep = []
     for d in range(D):
         desc.periodic[d] = int(periodicity[d])
@@ -109,11 +110,12 @@ class InterpolationFunctionTemplate:
     """
 
     def __init__(self, order, periodicity, mesh_dims, *x_ranges, precision="fp64",
-                 refine_steps=-1):
+                 refine_steps=-1, channels=1):
         lib = _lib.load()
         desc, self._coords, dims, periodicity = _make_desc(order, periodicity, mesh_dims, x_ranges,
-                                                           precision, refine_steps)
+                                                           precision, refine_steps, channels)
         D = len(dims)
+        self.channels = max(1, int(channels))
         h = C.c_void_p()
         _lib.check(lib.intp_table_create(C.byref(desc), C.byref(h)))
         self._h = h
@@ -136,14 +138,14 @@ class InterpolationFunctionTemplate:
         if _is_cuda_tensor(mesh):
             torch = _torch()
             m = mesh.to(torch.float64).contiguous()
-            if m.numel() != int(np.prod(self.dims)):
+            if m.numel() != int(np.prod(self.dims)) * self.channels:
                 raise ValueError("mesh shape mismatch")
             _lib.check(lib.intp_table_interpolate(self._h, C.c_void_p(m.data_ptr()), 1,
                                                   _stream_ptr(stream)))
             self._keep = m
         else:
             m = np.ascontiguousarray(np.asarray(mesh, np.float64))
-            if m.size != int(np.prod(self.dims)):
+            if m.size != int(np.prod(self.dims)) * self.channels:
                 raise ValueError("mesh shape mismatch")
             _lib.check(lib.intp_table_interpolate(self._h, m.ctypes.data, 0, _stream_ptr(stream)))
             _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
@@ -154,7 +156,7 @@ class InterpolationFunctionTemplate:
         f = InterpolationFunction.__new__(InterpolationFunction)
         f._template = InterpolationFunctionTemplate(self.order, self._periodicity, self.dims,
                                                     *self._x_ranges, precision=self.precision,
-                                                    refine_steps=self._refine)
+                                                    refine_steps=self._refine, channels=self.channels)
         f._template._solve(mesh, stream)
         f._init_from_template()
         return f
@@ -171,16 +173,23 @@ class InterpolationFunction:
     """
 
     def __init__(self, order, periodicity, mesh, *x_ranges, precision="fp64", refine_steps=-1,
-                 stream=None):
+                 stream=None, vector=False):
+        """vector=True: the last axis of `mesh` holds the C components of a
+        vector-valued T (the reference's InterpolationFunction<Vec<C, .>, D, O>);
+        evaluations then return C values per output."""
         if _is_cuda_tensor(mesh):
             dims = list(mesh.shape)
         else:
             dims = list(np.shape(mesh))
+        channels = 1
+        if vector:
+            channels = dims[-1]
+            dims = dims[:-1]
         if len(x_ranges) == 1 and len(dims) > 1 and not _is_range(x_ranges[0]):
             x_ranges = tuple(x_ranges[0])
         self._template = InterpolationFunctionTemplate(order, periodicity, dims, *x_ranges,
                                                        precision=precision,
-                                                       refine_steps=refine_steps)
+                                                       refine_steps=refine_steps, channels=channels)
         self._template._solve(mesh, stream)
         self._init_from_template()
 
@@ -190,6 +199,7 @@ class InterpolationFunction:
         self.dim = t.dim
         self.order = t.order
         self.precision = t.precision
+        self.channels = t.channels
         self._h = t._h
         self._range = []
         self._uniform = []
@@ -225,9 +235,10 @@ class InterpolationFunction:
         return out
 
     def control_points(self):
-        out = np.zeros(int(np.prod(self._template.dims)))
+        C = self.channels
+        out = np.zeros(int(np.prod(self._template.dims)) * C)
         _lib.check(_lib.load().intp_table_get_control_points(self._h, out.ctypes.data))
-        return out.reshape(self._template.dims)
+        return out.reshape(self._template.dims + ([C] if C > 1 else []))
 
     # -- batched evaluation --
     def evaluate(self, points, derivs=None, out=None, out_dtype=None, stream=None):
@@ -246,19 +257,21 @@ class InterpolationFunction:
             karr = np.ascontiguousarray(np.asarray(derivs, np.int32).reshape(-1, D))
             K = karr.shape[0]
             kp = karr.ctypes.data
+        # vector-valued tables: C values per output (shape N x K x C)
+        shape = (K,) if self.channels == 1 else (K, self.channels)
         if _is_cuda_tensor(points):
             torch = _torch()
             pts = points.to(torch.float64).contiguous().reshape(-1, D)
             n = pts.shape[0]
             if out is None:
-                out = torch.empty((n, K), dtype=torch.float32 if od == _lib.F32 else torch.float64,
+                out = torch.empty((n,) + shape, dtype=torch.float32 if od == _lib.F32 else torch.float64,
                                   device=pts.device)
             _lib.check(lib.intp_eval(self._h, C.c_void_p(pts.data_ptr()), n, kp, K,
                                      C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
             return out
         pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, D))
         n = pts.shape[0]
-        res = np.zeros((n, K), np.float32 if od == _lib.F32 else np.float64)
+        res = np.zeros((n,) + shape, np.float32 if od == _lib.F32 else np.float64)
         _lib.check(lib.intp_eval_host(self._h, pts.ctypes.data, n, kp, K, res.ctypes.data, od,
                                       _stream_ptr(stream)))
         return res
@@ -301,14 +314,17 @@ class InterpolationFunction:
                 raise IntpDomainError(_lib.ERR_DOMAIN,
                                       "Given coordinate out of interpolation function range!")
 
+    def _one(self, v):
+        return float(v) if self.channels == 1 else np.asarray(v)
+
     def __call__(self, *coords):
         c = self._coord(coords)
-        return float(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
+        return self._one(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
 
     def at(self, *coords):
         c = self._coord(coords)
         self._boundary_check(c)
-        return float(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
+        return self._one(self.evaluate(c.reshape(1, -1), out_dtype="f64")[0, 0])
 
     def _derivs(self, coord, orders):
         if len(orders) == 1 and np.ndim(orders[0]) == 1:
@@ -319,12 +335,12 @@ class InterpolationFunction:
 
     def derivative(self, coord, *orders):
         c, k = self._derivs(coord, orders)
-        return float(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
+        return self._one(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
 
     def derivative_at(self, coord, *orders):
         c, k = self._derivs(coord, orders)
         self._boundary_check(c[0])
-        return float(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
+        return self._one(self.evaluate(c, derivs=k.reshape(1, -1), out_dtype="f64")[0, 0])
 
 
 class InterpolationFunction1D(InterpolationFunction):
@@ -335,6 +351,8 @@ class InterpolationFunction1D(InterpolationFunction):
     def __init__(self, order, f, x_range=None, periodic=False, **kw):
         f = f if _is_cuda_tensor(f) else np.asarray(f, np.float64)
         n = f.shape[0]
+        if f.ndim == 2:
+            kw.setdefault("vector", True)  # n samples of a vector-valued function
         if x_range is None:
             x_range = (0.0, float(n - (0 if periodic else 1)))
         super().__init__(order, [periodic], f, x_range, **kw)

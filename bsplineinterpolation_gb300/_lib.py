@@ -41,6 +41,8 @@ class TableDesc(C.Structure):
         ("range_lo", C.c_double * MAX_DIM),
         ("range_hi", C.c_double * MAX_DIM),
         ("coords", C.c_void_p * MAX_DIM),
+        ("channels", C.c_int32),
+        ("reserved_", C.c_int32),
     ]
 
 

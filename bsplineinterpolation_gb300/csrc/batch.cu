@@ -447,6 +447,10 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
                 delete b;
                 return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables have dimension 1..3");
             }
+            if (d.channels > 1) {
+                delete b;
+                return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables are scalar (channels <= 1)");
+            }
             if (d.order < 0 || d.order > INTP_GPU_MAX_ORDER) {
                 delete b;
                 return bfail(INTP_ERR_UNSUPPORTED, where + "order must be in [0, 7]");

@@ -89,6 +89,7 @@ std::vector<float> to_f32(const std::vector<double>& v) {
 
 struct intp_table {
     TableModel model;
+    int channels = 1;  // values per mesh point (vector-valued tables)
     int precision = INTP_PRECISION_FP64;
     int refine_steps = 0;
     int device = 0;
@@ -128,6 +129,7 @@ struct intp_table {
     }
     bool mixed() const { return precision == INTP_PRECISION_MIXED; }
     size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
+    int64_t values() const { return model.total * channels; }  // control points over all channels
 };
 
 struct intp_bandlu {
@@ -202,9 +204,13 @@ intp_status upload_table(intp_table* t) {
     else
         INTP_CUDA(cudaMemcpy(t->arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice), "cudaMemcpy(table)");
     bind_table(m, t->lo_user, pt, static_cast<const unsigned char*>(t->arena), t->dev, t->fac);
-    INTP_CUDA(t->dmalloc(&t->ctrl, static_cast<size_t>(m.total) * t->elem()), "cudaMalloc(control points)");
+    INTP_CUDA(t->dmalloc(&t->ctrl, static_cast<size_t>(t->values()) * t->elem()), "cudaMalloc(control points)");
     t->dev.ctrl = t->ctrl;
-    if (t->mixed() && m.dim <= 3) {
+    t->dev.channels = t->channels;
+    t->dev.chan_stride = m.total;
+    // the binned path stages one channel's tiles: vector-valued tables
+    // evaluate with the direct kernel
+    if (t->mixed() && m.dim <= 3 && t->channels == 1) {
         t->bins = make_bin_geom(t->dev, kTileBytes);
         if (t->bins.smem_buckets > 0) t->has_tile_map = make_tile_map(t);
     }
@@ -226,6 +232,7 @@ ShiftDesc shift_desc(const intp_table* t) {
     const TableModel& m = t->model;
     sd.dim = m.dim;
     sd.total = m.total;
+    sd.channels = t->channels;
     for (int d = 0; d < m.dim; ++d) {
         sd.n[d] = m.axis[d].n;
         sd.shift[d] = m.axis[d].periodic ? (m.order / 2) % m.axis[d].n : 0;
@@ -243,7 +250,7 @@ LineGeom line_geom(const intp_table* t, int axis) {
     LineGeom g;
     g.n = m.axis[axis].n;
     g.S = t->dev.ax[axis].stride;
-    g.nlines = m.total / g.n;
+    g.nlines = t->values() / g.n;  // every channel's lines (channel-major storage)
     return g;
 }
 
@@ -273,7 +280,7 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
 
 intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_t s) {
     const TableModel& m = t->model;
-    const int64_t N = m.total;
+    const int64_t N = t->values();
     const ShiftDesc sd = shift_desc(t);
     if (!t->mixed()) {
         double* c = static_cast<double*>(t->ctrl);
@@ -429,6 +436,8 @@ intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaS
         return fail(INTP_ERR_INVALID_ARGUMENT, "unknown precision");
     if (desc->refine_steps < -1 || desc->refine_steps > 4)
         return fail(INTP_ERR_INVALID_ARGUMENT, "refine_steps must be in [-1, 4]");
+    if (desc->channels < 0 || desc->channels > INTP_GPU_MAX_CHANNELS)
+        return fail(INTP_ERR_INVALID_ARGUMENT, "channels must be in [0, 64]");
     TableSpec spec;
     spec.dim = desc->dim;
     spec.order = desc->order;
@@ -454,6 +463,7 @@ intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaS
     }
     t->precision = desc->precision;
     t->refine_steps = desc->refine_steps;
+    t->channels = desc->channels > 1 ? desc->channels : 1;
     t->stream_ordered = stream_ordered;
     t->alloc_stream = stream;
     for (int d = 0; d < desc->dim; ++d) t->lo_user[d] = desc->range_lo[d];
@@ -468,7 +478,7 @@ intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaS
 }
 
 size_t table_device_bytes(const intp_table* t) {
-    return t->arena_bytes + static_cast<size_t>(t->model.total) * t->elem() + t->scratch_bytes;
+    return t->arena_bytes + static_cast<size_t>(t->values()) * t->elem() + t->scratch_bytes;
 }
 
 size_t table_build_scratch_bytes(const intp_table_desc* desc) {
@@ -486,7 +496,7 @@ void table_release_scratch(intp_table* t) {
     t->scratch_bytes = 0;
 }
 
-int64_t table_values(const intp_table* t) { return t->model.total; }
+int64_t table_values(const intp_table* t) { return t->values(); }
 
 void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
     const int O = m.order;
@@ -540,6 +550,8 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
     const int O = m.order;
     dv.dim = m.dim;
     dv.order = O;
+    dv.channels = 1;
+    dv.chan_stride = m.total;
     int64_t stride = 1;
     for (int d = m.dim - 1; d >= 0; --d) {
         const AxisModel& ax = m.axis[d];
@@ -620,7 +632,7 @@ intp_status intp_table_interpolate(intp_table* t, const double* values, int32_t 
                                    void* stream) {
     if (!t || !values) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int64_t N = t->model.total;
+    const int64_t N = t->values();
     if (values_on_device) return run_interpolate(t, values, s);
     // host values: stage them on the device first
     void* stage = nullptr;
@@ -632,15 +644,21 @@ intp_status intp_table_interpolate(intp_table* t, const double* values, int32_t 
     return st;
 }
 
+// Control points cross the boundary as prod(size) x C doubles, channel
+// fastest (the reference's plain mesh of T values); on the device each
+// channel's mesh is contiguous.
 intp_status intp_table_set_control_points(intp_table* t, const double* ctrl) {
     if (!t || !ctrl) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
-    const int64_t N = t->model.total;
+    const int64_t P = t->model.total, C = t->channels, N = P * C;
+    std::vector<double> v(static_cast<size_t>(N));
+    for (int64_t i = 0; i < P; ++i)
+        for (int64_t c = 0; c < C; ++c) v[c * P + i] = ctrl[i * C + c];
     if (t->mixed()) {
         std::vector<float> f(static_cast<size_t>(N));
-        for (int64_t i = 0; i < N; ++i) f[i] = static_cast<float>(ctrl[i]);
+        for (int64_t i = 0; i < N; ++i) f[i] = static_cast<float>(v[i]);
         INTP_CUDA(cudaMemcpy(t->ctrl, f.data(), N * 4, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
     } else {
-        INTP_CUDA(cudaMemcpy(t->ctrl, ctrl, N * 8, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
+        INTP_CUDA(cudaMemcpy(t->ctrl, v.data(), N * 8, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
     }
     t->has_ctrl = true;
     return INTP_OK;
@@ -649,15 +667,18 @@ intp_status intp_table_set_control_points(intp_table* t, const double* ctrl) {
 intp_status intp_table_get_control_points(const intp_table* t, double* out) {
     if (!t || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     if (!t->has_ctrl) return fail(INTP_ERR_STATE, "table has no control points yet");
-    const int64_t N = t->model.total;
+    const int64_t P = t->model.total, C = t->channels, N = P * C;
     INTP_CUDA(cudaDeviceSynchronize(), "synchronize");
+    std::vector<double> v(static_cast<size_t>(N));
     if (t->mixed()) {
         std::vector<float> f(static_cast<size_t>(N));
         INTP_CUDA(cudaMemcpy(f.data(), t->ctrl, N * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
-        for (int64_t i = 0; i < N; ++i) out[i] = f[i];
+        for (int64_t i = 0; i < N; ++i) v[i] = f[i];
     } else {
-        INTP_CUDA(cudaMemcpy(out, t->ctrl, N * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+        INTP_CUDA(cudaMemcpy(v.data(), t->ctrl, N * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
     }
+    for (int64_t i = 0; i < P; ++i)
+        for (int64_t c = 0; c < C; ++c) out[i * C + c] = v[c * P + i];
     return INTP_OK;
 }
 
@@ -719,7 +740,7 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     if (!coords || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int D = t->model.dim;
-    const int K = derivs ? nderiv : 1;
+    const int K = (derivs ? nderiv : 1) * t->channels;  // output values per point
     const size_t osz = out_dtype == INTP_F32 ? 4 : 8;
     const int64_t chunk = eval_chunk();
     if (npts <= chunk) {

@@ -44,6 +44,8 @@ struct TableDev {
     int32_t order;
     AxisDev ax[kDevMaxDim];
     const void* ctrl;        // float (mixed) or double (fp64) control points, row-major
+    int32_t channels;        // values per mesh point (vector-valued tables; 1 = scalar)
+    int64_t chan_stride;     // control points of one channel (channel-major storage)
 };
 
 // Spatial buckets of the binned evaluation. Local span index l_d = c_d - O

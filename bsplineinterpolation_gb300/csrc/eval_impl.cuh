@@ -137,23 +137,31 @@ __device__ __forceinline__ void eval_point(const TableDev& t, const double* __re
 #pragma unroll
         for (int i = 0; i < W; ++i) off[d][i] = wrap_index(c - O + i, a.n, a.periodic) * a.stride;
     }
+    // vector-valued tables: channel ch's control points start at
+    // ch * chan_stride; the weights above are shared by all channels, and
+    // output k of channel ch goes to out[(o0 + k) * C + ch]
+    const int C = t.channels;
     if constexpr (MIXED) {
-        // same per-query code as the binned kernel (identical results)
-        const float cref = __ldg(cp + bucket_centre_offset<D, O>(t, cell));
-        mixed_point_outputs<D, O>(
-            t, plan, cell, xr, base, cref,
-            [&](const int (&ix)[D]) {
-                int64_t o = 0;
+        for (int ch = 0; ch < C; ++ch) {
+            const R* __restrict__ cpc = cp + ch * t.chan_stride;
+            // same per-query code as the binned kernel (identical results)
+            const float cref = __ldg(cpc + bucket_centre_offset<D, O>(t, cell));
+            mixed_point_outputs<D, O>(
+                t, plan, cell, xr, base, cref,
+                [&](const int (&ix)[D]) {
+                    int64_t o = 0;
 #pragma unroll
-                for (int d = 0; d < D; ++d) o += off[d][ix[d]];
-                return __ldg(cp + o) - cref;
-            },
-            [out, out_f32, o0](int k, float v) {
-                if (out_f32)
-                    static_cast<float*>(out)[o0 + k] = v;
-                else
-                    static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
-            });
+                    for (int d = 0; d < D; ++d) o += off[d][ix[d]];
+                    return __ldg(cpc + o) - cref;
+                },
+                [out, out_f32, o0, C, ch](int k, float v) {
+                    const int64_t e = (o0 + k) * C + ch;
+                    if (out_f32)
+                        static_cast<float*>(out)[e] = v;
+                    else
+                        static_cast<double*>(out)[e] = static_cast<double>(v);
+                });
+        }
     } else {
         for (int k = 0; k < K; ++k) {
             R w[D][W];
@@ -171,50 +179,54 @@ __device__ __forceinline__ void eval_point(const TableDev& t, const double* __re
                     deriv_transform<O, R>(t.ax[d], cell[d], kd, w[d]);
                 }
             }
-            R acc = 0;
-            if (!zero) {
-                if constexpr (ROWS <= 64) {
+            for (int ch = 0; ch < C; ++ch) {
+                const R* __restrict__ cpc = cp + ch * t.chan_stride;
+                R acc = 0;
+                if (!zero) {
+                    if constexpr (ROWS <= 64) {
 #pragma unroll
-                    for (int r = 0; r < ROWS; ++r) {
-                        int64_t o = 0;
-                        R wr = 1;
-                        int rem = r;
+                        for (int r = 0; r < ROWS; ++r) {
+                            int64_t o = 0;
+                            R wr = 1;
+                            int rem = r;
 #pragma unroll
-                        for (int d = D - 2; d >= 0; --d) {
-                            const int i = rem % W;
-                            rem /= W;
-                            o += off[d][i];
-                            wr *= w[d][i];
+                            for (int d = D - 2; d >= 0; --d) {
+                                const int i = rem % W;
+                                rem /= W;
+                                o += off[d][i];
+                                wr *= w[d][i];
+                            }
+                            R s = 0;
+#pragma unroll
+                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cpc + o + off[D - 1][i]);
+                            acc += wr * s;
                         }
-                        R s = 0;
-#pragma unroll
-                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
-                        acc += wr * s;
-                    }
-                } else {
-                    // large (O+1)^(D-1): runtime row loop, weights from local memory
+                    } else {
+                        // large (O+1)^(D-1): runtime row loop, weights from local memory
 #pragma unroll 1
-                    for (int r = 0; r < ROWS; ++r) {
-                        int64_t o = 0;
-                        R wr = 1;
-                        int rem = r;
-                        for (int d = D - 2; d >= 0; --d) {
-                            const int i = rem % W;
-                            rem /= W;
-                            o += off[d][i];
-                            wr *= w[d][i];
-                        }
-                        R s = 0;
+                        for (int r = 0; r < ROWS; ++r) {
+                            int64_t o = 0;
+                            R wr = 1;
+                            int rem = r;
+                            for (int d = D - 2; d >= 0; --d) {
+                                const int i = rem % W;
+                                rem /= W;
+                                o += off[d][i];
+                                wr *= w[d][i];
+                            }
+                            R s = 0;
 #pragma unroll
-                        for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cp + o + off[D - 1][i]);
-                        acc += wr * s;
+                            for (int i = 0; i < W; ++i) s += w[D - 1][i] * __ldg(cpc + o + off[D - 1][i]);
+                            acc += wr * s;
+                        }
                     }
                 }
+                const int64_t e = (o0 + k) * C + ch;
+                if (out_f32)
+                    static_cast<float*>(out)[e] = static_cast<float>(acc);
+                else
+                    static_cast<double*>(out)[e] = static_cast<double>(acc);
             }
-            if (out_f32)
-                static_cast<float*>(out)[o0 + k] = static_cast<float>(acc);
-            else
-                static_cast<double*>(out)[o0 + k] = static_cast<double>(acc);
         }
     }
 }

@@ -15,7 +15,8 @@ void note_launch(int count = 1);
 
 struct ShiftDesc {
     int dim;
-    int64_t total;
+    int64_t total;     // mesh points
+    int64_t channels;  // values per point (source channel fastest, destination channel-major)
     int64_t n[4];
     int64_t shift[4];
     int64_t stride[4];

@@ -503,6 +503,7 @@ intp_status intp_server_submit_build(intp_server* s, const intp_table_desc* desc
                                      int64_t* table_id, int64_t* request_id) {
     if (!s || !desc || !values || !table_id || !request_id) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     if (desc->dim < 1 || desc->dim > INTP_GPU_MAX_DIM) return sfail(INTP_ERR_UNSUPPORTED, "dimension must be in [1, 4]");
+    if (desc->channels > 1) return sfail(INTP_ERR_UNSUPPORTED, "served tables are scalar (channels <= 1)");
     Request* r = new (std::nothrow) Request();
     if (!r) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
     r->build = true;

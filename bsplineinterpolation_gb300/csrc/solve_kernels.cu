@@ -244,9 +244,13 @@ cudaError_t launch_solve_r(R* x, int64_t n, int64_t S, int64_t nlines, int p, in
 // (InterpolationTemplate.hpp:451-462).
 template <class Ti, class To>
 __global__ void shift_copy_kernel(const Ti* __restrict__ src, To* __restrict__ dst, ShiftDesc sd) {
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < sd.total;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int64_t r = i, o = 0;
+    const int64_t C = sd.channels;
+    for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < sd.total * C;
+         j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        // source element j = point i, channel ch (channel fastest); the
+        // destination holds channel ch's mesh at ch * total
+        const int64_t i = C == 1 ? j : j / C, ch = j - i * C;
+        int64_t r = i, o = ch * sd.total;
 #pragma unroll
         for (int d = 3; d >= 0; --d) {
             if (d < sd.dim) {
@@ -261,7 +265,7 @@ __global__ void shift_copy_kernel(const Ti* __restrict__ src, To* __restrict__ d
                 o += idx * sd.stride[d];
             }
         }
-        dst[o] = static_cast<To>(src[i]);
+        dst[o] = static_cast<To>(src[j]);
     }
 }
 
@@ -322,14 +326,14 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
 
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s) {
-    shift_copy_kernel<double, double><<<grid_for(sd.total, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    shift_copy_kernel<double, double><<<grid_for(sd.total * sd.channels, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
     note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const ShiftDesc& sd,
                                       cudaStream_t s) {
-    shift_copy_kernel<double, float><<<grid_for(sd.total, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    shift_copy_kernel<double, float><<<grid_for(sd.total * sd.channels, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
     note_launch();
     return cudaGetLastError();
 }

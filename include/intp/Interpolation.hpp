@@ -65,6 +65,25 @@ using TablePtr = std::shared_ptr<intp_table>;
 
 }  // namespace gpu
 
+// How a value type T crosses the C-ABI: `channels` doubles per value, channel
+// fastest. Arithmetic types are one channel and std::array<V, N> is N (a
+// vector-valued function, as the reference interpolates Vec<N, T> values,
+// test/src/interpolation-test.cpp "interpolation on vector"). Specialise it
+// for other vector types.
+template <typename T, typename = void>
+struct value_traits {
+    static constexpr std::size_t channels = 1;
+    static double get(const T& v, std::size_t) { return static_cast<double>(v); }
+    static void set(T& v, std::size_t, double x) { v = static_cast<T>(x); }
+};
+
+template <typename V, std::size_t N>
+struct value_traits<std::array<V, N>> {
+    static constexpr std::size_t channels = N;
+    static double get(const std::array<V, N>& v, std::size_t c) { return static_cast<double>(v[c]); }
+    static void set(std::array<V, N>& v, std::size_t c, double x) { v[c] = static_cast<V>(x); }
+};
+
 namespace detail {
 
 template <typename T>
@@ -119,12 +138,16 @@ class SplineView {
     static constexpr size_type get_order() { return O; }
     // control points, row-major, copied from the device
     Mesh<T, D> control_points() const {
+        using VT = value_traits<T>;
         std::array<std::size_t, D> dims{};
         for (size_type d = 0; d < D; ++d) dims[d] = ncp_[d];
         Mesh<T, D> m{MeshDimension<D>(dims)};
-        std::vector<double> buf(m.size());
+        std::vector<double> buf(m.size() * VT::channels);
         gpu::check(intp_table_get_control_points(table_.get(), buf.data()));
-        for (std::size_t i = 0; i < buf.size(); ++i) m(m.dimension().dimwise_indices(i)) = static_cast<T>(buf[i]);
+        for (std::size_t i = 0; i < m.size(); ++i) {
+            T& v = m(m.dimension().dimwise_indices(i));
+            for (std::size_t c = 0; c < VT::channels; ++c) VT::set(v, c, buf[i * VT::channels + c]);
+        }
         return m;
     }
 
@@ -247,8 +270,8 @@ class InterpolationFunction {
     }
 
     // -- batch evaluation (the fast path) --
-    // Host buffers: coords n x D, out n x nderiv (derivs nderiv x D, or
-    // nullptr for values).
+    // Host buffers: coords n x D, out n x nderiv x C with C =
+    // value_traits<T>::channels (derivs nderiv x D, or nullptr for values).
     void evaluate(const double* coords, std::size_t n, double* out, const int32_t* derivs = nullptr,
                   int32_t nderiv = 1) const {
         gpu::check(intp_eval_host(table_.get(), coords, static_cast<int64_t>(n), derivs, nderiv, out, INTP_F64, nullptr));
@@ -278,11 +301,14 @@ class InterpolationFunction {
     }
 
     val_type eval_one(const DimArray<coord_type>& c, const int32_t* k) const {
+        using VT = value_traits<T>;
         double x[D];
         for (size_type d = 0; d < D; ++d) x[d] = static_cast<double>(c[d]);
-        double r = 0.0;
-        gpu::check(intp_eval_host(table_.get(), x, 1, k, 1, &r, INTP_F64, nullptr));
-        return static_cast<val_type>(r);
+        double r[VT::channels] = {};
+        gpu::check(intp_eval_host(table_.get(), x, 1, k, 1, r, INTP_F64, nullptr));
+        val_type v{};
+        for (std::size_t ch = 0; ch < VT::channels; ++ch) VT::set(v, ch, r[ch]);
+        return v;
     }
 
     // Interpolation.hpp:482-491
@@ -316,6 +342,7 @@ class InterpolationFunctionTemplate {
         desc_.order = static_cast<int32_t>(O);
         desc_.precision = static_cast<int32_t>(gpu::default_precision());
         desc_.refine_steps = -1;
+        desc_.channels = static_cast<int32_t>(value_traits<T>::channels);
         for (size_type d = 0; d < D; ++d) {
             desc_.periodic[d] = periodicity[d] ? 1 : 0;
             desc_.size[d] = static_cast<int64_t>(dims.dim_size(d));
@@ -354,8 +381,12 @@ class InterpolationFunctionTemplate {
         intp_table* t = nullptr;
         gpu::check(intp_table_create(&desc_, &t));
         gpu::TablePtr tp(t, gpu::TableDeleter{});
-        std::vector<double> v(mesh.size());
-        for (size_type i = 0; i < mesh.size(); ++i) v[i] = static_cast<double>(mesh(mesh.dimension().dimwise_indices(i)));
+        using VT = value_traits<T>;
+        std::vector<double> v(mesh.size() * VT::channels);
+        for (size_type i = 0; i < mesh.size(); ++i) {
+            const T& x = mesh(mesh.dimension().dimwise_indices(i));
+            for (std::size_t c = 0; c < VT::channels; ++c) v[i * VT::channels + c] = VT::get(x, c);
+        }
         gpu::check(intp_table_interpolate(tp.get(), v.data(), 0, nullptr));
         gpu::check(intp_stream_synchronize(nullptr));
         f.attach(std::move(tp), ncp_);

@@ -61,7 +61,17 @@ typedef struct intp_table_desc {
     /* non-uniform axis: host array of size[d] (+1 if periodic) increasing
      * sample coordinates; NULL for a uniform axis */
     const double* coords[INTP_GPU_MAX_DIM];
+    /* values per mesh point: 0 or 1 = scalar table; C > 1 = vector-valued
+     * table (the reference's InterpolationFunction<T, D, O> with a vector
+     * type T, Interpolation.hpp:17-507). Values and control points are then
+     * prod(size) x C, channel fastest, and every evaluation output is C
+     * values. All channels share the knots, the factors and, per query, the
+     * basis weights. Single tables only (not batches or the serving loop). */
+    int32_t channels;
+    int32_t reserved_;
 } intp_table_desc;
+
+#define INTP_GPU_MAX_CHANNELS 64
 
 /* Knot vectors, collocation matrices and their band LU factors, uploaded to
  * the current device.

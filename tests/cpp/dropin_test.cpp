@@ -14,6 +14,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <array>
 #include <vector>
 
 struct Case {
@@ -184,6 +185,32 @@ static int extras() {
     intp::InterpolationFunctionTemplate1D<3> t1(v.size());
     auto h1 = t1.interpolate(std::make_pair(v.begin(), v.end()));
     if (std::fabs(h1(4.0) - v[4]) > 1e-14) ++bad;
+    // vector-valued T (test/src/interpolation-test.cpp, interpolation on
+    // vector): 31 points on the unit circle, periodic cubic of 2-vectors
+    {
+        constexpr std::size_t pn = 31;
+        std::vector<std::array<float, 2>> pts;
+        for (std::size_t i = 0; i < pn; ++i) {
+            const double th = 2. * M_PI * static_cast<double>(i) / pn;
+            pts.push_back({static_cast<float>(std::cos(th)), static_cast<float>(std::sin(th))});
+        }
+        intp::InterpolationFunction1D<3, std::array<float, 2>, float> circle(std::make_pair(pts.begin(), pts.end()),
+                                                                              true);
+        float err = 0;
+        constexpr std::size_t sn = 1024;
+        for (std::size_t i = 0; i < sn; ++i) {
+            const float th = 2.f * static_cast<float>(M_PI) * static_cast<float>(i) / sn;
+            const std::array<float, 2> p = circle(th);
+            err += std::fabs(std::hypot(p[0], p[1]) - 1.f);
+        }
+        err /= sn;
+        if (!(err < 1e-5f)) {
+            std::printf("vector circle error %g\n", static_cast<double>(err));
+            ++bad;
+        }
+        const auto cp = circle.spline().control_points();
+        if (cp.size() != pn) ++bad;
+    }
     std::printf("extras %d\n", bad);
     return bad;
 }
