@@ -162,20 +162,15 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
     R* base = data + off[it.table];
     if (it.staged) {
         // S == 1: lines line0 .. line0+rows-1 are one contiguous run of rows*n
-        const int64_t pitch = n + 1;
+        const int ni = static_cast<int>(n), pitch = ni + 1;
         R* src = base + it.line0 * n;
-        const int64_t total = static_cast<int64_t>(it.rows) * n;
-        for (int64_t e = lane; e < total; e += 32) {
-            const int64_t r = e / n, k = e - r * n;
-            tile[r * pitch + k] = src[e];
-        }
+        for (int r = 0; r < it.rows; ++r)
+            for (int k = lane; k < ni; k += 32) tile[r * pitch + k] = src[static_cast<int64_t>(r) * ni + k];
         __syncwarp();
         if (lane < it.rows) solve_dispatch<R>(band.x, band.y != 0, fv, SmemLine<R>{tile + lane * pitch});
         __syncwarp();
-        for (int64_t e = lane; e < total; e += 32) {
-            const int64_t r = e / n, k = e - r * n;
-            src[e] = tile[r * pitch + k];
-        }
+        for (int r = 0; r < it.rows; ++r)
+            for (int k = lane; k < ni; k += 32) src[static_cast<int64_t>(r) * ni + k] = tile[r * pitch + k];
         return;
     }
     if (lane < it.rows) {
@@ -185,8 +180,26 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
     }
 }
 
-// Residual pass of the refinement: one lane per line, mid = A_axis in, or
-// res = fsh - A_axis in on the table's last pass (axis 0).
+// Residual pass of the refinement: mid = A_axis in, or res = fsh - A_axis in
+// on the table's last pass (axis 0), for every line of the item. Each output
+// element is an independent sparse row product (stencil_row, the arithmetic
+// of the single-table stencil), so the lanes spread over the elements of each
+// line of the contiguous axis (coalesced) and over adjacent lines of a
+// strided axis.
+template <class Ti>
+__device__ __forceinline__ void stencil_row(const Ti* __restrict__ in, double* __restrict__ out,
+                                            const double* __restrict__ rhs, int64_t base, int64_t i, int64_t S,
+                                            int width, const int64_t* __restrict__ col,
+                                            const double* __restrict__ val) {
+    double acc = 0.0;
+    for (int w = 0; w < width; ++w) {
+        const double a = __ldg(val + i * width + w);
+        const int64_t j = __ldg(col + i * width + w);
+        acc = fma(a, static_cast<double>(in[base + j * S]), acc);
+    }
+    out[base + i * S] = rhs ? rhs[base + i * S] - acc : acc;
+}
+
 template <class Ti>
 __global__ void __launch_bounds__(32) batch_stencil_kernel(const Ti* __restrict__ in, double* __restrict__ mid,
                                                            double* __restrict__ res, const double* __restrict__ fsh,
@@ -198,17 +211,25 @@ __global__ void __launch_bounds__(32) batch_stencil_kernel(const Ti* __restrict_
     const SolveItem it = items[blockIdx.x];
     if (refine[it.table] <= step) return;
     const int lane = threadIdx.x;
-    if (lane >= it.rows) return;
     const TableDev& t = tables[it.table];
     const AxisDev& ax = t.ax[it.axis];
     const AxisFactorDev& f = fac[it.table * kBatchMaxDim + it.axis];
     const int64_t n = ax.n, S = ax.stride;
-    const int64_t l = it.line0 + lane;
-    const int64_t o = l / S, tt = l - o * S;
     const int64_t o0 = off[it.table];
     double* out = it.last ? res + o0 : mid + o0;
     const double* rhs = it.last ? fsh + o0 : nullptr;
-    stencil_line<Ti>(in + o0, out, rhs, o * n * S + tt, n, S, f.width, f.scol, f.sval);
+    if (S == 1) {
+        for (int r = 0; r < it.rows; ++r) {
+            const int64_t base = (it.line0 + r) * n;
+            for (int64_t i = lane; i < n; i += 32) stencil_row<Ti>(in + o0, out, rhs, base, i, 1, f.width, f.scol, f.sval);
+        }
+        return;
+    }
+    if (lane >= it.rows) return;
+    const int64_t l = it.line0 + lane;
+    const int64_t o = l / S, tt = l - o * S;
+    const int64_t base = o * n * S + tt;
+    for (int64_t i = 0; i < n; ++i) stencil_row<Ti>(in + o0, out, rhs, base, i, S, f.width, f.scol, f.sval);
 }
 
 // Element-wise passes over chunk items:
@@ -231,19 +252,21 @@ __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const do
     const int64_t o0 = off[c.table];
     if (op == 0) {
         const TableDev& t = tables[c.table];
+        // batched tables hold fewer than 2^31 values each: 32-bit index math
         for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
             const int64_t i = c.start + e;
-            int64_t r = i, o = 0;
+            int r = static_cast<int>(i), o = 0;
             for (int d = t.dim - 1; d >= 0; --d) {
                 const AxisDev& a = t.ax[d];
-                const int64_t q = r / a.n;
-                int64_t idx = r - q * a.n;
+                const int na = static_cast<int>(a.n);
+                const int q = r / na;
+                int idx = r - q * na;
                 r = q;
                 if (a.periodic) {
-                    idx += (t.order / 2) % a.n;
-                    if (idx >= a.n) idx -= a.n;
+                    idx += (t.order / 2) % na;
+                    if (idx >= na) idx -= na;
                 }
-                o += idx * a.stride;
+                o += idx * static_cast<int>(a.stride);
             }
             const double v = src[o0 + i];
             dst[o0 + o] = static_cast<R>(v);
@@ -473,6 +496,10 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
             if (!err.empty()) {
                 delete b;
                 return bfail(INTP_ERR_INVALID_ARGUMENT, where + err);
+            }
+            if (b->models[i].total >= (int64_t{1} << 31)) {
+                delete b;
+                return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables hold fewer than 2^31 values each");
             }
             b->off[i + 1] = b->off[i] + b->models[i].total;
             if (b->mixed()) {

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128) solve_strided_kernel(R* __restrict__ x, i
 template <class R, int P, int Q, bool CYC>
 __global__ void __launch_bounds__(32) solve_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
                                                           FactorView<R> f) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     R* tile = reinterpret_cast<R*>(smem_raw);
     const int64_t pitch = n + 1;
     const int lane = threadIdx.x;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(32) solve_tile_strided_kernel(R* __restrict__ 
 template <class R, int P, int Q, bool CYC>
 __global__ void __launch_bounds__(32) solve_tile_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
                                                                FactorView<R> f) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     R* tile = reinterpret_cast<R*>(smem_raw);
     const int64_t pitch = n + 1;
     const int lane = threadIdx.x;
@@ -284,6 +284,27 @@ __global__ void __launch_bounds__(128) stencil_kernel(const Ti* __restrict__ in,
     }
 }
 
+// Contiguous axis (S = 1): one block per line, threads over its elements
+// (coalesced); each element is the same row product as in stencil_line.
+template <class Ti>
+__global__ void __launch_bounds__(256) stencil_contig_kernel(const Ti* __restrict__ in, double* __restrict__ out,
+                                                             const double* __restrict__ rhs, int64_t n, int64_t nlines,
+                                                             int width, const int64_t* __restrict__ col,
+                                                             const double* __restrict__ val) {
+    for (int64_t l = blockIdx.x; l < nlines; l += gridDim.x) {
+        const int64_t base = l * n;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            double acc = 0.0;
+            for (int w = 0; w < width; ++w) {
+                const double a = __ldg(val + i * width + w);
+                const int64_t j = __ldg(col + i * width + w);
+                acc = fma(a, static_cast<double>(in[base + j]), acc);
+            }
+            out[base + i] = rhs ? rhs[base + i] - acc : acc;
+        }
+    }
+}
+
 template <class Ti, class To>
 __global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
@@ -341,6 +362,12 @@ cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const Shift
 cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs, int64_t n, int64_t S,
                                  int64_t nlines, int width, const int64_t* col, const double* val,
                                  cudaStream_t s) {
+    if (S == 1) {
+        stencil_contig_kernel<float><<<grid_for(nlines, 1, 152 * 64), 256, 0, s>>>(in, out, rhs, n, nlines, width,
+                                                                                col, val);
+        note_launch();
+        return cudaGetLastError();
+    }
     stencil_kernel<float><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
                                                                         width, col, val);
     note_launch();
@@ -350,6 +377,12 @@ cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs
 cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
                                  int64_t S, int64_t nlines, int width, const int64_t* col,
                                  const double* val, cudaStream_t s) {
+    if (S == 1) {
+        stencil_contig_kernel<double><<<grid_for(nlines, 1, 152 * 64), 256, 0, s>>>(in, out, rhs, n, nlines, width,
+                                                                                 col, val);
+        note_launch();
+        return cudaGetLastError();
+    }
     stencil_kernel<double><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
                                                                          width, col, val);
     note_launch();
