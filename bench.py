@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop workload")
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--batched-tables", type=int, default=4096)
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the batched-tables workload (profiling)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving-loop workload")
     return ap.parse_args()
 
 
@@ -601,6 +604,11 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    if args.batched_only or args.serve_only:
+        import torch
+        res = run_batched(args, torch) if args.batched_only else run_serving(args, torch)
+        print(json.dumps(res), flush=True)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus else 1))
     if args.impl == "reference":
