@@ -151,8 +151,7 @@ cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* co
     return cudaErrorInvalidValue;
 }
 
-BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes) {
-    (void)tile_bytes;
+BinGeom make_bin_geom(const TableDev& t) {
     BinGeom g{};
     const int D = t.dim, O = t.order;
     g.dim = D;

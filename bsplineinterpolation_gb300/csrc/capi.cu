@@ -25,9 +25,7 @@ namespace {
 
 std::atomic<unsigned long long> g_launches{0};
 
-// binned evaluation: shared-memory tile budget per CTA, queries per chunk
-// (chunk outputs stay L2-resident), smallest batch worth binning
-constexpr int64_t kTileBytes = 48 * 1024;
+// binned evaluation: queries per chunk, smallest batch worth binning
 constexpr int64_t kDefaultChunk = int64_t{1} << 24;
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
@@ -44,7 +42,8 @@ int64_t eval_chunk() {
     const char* v = std::getenv("INTP_GB300_CHUNK");
     if (!v) return kDefaultChunk;
     const long long c = std::atoll(v);
-    return c >= 1024 ? c : kDefaultChunk;
+    // a record holds its query's index within a sort CTA's slice in 20 bits
+    return c >= 1024 ? std::min<long long>(c, int64_t{1} << 28) : kDefaultChunk;
 }
 
 // Keep memory freed by cudaFreeAsync in the device's default pool so
@@ -211,7 +210,7 @@ intp_status upload_table(intp_table* t) {
     // the binned path stages one channel's tiles: vector-valued tables
     // evaluate with the direct kernel
     if (t->mixed() && m.dim <= 3 && t->channels == 1) {
-        t->bins = make_bin_geom(t->dev, kTileBytes);
+        t->bins = make_bin_geom(t->dev);
         if (t->bins.smem_buckets > 0) t->has_tile_map = make_tile_map(t);
     }
     return INTP_OK;

@@ -22,7 +22,7 @@ struct ShiftDesc {
     int64_t stride[4];
 };
 
-// evaluation (eval_kernels.cu)
+// direct evaluation (eval_misc.cu dispatching to eval_f32_* / eval_f64_*)
 cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coords, int64_t npts,
                                const DerivPlan& plan, void* out, bool out_f32, cudaStream_t s);
 // Binned evaluation of the mixed form (bin_host.cu); `chunk` queries per round.
@@ -49,8 +49,10 @@ cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const CUtensorMa
 // Read and clear the device error flag of the binned evaluation units.
 int take_device_error_bin_d12(cudaStream_t s);
 int take_device_error_bin_d3(cudaStream_t s);
-// Bucket geometry for a table (tile of at most `tile_bytes` FP32 control points).
-BinGeom make_bin_geom(const TableDev& t, int64_t tile_bytes);
+// Bucket geometry of the binned evaluation for a table: compile-time bucket
+// sizes per dimension (bucket_log2); smem_buckets = 0 when the table has too
+// many buckets or too many knots for the binned path.
+BinGeom make_bin_geom(const TableDev& t);
 
 cudaError_t launch_locate(const TableDev& t, const double* coords, int64_t npts, int64_t* cells,
                           double* wrapped, cudaStream_t s);
