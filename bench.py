@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--npts", type=int, default=N_PTS)
     ap.add_argument("--mesh", type=int, default=N_MESH)
+    ap.add_argument("--refine", type=int, default=-1,
+                    help="refinement steps of the mixed solve (-1: the table's automatic choice)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement")
@@ -267,7 +269,7 @@ def run_ours(args, rank, world):
 
     def build(precision):
         return bi.InterpolationFunction(3, [False] * 3, vals, (-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0),
-                                        precision=precision)
+                                        precision=precision, refine_steps=args.refine)
 
     def timed_steps(f, steps, warmup, out):
         tpl = f._template
@@ -322,7 +324,7 @@ def run_ours(args, rank, world):
         "config": {"workload": "3D cubic 256^3 build + 1e8 queries value+d/dx"
                    if (n == N_MESH and npts == N_PTS) else "3D cubic %d^3 build + %d queries" % (n, npts),
                    "mesh": [n, n, n], "order": 3, "periodic": [False] * 3, "queries": npts,
-                   "outputs": ["value", "d/dx"], "precision": prec,
+                   "outputs": ["value", "d/dx"], "precision": prec, "refine_steps": args.refine,
                    "l2": "inputs larger than L2 (values %.0f MB, coordinates %.0f MB)"
                          % (n ** 3 * 8 / 1e6, npts * 24 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},

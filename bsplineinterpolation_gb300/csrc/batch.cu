@@ -10,8 +10,9 @@
 // longest lines first. The arithmetic per line is solve_line, the same as the
 // single-table solves, so a batched table gets the control points that
 // intp_table_interpolate gives it, bit for bit. Mixed-precision batches
-// refine per table (FP64 residual, FP32 correction) with the same step count
-// a single table would choose.
+// refine per table (double-float residual, FP32 correction, double-float
+// control points) with the same step count and the same arithmetic as a
+// single table.
 //
 // Evaluation takes one list of query runs per (dimension, order) class and
 // evaluates each run with the per-point code of the direct kernel
@@ -27,6 +28,7 @@
 #include "batch.hpp"
 #include "intp_gpu.h"
 #include "launch.hpp"
+#include "refine_df.cuh"
 #include "solve_line.cuh"
 #include "spline_model.hpp"
 #include "table_pack.hpp"
@@ -56,6 +58,7 @@ struct intp_batch {
     std::vector<TableDev> h_tables;
     void* arena = nullptr;         // per-axis data, descriptors, work lists
     void* ctrl = nullptr;
+    float* ctrl_lo = nullptr;      // control-point remainders of refining tables (mixed)
     void* scratch = nullptr;       // refinement buffers
     size_t scratch_bytes = 0;
     TableDev* d_tables = nullptr;
@@ -76,6 +79,7 @@ struct intp_batch {
     ~intp_batch() {
         if (arena) cudaFree(arena);
         if (ctrl) cudaFree(ctrl);
+        if (ctrl_lo) cudaFree(ctrl_lo);
         if (scratch) cudaFree(scratch);
     }
     bool mixed() const { return precision == INTP_PRECISION_MIXED; }
@@ -180,29 +184,18 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
     }
 }
 
-// Residual pass of the refinement: mid = A_axis in, or res = fsh - A_axis in
-// on the table's last pass (axis 0), for every line of the item. Each output
-// element is an independent sparse row product (stencil_row, the arithmetic
-// of the single-table stencil), so the lanes spread over the elements of each
-// line of the contiguous axis (coalesced) and over adjacent lines of a
-// strided axis.
-template <class Ti>
-__device__ __forceinline__ void stencil_row(const Ti* __restrict__ in, double* __restrict__ out,
-                                            const double* __restrict__ rhs, int64_t base, int64_t i, int64_t S,
-                                            int width, const int64_t* __restrict__ col,
-                                            const double* __restrict__ val) {
-    double acc = 0.0;
-    for (int w = 0; w < width; ++w) {
-        const double a = __ldg(val + i * width + w);
-        const int64_t j = __ldg(col + i * width + w);
-        acc = fma(a, static_cast<double>(in[base + j * S]), acc);
-    }
-    out[base + i * S] = rhs ? rhs[base + i * S] - acc : acc;
-}
-
-template <class Ti>
-__global__ void __launch_bounds__(32) batch_stencil_kernel(const Ti* __restrict__ in, double* __restrict__ mid,
-                                                           double* __restrict__ res, const double* __restrict__ fsh,
+// Residual pass of the refinement with Dot2 accumulation: mid = A_axis in
+// as a double-float, or corr = F - A_axis in (FP32) on the table's last pass
+// (axis 0), for every line of the item. Each output element is an
+// independent sparse row product (dot2_row, the arithmetic of the
+// single-table residual), so the lanes spread over the elements of each line
+// of the contiguous axis (coalesced) and over adjacent lines of a strided
+// axis. HAS_LO: the input is double-float (else plain FP32).
+template <bool HAS_LO>
+__global__ void __launch_bounds__(32) batch_stencil_kernel(const float* __restrict__ in_hi,
+                                                           const float* __restrict__ in_lo, float* __restrict__ mid_hi,
+                                                           float* __restrict__ mid_lo, float* __restrict__ corr,
+                                                           const float* __restrict__ fhi, const float* __restrict__ flo,
                                                            const SolveItem* __restrict__ items,
                                                            const TableDev* __restrict__ tables,
                                                            const AxisFactorDev* __restrict__ fac,
@@ -214,35 +207,51 @@ __global__ void __launch_bounds__(32) batch_stencil_kernel(const Ti* __restrict_
     const TableDev& t = tables[it.table];
     const AxisDev& ax = t.ax[it.axis];
     const AxisFactorDev& f = fac[it.table * kBatchMaxDim + it.axis];
-    const int64_t n = ax.n, S = ax.stride;
+    // batched tables hold fewer than 2^31 values each: 32-bit index math
+    const int n = static_cast<int>(ax.n), S = static_cast<int>(ax.stride);
     const int64_t o0 = off[it.table];
-    double* out = it.last ? res + o0 : mid + o0;
-    const double* rhs = it.last ? fsh + o0 : nullptr;
+    const float* ih = in_hi + o0;
+    const float* il = HAS_LO ? in_lo + o0 : nullptr;
+    auto row = [&](int base, int i) {
+        const int e = base + i * S;
+        Dot2 acc{0.0f, 0.0f};
+        if (it.last) acc = Dot2{fhi[o0 + e], flo[o0 + e]};
+        dot2_row<HAS_LO, int>(acc, it.last ? -1.0f : 1.0f, ih, il, base, i, S, f.width, f.scol, f.sval);
+        if (it.last) {
+            corr[o0 + e] = __fadd_rn(acc.s, acc.c);
+        } else {
+            const DF v = dot2_value(acc);
+            mid_hi[o0 + e] = v.hi;
+            mid_lo[o0 + e] = v.lo;
+        }
+    };
     if (S == 1) {
         for (int r = 0; r < it.rows; ++r) {
-            const int64_t base = (it.line0 + r) * n;
-            for (int64_t i = lane; i < n; i += 32) stencil_row<Ti>(in + o0, out, rhs, base, i, 1, f.width, f.scol, f.sval);
+            const int base = static_cast<int>(it.line0 + r) * n;
+            for (int i = lane; i < n; i += 32) row(base, i);
         }
         return;
     }
     if (lane >= it.rows) return;
-    const int64_t l = it.line0 + lane;
-    const int64_t o = l / S, tt = l - o * S;
-    const int64_t base = o * n * S + tt;
-    for (int64_t i = 0; i < n; ++i) stencil_row<Ti>(in + o0, out, rhs, base, i, S, f.width, f.scol, f.sval);
+    const int l = static_cast<int>(it.line0) + lane;
+    const int o = l / S, tt = l - o * S;
+    const int base = o * n * S + tt;
+    for (int i = 0; i < n; ++i) row(base, i);
 }
 
 // Element-wise passes over chunk items:
-//  op 0: dst[shift(i)] = (R) src[i] (and fsh[shift(i)] = src[i] when fsh)
-//  op 1: corr[i] = (float) res[i]            (refining tables only)
-//  op 2: ctrl[i] += corr[i]                  (refining tables only)
+//  op 0: dst[shift(i)] = (R) src[i], or for refining tables with fhi (FP32
+//        destination) the double-float split of src[i] into fhi[shift(i)]
+//        (= dst) and flo[shift(i)]
+//  op 1: (ctrl, ctrl_lo)[i] += corr[i] in double-float  (refining tables only)
 // The periodic shift moves index i to (i + O/2) mod n along every periodic
 // axis (InterpolationTemplate.hpp:451-462).
 template <class R>
 __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const double* __restrict__ src,
-                                                                R* __restrict__ dst, double* __restrict__ fsh,
-                                                                const double* __restrict__ res,
-                                                                float* __restrict__ corr,
+                                                                R* __restrict__ dst, float* __restrict__ fhi,
+                                                                float* __restrict__ flo,
+                                                                float* __restrict__ ctrl_lo,
+                                                                const float* __restrict__ corr,
                                                                 const ChunkItem* __restrict__ chunks,
                                                                 const TableDev* __restrict__ tables,
                                                                 const int64_t* __restrict__ off,
@@ -269,19 +278,28 @@ __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const do
                 o += idx * static_cast<int>(a.stride);
             }
             const double v = src[o0 + i];
+            if constexpr (sizeof(R) == 4) {
+                if (fhi && refine[c.table] > 0) {
+                    // integer split, as the single-table shift copy of a
+                    // refining table
+                    float h, l;
+                    split_double(v, h, l);
+                    dst[o0 + o] = h;
+                    fhi[o0 + o] = h;
+                    flo[o0 + o] = l;
+                    continue;
+                }
+            }
             dst[o0 + o] = static_cast<R>(v);
-            if (fsh) fsh[o0 + o] = v;
-        }
-    } else if (op == 1) {
-        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
-            const int64_t i = o0 + c.start + e;
-            corr[i] = static_cast<float>(res[i]);
         }
     } else {
         float* x = reinterpret_cast<float*>(dst);
         for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
             const int64_t i = o0 + c.start + e;
-            x[i] += corr[i];
+            float h = x[i], l = step > 0 ? ctrl_lo[i] : 0.0f;
+            df_correct(h, l, corr[i], step > 0);
+            x[i] = h;
+            ctrl_lo[i] = l;
         }
     }
 }
@@ -378,8 +396,8 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
     const unsigned nch = static_cast<unsigned>(b->nchunks);
     if (!b->mixed()) {
         double* c = static_cast<double*>(b->ctrl);
-        batch_elementwise_kernel<double><<<nch, 256, 0, s>>>(0, values, c, nullptr, nullptr, nullptr, b->d_chunks,
-                                                             b->d_tables, b->d_off, b->d_refine, -1);
+        batch_elementwise_kernel<double><<<nch, 256, 0, s>>>(0, values, c, nullptr, nullptr, nullptr, nullptr,
+                                                             b->d_chunks, b->d_tables, b->d_off, b->d_refine, -1);
         note_launch();
         BATCH_CUDA(cudaGetLastError(), "batch shift copy");
         BATCH_CUDA(run_passes<double>(b, c, -1, bands, s), "batch line solve (fp64)");
@@ -387,11 +405,10 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
         return INTP_OK;
     }
     float* c = static_cast<float*>(b->ctrl);
-    double* fsh = nullptr;
-    double *tmp = nullptr, *tmp2 = nullptr, *res = nullptr;
-    float* corr = nullptr;
+    float *fhi = nullptr, *flo = nullptr, *corr = nullptr;
+    float* ping[2][2] = {};
     if (b->max_refine > 0) {
-        const size_t need = static_cast<size_t>(N) * (8 * 4 + 4) + 1024;
+        const size_t need = static_cast<size_t>(N) * 28 + 1024;
         if (b->scratch_bytes < need) {
             if (b->scratch) cudaFree(b->scratch);
             b->scratch = nullptr;
@@ -399,40 +416,39 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
             BATCH_CUDA(cudaMalloc(&b->scratch, need), "cudaMalloc(batch refinement scratch)");
             b->scratch_bytes = need;
         }
-        unsigned char* p = static_cast<unsigned char*>(b->scratch);
-        fsh = reinterpret_cast<double*>(p);
-        tmp = reinterpret_cast<double*>(p + N * 8);
-        tmp2 = reinterpret_cast<double*>(p + N * 16);
-        res = reinterpret_cast<double*>(p + N * 24);
-        corr = reinterpret_cast<float*>(p + N * 32);
+        float* p = static_cast<float*>(b->scratch);
+        fhi = p;
+        flo = p + N;
+        ping[0][0] = p + 2 * N;
+        ping[0][1] = p + 3 * N;
+        ping[1][0] = p + 4 * N;
+        ping[1][1] = p + 5 * N;
+        corr = p + 6 * N;
     }
-    batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(0, values, c, fsh, nullptr, nullptr, b->d_chunks, b->d_tables,
-                                                        b->d_off, b->d_refine, -1);
+    batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(0, values, c, fhi, flo, nullptr, nullptr, b->d_chunks,
+                                                        b->d_tables, b->d_off, b->d_refine, -1);
     note_launch();
     BATCH_CUDA(cudaGetLastError(), "batch shift copy");
     BATCH_CUDA(run_passes<float>(b, c, -1, bands, s), "batch line solve (fp32)");
     for (int step = 0; step < b->max_refine; ++step) {
-        // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass, FP64:
-        // c -> tmp -> tmp2 -> ..., each table's last pass writing res
+        // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass, double-float:
+        // c -> ping[0] -> ping[1] -> ..., each table's last pass writing corr
+        const float *ih = c, *il = step > 0 ? b->ctrl_lo : nullptr;
         for (int j = 0; j < b->npasses; ++j) {
             const intp_batch::Pass& p = b->pass[j];
             if (p.nitems == 0) continue;
-            if (j == 0)
-                batch_stencil_kernel<float><<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(
-                    c, tmp, res, fsh, p.items, b->d_tables, b->d_fac, b->d_off, b->d_refine, step);
-            else
-                batch_stencil_kernel<double><<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(
-                    j == 1 ? tmp : tmp2, j == 1 ? tmp2 : tmp, res, fsh, p.items, b->d_tables, b->d_fac, b->d_off,
-                    b->d_refine, step);
+            float** out = ping[j & 1];
+            auto k = il ? batch_stencil_kernel<true> : batch_stencil_kernel<false>;
+            k<<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(ih, il, out[0], out[1], corr, fhi, flo, p.items,
+                                                             b->d_tables, b->d_fac, b->d_off, b->d_refine, step);
             note_launch();
             BATCH_CUDA(cudaGetLastError(), "batch residual");
+            ih = out[0];
+            il = out[1];
         }
-        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, nullptr, nullptr, res, corr, b->d_chunks,
-                                                            b->d_tables, b->d_off, b->d_refine, step);
-        note_launch();
         BATCH_CUDA(run_passes<float>(b, corr, step, bands, s), "batch line solve (correction)");
-        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(2, nullptr, c, nullptr, nullptr, corr, b->d_chunks,
-                                                            b->d_tables, b->d_off, b->d_refine, step);
+        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, c, nullptr, nullptr, b->ctrl_lo, corr,
+                                                            b->d_chunks, b->d_tables, b->d_off, b->d_refine, step);
         note_launch();
         BATCH_CUDA(cudaGetLastError(), "batch correction");
     }
@@ -543,6 +559,8 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     }
     const size_t N = static_cast<size_t>(b->off[ntables]);
     e = cudaMalloc(&b->ctrl, std::max<size_t>(N, 1) * b->elem());
+    if (e == cudaSuccess && b->max_refine > 0)
+        e = cudaMalloc(reinterpret_cast<void**>(&b->ctrl_lo), std::max<size_t>(N, 1) * sizeof(float));
     if (e != cudaSuccess) {
         delete b;
         return bcuda(e, "cudaMalloc(batch control points)");
@@ -557,6 +575,7 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
         std::memset(&dv, 0, sizeof dv);
         bind_table(b->models[i], lo_user, packed[i], base, dv, &fac[i * kBatchMaxDim]);
         dv.ctrl = static_cast<const unsigned char*>(b->ctrl) + static_cast<size_t>(b->off[i]) * b->elem();
+        dv.ctrl_lo = b->refine[i] > 0 ? b->ctrl_lo + b->off[i] : nullptr;
     }
     std::memcpy(ar.host.data() + o_tables, b->h_tables.data(), sizeof(TableDev) * static_cast<size_t>(ntables));
     std::memcpy(ar.host.data() + o_fac, fac.data(), sizeof(AxisFactorDev) * fac.size());
@@ -617,9 +636,14 @@ intp_status intp_batch_get_control_points(const intp_batch* b, int64_t table, do
     BATCH_CUDA(cudaDeviceSynchronize(), "synchronize");
     const unsigned char* src = static_cast<const unsigned char*>(b->ctrl) + static_cast<size_t>(b->off[table]) * b->elem();
     if (b->mixed()) {
-        std::vector<float> f(static_cast<size_t>(n));
+        const bool lo = b->refine[table] > 0;
+        std::vector<float> f(static_cast<size_t>(n)), r(lo ? static_cast<size_t>(n) : 0);
         BATCH_CUDA(cudaMemcpy(f.data(), src, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
-        for (int64_t i = 0; i < n; ++i) out[i] = f[i];
+        if (lo)
+            BATCH_CUDA(cudaMemcpy(r.data(), b->ctrl_lo + b->off[table], static_cast<size_t>(n) * 4,
+                                  cudaMemcpyDeviceToHost),
+                       "cudaMemcpy(ctrl)");
+        for (int64_t i = 0; i < n; ++i) out[i] = static_cast<double>(f[i]) + (lo ? static_cast<double>(r[i]) : 0.0);
     } else {
         BATCH_CUDA(cudaMemcpy(out, src, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
     }

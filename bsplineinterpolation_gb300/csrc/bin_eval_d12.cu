@@ -10,14 +10,18 @@ cudaError_t launch_do(const TableDev& t, const BinGeom& g, const CUtensorMap* tm
                       int64_t slice, const uint32_t* rec,
                       int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid, cudaStream_t s) {
     auto k = bin_detail::eval_kernel<D, O>;
-    const size_t smem = static_cast<size_t>(g.tile_elems) * 4 + 128;  // + alignment of the TMA destination
+    // the tile, and the remainders' tile when the table keeps them, + the
+    // alignment of the TMA destination
+    const size_t tile_bytes = (static_cast<size_t>(g.tile_elems) * 4 + 127) & ~size_t(127);
+    const size_t smem = tile_bytes * (t.ctrl_lo ? 2 : 1) + 128;
     // static + dynamic shared memory may pass 48 KB even when the tile alone
     // does not, so the opt-in limit is set on every launch
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     CUtensorMap none{};
     k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32 ? 1 : 0,
-                                                  tmap ? *tmap : none, tmap ? 1 : 0);
+                                                  tmap ? tmap[0] : none, tmap && t.ctrl_lo ? tmap[1] : none,
+                                                  tmap ? 1 : 0);
     note_launch();
     return cudaGetLastError();
 }

@@ -215,6 +215,14 @@ struct TileShape {
     static constexpr int elems() { return D == 1 ? PL() : P(0) * S(0); }
 };
 
+// Offset (floats) of the remainders' tile after the control points' tile,
+// keeping it 128-byte aligned; the launchers size the dynamic shared memory
+// the same way.
+template <class TS>
+constexpr int tile_lo_offset() {
+    return (TS::elems() + 31) & ~31;
+}
+
 // Control-point index along axis a of tile position org + i (periodic wrap,
 // clamp at the end of a non-periodic axis: positions past the last control
 // point are never read by a query of the bucket).
@@ -232,7 +240,7 @@ __device__ __forceinline__ int tile_index(const AxisDev& a, int gi) {
 // identical.
 template <int D, int O, class TS, class Emit>
 __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D], const float (&u)[D], const float* tl,
-                                           const DerivPlan& plan, float cref, const Emit& emit) {
+                                           const DerivPlan& plan, float cref, float cbase, const Emit& emit) {
     constexpr int W = O + 1;
     constexpr int ROWS1 = D >= 2 ? ipow_c(W, D - 2) : 1;
     float w[D][W];
@@ -255,11 +263,11 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
                 off += i * TS::S(d);
             }
             if constexpr (D == 1) {
-                acc = tl[off];
+                acc = tl[off] - cref;
             } else {
                 float s = 0.0f;
 #pragma unroll
-                for (int i = 0; i < W; ++i) s += w[D - 1][i] * tl[off + i];
+                for (int i = 0; i < W; ++i) s += w[D - 1][i] * (tl[off + i] - cref);
                 acc += wr * s;
             }
         }
@@ -274,7 +282,7 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
             axis_weights32<O>(t.ax[0], c[0], u[0], k0, wl);
 #pragma unroll
             for (int i = 0; i < W; ++i) v += wl[i] * Pz[i];
-            if (k0 == 0) v += cref;
+            if (k0 == 0) v = (v + cref) + cbase;
         }
         emit(k, v);
     }
@@ -286,7 +294,7 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
 // LEAN: a DerivPlan::simple plan.
 template <int D, int O, bool LEAN, class TS>
 __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
-                                             const float* tile, const int (&org)[D], float cref,
+                                             const float* tile, const int (&org)[D], float cbase,
                                              const uint32_t* seg, int nblk, int64_t slice,
                                              const uint32_t* __restrict__ rec, int64_t r, int64_t end,
                                              void* __restrict__ out, int out_f32) {
@@ -324,6 +332,11 @@ __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g
             tb += cl[d] * TS::S(d);
         }
         const float* tl = tile + tb;
+        // the query's reference: its central control point
+        int tref = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) tref += ref_tap<O>() * TS::S(d);
+        const float cref = tl[tref];
         const int64_t o0 = idx * K;
         auto emit = [out, out_f32, o0](int k, float v) {
             if (out_f32)
@@ -339,7 +352,7 @@ __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g
                 u[d] = __uint_as_float(cur[d]);
                 c[d] = org[d] + cl[d] + O;
             }
-            lean_point<D, O, TS>(t, c, u, tl, plan, cref, emit);
+            lean_point<D, O, TS>(t, c, u, tl, plan, cref, cbase, emit);
         } else {
             float u[D];
             int64_t c[D];
@@ -351,12 +364,12 @@ __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g
                 axis_weights32<O>(t.ax[d], c[d], u[d], 0, base[d]);
             }
             mixed_point_outputs<D, O>(
-                t, plan, c, u, base, cref,
-                [tl](const int (&ix)[D]) {
+                t, plan, c, u, base, cref, cbase,
+                [tl, cref](const int (&ix)[D]) {
                     int off = 0;
 #pragma unroll
                     for (int d = 0; d < D; ++d) off += ix[d] * TS::S(d);
-                    return tl[off];
+                    return tl[off] - cref;
                 },
                 emit);
         }
@@ -368,11 +381,11 @@ __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g
 // the lean path's allocation.
 template <int D, int O, class TS>
 __device__ __noinline__ void eval_records_general(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
-                                                  const float* tile, const int (&org)[D], float cref,
+                                                  const float* tile, const int (&org)[D], float cbase,
                                                   const uint32_t* seg, int nblk, int64_t slice,
                                                   const uint32_t* __restrict__ rec, int64_t r, int64_t end,
                                                   void* __restrict__ out, int out_f32) {
-    eval_records<D, O, false, TS>(t, g, plan, tile, org, cref, seg, nblk, slice, rec, r, end, out, out_f32);
+    eval_records<D, O, false, TS>(t, g, plan, tile, org, cbase, seg, nblk, slice, rec, r, end, out, out_f32);
 }
 
 template <int D, int O>
@@ -380,13 +393,17 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
                                                            int nblk, int64_t slice, const uint32_t* __restrict__ rec,
                                                            int64_t nrec, DerivPlan plan, void* __restrict__ out,
                                                            int out_f32, const __grid_constant__ CUtensorMap tmap,
+                                                           const __grid_constant__ CUtensorMap tmap_lo,
                                                            int use_tma) {
     using TS = TileShape<D, O>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    // 128-byte aligned tile (the TMA destination)
+    // 128-byte aligned tiles (TMA destinations): the control points, then
+    // their remainders when the table keeps them
     float* tile = reinterpret_cast<float*>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
+    float* tile_lo = tile + tile_lo_offset<TS>();
+    const float* __restrict__ cl = t.ctrl_lo;
     __shared__ __align__(8) uint64_t sh_bar;
-    __shared__ float sh_cref;
+    __shared__ float sh_cbase;
     __shared__ DerivPlan sh_plan;  // indexed by runtime output / group numbers
     __shared__ TableDev sh_t;      // passed by reference to the out-of-line path
     __shared__ int sh_last[TS::P(D - 1)];                          // last-axis control-point indices
@@ -433,12 +450,15 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
         }
         __syncthreads();
         for (int j = threadIdx.x; j < nblk; j += kBinThreads) sh_seg[j] = __ldg(blkoffset + b * nblk + j);
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && cl) {
+            // the operands' base: the control point at the tile's centre
+            // (clamped at the end of a non-periodic axis, as in the direct
+            // kernel)
             int64_t off = 0;
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 off += static_cast<int64_t>(tile_index(t.ax[d], org[d] + TS::P(d) / 2)) * t.ax[d].stride;
-            sh_cref = __ldg(cp + off);
+            sh_cbase = __ldg(cp + off);
         }
         // one TMA box unless the tile wraps around a periodic axis
         bool tma = use_tma != 0;
@@ -447,10 +467,14 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
             if (t.ax[d].periodic && org[d] + TS::P(d) > t.ax[d].n) tma = false;
         if (tma) {
             if (threadIdx.x == 0) {
-                fence_async_smem();  // the tile's earlier generic-proxy accesses before the async write
-                mbar_expect_tx(&sh_bar, static_cast<uint32_t>(TS::elems() * 4));
+                fence_async_smem();  // the tiles' earlier generic-proxy accesses before the async write
+                mbar_expect_tx(&sh_bar, static_cast<uint32_t>(TS::elems() * 4 * (cl ? 2 : 1)));
                 if constexpr (D == 3) tma_load_3d(tile, &tmap, org[2], org[1], org[0], &sh_bar);
                 if constexpr (D == 2) tma_load_2d(tile, &tmap, org[1], org[0], &sh_bar);
+                if (cl) {
+                    if constexpr (D == 3) tma_load_3d(tile_lo, &tmap_lo, org[2], org[1], org[0], &sh_bar);
+                    if constexpr (D == 2) tma_load_2d(tile_lo, &tmap_lo, org[1], org[0], &sh_bar);
+                }
             }
             const bool ok = mbar_wait(&sh_bar, bar_phase);
             if (!__syncthreads_and(ok)) {
@@ -485,22 +509,25 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
                     off += sh_outer[d][i];
                 }
                 cp_async<4>(tile + e, cp + off);
+                if (cl) cp_async<4>(tile_lo + e, cl + off);
             }
             cp_async_wait_all();
         }
         __syncthreads();
-        // The tile is stored relative to a reference control point near its
-        // centre (clamped at the end of a non-periodic axis, as in the direct
-        // kernel): value weights sum to 1 and derivative weights to 0, so the
-        // FP32 rounding of the weights only multiplies the local variation.
-        const float cref = sh_cref;
-        for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) tile[e] -= cref;
-        __syncthreads();
+        // operands, once per tile element: the stored FP32 control point, or
+        // with remainders (ctrl - cbase) + ctrl_lo; each query then reads them
+        // relative to its own central tap
+        float cbase = 0.0f;
+        if (cl) {
+            cbase = sh_cbase;
+            for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) tile[e] = (tile[e] - cbase) + tile_lo[e];
+            __syncthreads();
+        }
         if (sh_plan.simple)
-            eval_records<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cref, sh_seg, nblk, slice, rec, r, end, out,
+            eval_records<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cbase, sh_seg, nblk, slice, rec, r, end, out,
                                          out_f32);
         else
-            eval_records_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cref, sh_seg, nblk, slice, rec, r, end, out,
+            eval_records_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cbase, sh_seg, nblk, slice, rec, r, end, out,
                                            out_f32);
         r = end;
     }

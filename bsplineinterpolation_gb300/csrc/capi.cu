@@ -94,6 +94,9 @@ struct intp_table {
     int device = 0;
     void* arena = nullptr;
     void* ctrl = nullptr;
+    // refined mixed tables: the FP32 remainder of every control point
+    // (control point = ctrl + ctrl_lo as a double-float), else null
+    float* ctrl_lo = nullptr;
     bool has_ctrl = false;
     TableDev dev{};
     BinGeom bins{};
@@ -102,9 +105,10 @@ struct intp_table {
     size_t scratch_bytes = 0;
     double lo_user[kMaxDim]{};  // uniform axes: x_range.first
     size_t arena_bytes = 0;
-    // TMA map of the FP32 control points whose box is one bucket tile of the
-    // binned evaluation (D = 2, 3 with 16-byte aligned row strides)
-    CUtensorMap tile_map{};
+    // TMA maps of the FP32 control points and of their remainders (when the
+    // table keeps them) whose box is one bucket tile of the binned
+    // evaluation (D = 2, 3 with 16-byte aligned row strides)
+    CUtensorMap tile_map[2]{};
     bool has_tile_map = false;
     // Tables of the serving loop take their memory from the stream-ordered
     // pool on alloc_stream (no device-wide synchronisation on free).
@@ -124,9 +128,12 @@ struct intp_table {
     ~intp_table() {
         dfree(arena);
         dfree(ctrl);
+        dfree(ctrl_lo);
         dfree(scratch);
     }
     bool mixed() const { return precision == INTP_PRECISION_MIXED; }
+    // refinement steps of the mixed solve (the automatic choice resolved)
+    int steps() const { return !mixed() ? 0 : refine_steps < 0 ? auto_refine_steps(model) : refine_steps; }
     size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
     int64_t values() const { return model.total * channels; }  // control points over all channels
 };
@@ -164,7 +171,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // per axis, the last padded to a multiple of 4 floats. Positions past the end
 // of a non-periodic axis read zeros (no query reads them). Needs row strides
 // that are multiples of 16 bytes and boxes of at most 256 per axis.
-bool make_tile_map(intp_table* t) {
+bool make_tile_map(intp_table* t, void* base, CUtensorMap* map) {
     const TableModel& m = t->model;
     const BinGeom& g = t->bins;
     const int D = m.dim;
@@ -183,7 +190,7 @@ bool make_tile_map(intp_table* t) {
     if (D == 3) strides[1] = strides[0] * static_cast<cuuint64_t>(m.axis[1].n);
     for (int i = 0; i < D - 1; ++i)
         if (strides[i] % 16 != 0) return false;
-    const CUresult r = enc(&t->tile_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, static_cast<cuuint32_t>(D), t->ctrl, dims,
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, static_cast<cuuint32_t>(D), base, dims,
                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -205,13 +212,20 @@ intp_status upload_table(intp_table* t) {
     bind_table(m, t->lo_user, pt, static_cast<const unsigned char*>(t->arena), t->dev, t->fac);
     INTP_CUDA(t->dmalloc(&t->ctrl, static_cast<size_t>(t->values()) * t->elem()), "cudaMalloc(control points)");
     t->dev.ctrl = t->ctrl;
+    if (t->steps() > 0) {
+        INTP_CUDA(t->dmalloc(reinterpret_cast<void**>(&t->ctrl_lo), static_cast<size_t>(t->values()) * sizeof(float)),
+                  "cudaMalloc(control point remainders)");
+        t->dev.ctrl_lo = t->ctrl_lo;
+    }
     t->dev.channels = t->channels;
     t->dev.chan_stride = m.total;
     // the binned path stages one channel's tiles: vector-valued tables
     // evaluate with the direct kernel
     if (t->mixed() && m.dim <= 3 && t->channels == 1) {
         t->bins = make_bin_geom(t->dev);
-        if (t->bins.smem_buckets > 0) t->has_tile_map = make_tile_map(t);
+        if (t->bins.smem_buckets > 0)
+            t->has_tile_map = make_tile_map(t, t->ctrl, &t->tile_map[0]) &&
+                              (!t->ctrl_lo || make_tile_map(t, t->ctrl_lo, &t->tile_map[1]));
     }
     return INTP_OK;
 }
@@ -289,40 +303,41 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
         return INTP_OK;
     }
     float* c = static_cast<float*>(t->ctrl);
-    INTP_CUDA(launch_shift_copy_f64_f32(values_dev, c, sd, s), "shift copy");
-    INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
-    const int steps = t->refine_steps < 0 ? auto_refine_steps(m) : t->refine_steps;
-    if (steps > 0) {
-        // scratch: shifted values (f64), two f64 ping-pong buffers, f32 correction
-        const size_t need = static_cast<size_t>(N) * (8 * 3 + 4) + 1024;
+    const int steps = t->steps();
+    if (steps == 0) {
+        INTP_CUDA(launch_shift_copy_f64_f32(values_dev, c, nullptr, nullptr, sd, s), "shift copy");
+        INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
+    } else {
+        // Refinement in double-float: F split into (fhi, flo), residual
+        // passes ping-pong between two double-float buffers, the last one
+        // writing r = F - A c in FP32; the correction solve runs in place on
+        // r, and the control points accumulate it as (ctrl, ctrl_lo).
+        const size_t need = static_cast<size_t>(N) * 28 + 1024;
         intp_status st = ensure_scratch(t, need);
         if (st != INTP_OK) return st;
-        unsigned char* b = static_cast<unsigned char*>(t->scratch);
-        double* fsh = reinterpret_cast<double*>(b);
-        double* ta = reinterpret_cast<double*>(b + N * 8);
-        double* tb = reinterpret_cast<double*>(b + N * 16);
-        float* corr = reinterpret_cast<float*>(b + N * 24);
-        INTP_CUDA(launch_shift_copy_f64_f64(values_dev, fsh, sd, s), "shift copy");
+        float* b = static_cast<float*>(t->scratch);
+        float *fhi = b, *flo = b + N, *corr = b + 6 * N;
+        float* ping[2][2] = {{b + 2 * N, b + 3 * N}, {b + 4 * N, b + 5 * N}};
+        INTP_CUDA(launch_shift_copy_f64_f32(values_dev, fhi, flo, c, sd, s), "shift copy");
+        INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
         for (int it = 0; it < steps; ++it) {
-            // r = F - (A_0 x ... x A_{D-1}) c, applied one axis at a time in FP64
-            const double* in64 = nullptr;
-            double* outb = ta;
+            // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass
+            const float *ih = c, *il = it > 0 ? t->ctrl_lo : nullptr;
+            int pp = 0;
             for (int a = m.dim - 1; a >= 0; --a) {
                 const LineGeom g = line_geom(t, a);
                 const AxisFactorDev& f = t->fac[a];
-                const double* rhs = (a == 0) ? fsh : nullptr;
-                cudaError_t e = (a == m.dim - 1)
-                                    ? launch_stencil_f32in(c, outb, rhs, g.n, g.S, g.nlines, f.width,
-                                                           f.scol, f.sval, s)
-                                    : launch_stencil_f64in(in64, outb, rhs, g.n, g.S, g.nlines,
-                                                           f.width, f.scol, f.sval, s);
+                const bool last = a == 0;
+                cudaError_t e = launch_residual_pass(ih, il, last ? nullptr : ping[pp][0], last ? nullptr : ping[pp][1],
+                                                     last ? fhi : nullptr, last ? flo : nullptr, last ? corr : nullptr,
+                                                     g.n, g.S, N, f.width, f.scol, f.sval, s);
                 if (e != cudaSuccess) return cuda_fail(e, "residual");
-                in64 = outb;
-                outb = (outb == ta) ? tb : ta;
+                ih = ping[pp][0];
+                il = ping[pp][1];
+                pp ^= 1;
             }
-            INTP_CUDA(launch_convert_f64_f32(in64, corr, N, s), "residual convert");
             INTP_CUDA(solve_f32_all(t, corr, s), "line solve (correction)");
-            INTP_CUDA(launch_add_f32(c, corr, N, s), "correction");
+            INTP_CUDA(launch_correct(c, t->ctrl_lo, corr, N, it > 0, s), "correction");
         }
     }
     t->has_ctrl = true;
@@ -412,13 +427,19 @@ bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv,
 }
 
 int auto_refine_steps(const TableModel& m) {
-    // The FP32 solve's relative error is about 6e-8 * sum_d kappa_d (kappa ~ 3
-    // per axis for cubic collocation, tens for periodic order >= 6). Each
-    // FP64-residual step squares that relative error, down to FP32 storage.
-    double e = fp32_solve_error_estimate(m);
-    int steps = 0;
-    while (e > 1e-6 && steps < 4) {
-        e = e * e + 6e-8;
+    // The FP32 solve's relative error is about e0 = 6e-8 * sum_d kappa_d
+    // (kappa ~ 3 per axis for cubic collocation, tens for periodic order
+    // >= 6). Each double-float residual step multiplies the error by about
+    // e0, with the control points kept as double-floats (no FP32 storage
+    // floor). One step always: a derivative multiplies the control points'
+    // error by about the axis length per order, so the FP32 solve alone
+    // leaves derivatives above 1e-6. Further steps until about 1e-12, enough
+    // for second derivatives of a 512-point axis.
+    const double e0 = fp32_solve_error_estimate(m);
+    double e = e0 * e0;
+    int steps = 1;
+    while (e > 1e-12 && steps < 4) {
+        e *= e0;
         ++steps;
     }
     return steps;
@@ -477,7 +498,8 @@ intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaS
 }
 
 size_t table_device_bytes(const intp_table* t) {
-    return t->arena_bytes + static_cast<size_t>(t->values()) * t->elem() + t->scratch_bytes;
+    return t->arena_bytes + static_cast<size_t>(t->values()) * (t->elem() + (t->ctrl_lo ? sizeof(float) : 0)) +
+           t->scratch_bytes;
 }
 
 size_t table_build_scratch_bytes(const intp_table_desc* desc) {
@@ -496,6 +518,16 @@ void table_release_scratch(intp_table* t) {
 }
 
 int64_t table_values(const intp_table* t) { return t->values(); }
+
+int stencil_taps(const RowStencil& st) {
+    int taps = 1;
+    for (int64_t i = 0; i < st.n; ++i) {
+        int k = 0;
+        for (int w = 0; w < st.width; ++w) k += st.val[i * st.width + w] != 0.0;
+        taps = std::max(taps, k);
+    }
+    return taps;
+}
 
 void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
     const int O = m.order;
@@ -539,8 +571,26 @@ void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
         o.dinvf = ar.put(to_f32(f.dinv));
         o.bottomf = ar.put(to_f32(f.bottom));
         o.rightf = ar.put(to_f32(f.right));
-        o.scol = ar.put(ax.stencil.col);
-        o.sval = ar.put(ax.stencil.val);
+        // stencil rows with their nonzero taps first (column order kept),
+        // trimmed to the widest row; values as double-floats
+        const RowStencil& st = ax.stencil;
+        const int taps = stencil_taps(st);
+        std::vector<int32_t> col32(static_cast<size_t>(st.n * taps));
+        std::vector<float2> val2(static_cast<size_t>(st.n * taps), make_float2(0.0f, 0.0f));
+        for (int64_t i = 0; i < st.n; ++i) {
+            int k = 0;
+            for (int w = 0; w < st.width; ++w) {
+                const double v = st.val[i * st.width + w];
+                if (v == 0.0) continue;
+                const float h = static_cast<float>(v);
+                col32[i * taps + k] = static_cast<int32_t>(st.col[i * st.width + w]);
+                val2[i * taps + k] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+                ++k;
+            }
+            for (; k < taps; ++k) col32[i * taps + k] = static_cast<int32_t>(i);
+        }
+        o.scol = ar.put(col32);
+        o.sval = ar.put(val2);
     }
 }
 
@@ -603,9 +653,9 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
         fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
         fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
-        fd.scol = reinterpret_cast<const int64_t*>(base + o.scol);
-        fd.sval = reinterpret_cast<const double*>(base + o.sval);
-        fd.width = ax.stencil.width;
+        fd.scol = reinterpret_cast<const int32_t*>(base + o.scol);
+        fd.sval = reinterpret_cast<const float2*>(base + o.sval);
+        fd.width = stencil_taps(ax.stencil);
     }
 }
 
@@ -653,9 +703,15 @@ intp_status intp_table_set_control_points(intp_table* t, const double* ctrl) {
     for (int64_t i = 0; i < P; ++i)
         for (int64_t c = 0; c < C; ++c) v[c * P + i] = ctrl[i * C + c];
     if (t->mixed()) {
-        std::vector<float> f(static_cast<size_t>(N));
-        for (int64_t i = 0; i < N; ++i) f[i] = static_cast<float>(v[i]);
+        // FP32 rounding, and its remainder where the table keeps one
+        std::vector<float> f(static_cast<size_t>(N)), r(t->ctrl_lo ? static_cast<size_t>(N) : 0);
+        for (int64_t i = 0; i < N; ++i) {
+            f[i] = static_cast<float>(v[i]);
+            if (t->ctrl_lo) r[i] = static_cast<float>(v[i] - static_cast<double>(f[i]));
+        }
         INTP_CUDA(cudaMemcpy(t->ctrl, f.data(), N * 4, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
+        if (t->ctrl_lo)
+            INTP_CUDA(cudaMemcpy(t->ctrl_lo, r.data(), N * 4, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
     } else {
         INTP_CUDA(cudaMemcpy(t->ctrl, v.data(), N * 8, cudaMemcpyHostToDevice), "cudaMemcpy(ctrl)");
     }
@@ -670,9 +726,12 @@ intp_status intp_table_get_control_points(const intp_table* t, double* out) {
     INTP_CUDA(cudaDeviceSynchronize(), "synchronize");
     std::vector<double> v(static_cast<size_t>(N));
     if (t->mixed()) {
-        std::vector<float> f(static_cast<size_t>(N));
+        std::vector<float> f(static_cast<size_t>(N)), r(t->ctrl_lo ? static_cast<size_t>(N) : 0);
         INTP_CUDA(cudaMemcpy(f.data(), t->ctrl, N * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
-        for (int64_t i = 0; i < N; ++i) v[i] = f[i];
+        if (t->ctrl_lo)
+            INTP_CUDA(cudaMemcpy(r.data(), t->ctrl_lo, N * 4, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
+        for (int64_t i = 0; i < N; ++i)
+            v[i] = static_cast<double>(f[i]) + (t->ctrl_lo ? static_cast<double>(r[i]) : 0.0);
     } else {
         INTP_CUDA(cudaMemcpy(v.data(), t->ctrl, N * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
     }
@@ -719,7 +778,7 @@ intp_status intp_eval(const intp_table* t, const double* coords, int64_t npts, c
                         (mode == 2 || (mode == 0 && npts >= kBinnedMinPoints));
     if (binned) {
         retain_pool_memory();
-        INTP_CUDA(run_binned_eval(t->dev, t->bins, t->has_tile_map ? &t->tile_map : nullptr, coords, npts, plan, out,
+        INTP_CUDA(run_binned_eval(t->dev, t->bins, t->has_tile_map ? t->tile_map : nullptr, coords, npts, plan, out,
                                   out_dtype == INTP_F32, eval_chunk(), static_cast<cudaStream_t>(stream)),
                   "binned evaluation");
         return INTP_OK;
@@ -1000,7 +1059,7 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
                                  in_rec, rec, &slice, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
-        const CUtensorMap* tm = t->has_tile_map ? &t->tile_map : nullptr;
+        const CUtensorMap* tm = t->has_tile_map ? t->tile_map : nullptr;
         INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
                                                out_f32, sms * 2, s)
                          : launch_bin_eval_d3(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,

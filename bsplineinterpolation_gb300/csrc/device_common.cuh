@@ -44,6 +44,9 @@ struct TableDev {
     int32_t order;
     AxisDev ax[kDevMaxDim];
     const void* ctrl;        // float (mixed) or double (fp64) control points, row-major
+    // mixed form after refinement: the FP32 remainder of every control point
+    // (control point = ctrl + ctrl_lo as a double-float), else NULL
+    const float* ctrl_lo;
     int32_t channels;        // values per mesh point (vector-valued tables; 1 = scalar)
     int64_t chan_stride;     // control points of one channel (channel-major storage)
 };
@@ -81,6 +84,25 @@ struct DerivPlan {
 __host__ __device__ constexpr int bucket_log2(int dim, int axis) {
     return dim == 1 ? 12 : dim == 2 ? 6 : 4;
 }
+
+// Division of 32-bit unsigned integers below 2^31 by a fixed divisor d >= 1
+// as a multiply-high, add and shift (Granlund and Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994, round-up variant):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(m, n)
+// + n) >> l.
+struct FastDiv {
+    uint32_t d, m;
+    int l;
+    __host__ __device__ static FastDiv make(uint32_t d) {
+        FastDiv f{};
+        f.d = d;
+        f.l = 0;
+        while ((uint64_t{1} << f.l) < d) ++f.l;
+        f.m = static_cast<uint32_t>(((uint64_t{1} << 32) * ((uint64_t{1} << f.l) - d)) / d + 1);
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
+};
 
 // Order-preserving integer key of a double: a < b  <=>  key(a) < key(b) for
 // all non-NaN values, with -0 mapped onto +0 (IEEE compares them equal).

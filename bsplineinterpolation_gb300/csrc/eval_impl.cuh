@@ -145,14 +145,23 @@ __device__ __forceinline__ void eval_point(const TableDev& t, const double* __re
         for (int ch = 0; ch < C; ++ch) {
             const R* __restrict__ cpc = cp + ch * t.chan_stride;
             // same per-query code as the binned kernel (identical results)
-            const float cref = __ldg(cpc + bucket_centre_offset<D, O>(t, cell));
+            const float* __restrict__ loc = t.ctrl_lo ? t.ctrl_lo + ch * t.chan_stride : nullptr;
+            const float cbase = loc ? __ldg(cpc + bucket_centre_offset<D, O>(t, cell)) : 0.0f;
+            auto operand = [&](int64_t o) {
+                const float h = __ldg(cpc + o);
+                return loc ? (h - cbase) + __ldg(loc + o) : h;
+            };
+            int64_t oref = 0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) oref += off[d][ref_tap<O>()];
+            const float cref = operand(oref);
             mixed_point_outputs<D, O>(
-                t, plan, cell, xr, base, cref,
+                t, plan, cell, xr, base, cref, cbase,
                 [&](const int (&ix)[D]) {
                     int64_t o = 0;
 #pragma unroll
                     for (int d = 0; d < D; ++d) o += off[d][ix[d]];
-                    return __ldg(cpc + o) - cref;
+                    return operand(o) - cref;
                 },
                 [out, out_f32, o0, C, ch](int k, float v) {
                     const int64_t e = (o0 + k) * C + ch;

@@ -26,8 +26,9 @@ struct ShiftDesc {
 cudaError_t launch_eval_direct(const TableDev& t, bool mixed, const double* coords, int64_t npts,
                                const DerivPlan& plan, void* out, bool out_f32, cudaStream_t s);
 // Binned evaluation of the mixed form (bin_host.cu); `chunk` queries per round.
-// tmap: TMA map of the control points with the tile as its box (NULL: the
-// tiles are staged with element copies).
+// tmap: TMA maps of the control points and of their remainders (the second
+// used when t.ctrl_lo is set) with the tile as their box (NULL: the tiles
+// are staged with element copies).
 cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorMap* tmap, const double* coords,
                             int64_t npts, const DerivPlan& plan, void* out, bool out_f32, int64_t chunk,
                             cudaStream_t s);
@@ -70,18 +71,20 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
                                   cudaStream_t s);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
-cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const ShiftDesc& sd,
+// FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),
+// the high part written to dst2 as well.
+cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_lo, float* dst2, const ShiftDesc& sd,
                                       cudaStream_t s);
-cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs, int64_t n, int64_t S,
-                                 int64_t nlines, int width, const int64_t* col, const double* val,
-                                 cudaStream_t s);
-cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
-                                 int64_t S, int64_t nlines, int width, const int64_t* col,
-                                 const double* val, cudaStream_t s);
+// One double-float residual pass along an axis (n points, stride S) over N
+// values: out = A in, or r = rhs - A in (FP32) when rhs_hi is given. in_lo
+// may be null (plain FP32 input).
+cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
+                                 const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
+                                 int width, const int32_t* col, const float2* val, cudaStream_t s);
+// (c, lo) += corr in double-float (lo read as 0 unless has_lo).
+cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait
 // ran out (0 = none).
 int take_device_error(cudaStream_t s);
-cudaError_t launch_convert_f64_f32(const double* in, float* out, int64_t n, cudaStream_t s);
-cudaError_t launch_add_f32(float* x, const float* d, int64_t n, cudaStream_t s);
 
 }  // namespace intp_gb300

@@ -1,12 +1,24 @@
 // Outputs of one query in the mixed form, shared by the direct and the
 // binned evaluation kernels so both produce identical results.
 //
-// Control points are read relative to a reference value `cref` (the control
-// point at the centre of the query's bucket tile): value weights sum to 1 and
-// derivative weights to 0, so FP32 rounding of the weights multiplies only the
-// local variation of the control points. Outputs sharing their derivative
-// orders on axes 1..D-1 form a group and share the contraction over those
-// axes; each then applies its own axis-0 weights.
+// Operands. A control point enters as v = ctrl where the table keeps FP32
+// control points only, and as v = (ctrl - cbase) + ctrl_lo where the refined
+// solve kept each point's FP32 remainder; cbase is the control point at the
+// centre of the query's bucket tile (the binned kernel forms v once per tile
+// element when it stages the tile). The contraction then reads v relative to
+// the query's own central tap, cref = v at index ref_tap<O>() on every axis:
+// value weights sum to 1 and derivative weights to 0, so the FP32 rounding of
+// the weights and of the partial sums scales with the variation across the
+// query's stencil only. The value adds cref and cbase back.
+//
+// Both matter for derivatives: FP32 storage alone rounds each control point
+// by up to 2^-24 of its magnitude, and a reference shared by a whole tile
+// leaves operands as large as half a tile's variation; a first derivative
+// multiplies either by about 1/dx (above 1e-6 relative on a 256-point axis).
+//
+// Outputs sharing their derivative orders on axes 1..D-1 form a group and
+// share the contraction over those axes; each then applies its own axis-0
+// weights.
 #pragma once
 
 #include "basis32.cuh"
@@ -16,12 +28,19 @@ namespace intp_gb300 {
 
 constexpr int ipow_i(int b, int e) { return e == 0 ? 1 : b * ipow_i(b, e - 1); }
 
-// fetch(idx) returns control point (c_d - O + idx_d)_d minus cref;
-// emit(k, v) stores output k.
+// Stencil position (on every axis) of the reference control point: the tap
+// nearest the query's position within its O + 1 taps.
+template <int O>
+constexpr int ref_tap() {
+    return (O + 1) / 2;
+}
+
+// fetch(idx) returns the operand of control point (c_d - O + idx_d)_d minus
+// cref; emit(k, v) stores output k.
 template <int D, int O, class Fetch, class Emit>
 __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const DerivPlan& plan, const int64_t (&c)[D],
                                                     const float (&u)[D], const float (&base)[D][O + 1], float cref,
-                                                    const Fetch& fetch, const Emit& emit) {
+                                                    float cbase, const Fetch& fetch, const Emit& emit) {
     constexpr int W = O + 1;
     constexpr int ROWS1 = D >= 2 ? ipow_i(W, D - 2) : 1;  // rows over axes 1..D-2
     const int K = plan.k;
@@ -88,7 +107,7 @@ __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const Der
                 bool value_out = k0 == 0;
 #pragma unroll
                 for (int d = 1; d < D; ++d) value_out = value_out && plan.ord[k][d] == 0;
-                if (value_out) v += cref;
+                if (value_out) v = (v + cref) + cbase;
             }
             emit(k, v);
         }
@@ -96,7 +115,7 @@ __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const Der
 }
 
 // Index of the control point at the centre of the bucket tile holding span
-// c (the reference value of the centred contraction), for each axis.
+// c (the operands' base cbase), for each axis.
 template <int D, int O>
 __device__ __forceinline__ int64_t bucket_centre_offset(const TableDev& t, const int64_t (&c)[D]) {
     int64_t off = 0;

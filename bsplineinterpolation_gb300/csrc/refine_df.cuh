@@ -1,0 +1,111 @@
+// Double-float arithmetic of the mixed form's iterative refinement, shared by
+// the single-table build (solve_kernels.cu) and the batched build (batch.cu)
+// so both round identically.
+//
+// A double-float value is an unevaluated sum hi + lo of two FP32 numbers with
+// |lo| <= ulp(hi) / 2: about 48 significant bits from FP32 arithmetic only.
+// GB300's FP32 pipes are many times faster than its FP64 ones, so the
+// refinement residual r = F - A c (the one step that needs more than FP32)
+// runs in double-float instead of FP64, and refined control points are kept
+// as double-floats (ctrl + ctrl_lo): FP32 storage alone rounds every control
+// point by up to 2^-24 of its magnitude, and a first derivative multiplies
+// that by about 1/dx -- above 1e-6 of the derivative on a 256-point axis.
+//
+// The building blocks are the classical error-free transformations (Knuth's
+// TwoSum, Dekker's Fast2Sum, the FMA form of TwoProd), the compensated dot
+// product Dot2 of Ogita, Rump and Oishi, "Accurate sum and dot product",
+// SIAM J. Sci. Comput. 26(6), 2005 (the result is as accurate as if computed
+// in twice the working precision: |error| <= u |x.y| + gamma_n^2 |x|.|y|),
+// and the double-word addition of Joldes, Muller and Popescu, "Tight and
+// rigorous error bounds for basic building blocks of double-word
+// arithmetic", ACM TOMS 44(2), 2017 (DWPlusFP, relative error below 2u^2,
+// u = 2^-24). The residual needs only an absolute error well below the
+// residual itself (about kappa * u * |F|), which Dot2 gives with a quarter
+// of the operations of full double-word products and sums. Every rounding
+// step is written with an explicit _rn intrinsic so that the compiler cannot
+// contract or reassociate them.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace intp_gb300 {
+
+struct DF {
+    float hi, lo;
+};
+
+// s + e = a + b exactly (any a, b).
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return DF{s, e};
+}
+
+// s + e = a + b exactly when |a| >= |b| (or a = 0).
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float e = __fsub_rn(b, __fsub_rn(s, a));
+    return DF{s, e};
+}
+
+// x + y, y a single float (DWPlusFP).
+__device__ __forceinline__ DF df_add_f(DF x, float y) {
+    const DF s = df_two_sum(x.hi, y);
+    const float v = __fadd_rn(x.lo, s.lo);
+    return df_fast_two_sum(s.hi, v);
+}
+
+// Dot2 accumulator: the running sum is s + c (c collects the rounding errors
+// of the products and of the sums of their high parts).
+struct Dot2 {
+    float s, c;
+};
+
+// acc += a * x for a double-float coefficient a = (a.x, a.y) and an operand
+// x = xh + xl (xl = 0 when HAS_LO is false). The products a.y*xh and a.x*xl
+// are below u of the leading product and enter the error term directly
+// (their own rounding is of order u^2).
+template <bool HAS_LO>
+__device__ __forceinline__ void dot2_add(Dot2& acc, float2 a, float xh, float xl) {
+    const float p = __fmul_rn(a.x, xh);
+    float q = __fmaf_rn(a.x, xh, -p);
+    q = __fmaf_rn(a.y, xh, q);
+    if (HAS_LO) q = __fmaf_rn(a.x, xl, q);
+    const DF t = df_two_sum(acc.s, p);
+    acc.s = t.hi;
+    acc.c = __fadd_rn(acc.c, __fadd_rn(t.lo, q));
+}
+
+// One element of a residual pass along one axis: acc += sign * (row i of
+// the axis' collocation matrix) times the line whose element k sits at
+// hi[base + k * S] (+ lo[...] when HAS_LO). The row has `width` taps,
+// columns col and double-float values val (zero-valued padding taps add
+// exact zeros). Taps are summed in column-list order.
+template <bool HAS_LO, class I>
+__device__ __forceinline__ void dot2_row(Dot2& acc, float sign, const float* __restrict__ hi,
+                                         const float* __restrict__ lo, I base, int i, I S, int width,
+                                         const int32_t* __restrict__ col, const float2* __restrict__ val) {
+    for (int w = 0; w < width; ++w) {
+        float2 a = __ldg(val + i * width + w);
+        a.x *= sign;
+        a.y *= sign;
+        const I j = base + static_cast<I>(__ldg(col + i * width + w)) * S;
+        dot2_add<HAS_LO>(acc, a, __ldg(hi + j), HAS_LO ? __ldg(lo + j) : 0.0f);
+    }
+}
+
+// Normalised double-float value of an accumulator.
+__device__ __forceinline__ DF dot2_value(const Dot2& acc) { return df_two_sum(acc.s, acc.c); }
+
+// Refined control point: (c + lo) + corr as a double-float; lo is taken as
+// zero on the first step (has_lo false).
+__device__ __forceinline__ void df_correct(float& c, float& lo, float corr, bool has_lo) {
+    const DF r = df_add_f(DF{c, has_lo ? lo : 0.0f}, corr);
+    c = r.hi;
+    lo = r.lo;
+}
+
+}  // namespace intp_gb300

@@ -1,6 +1,6 @@
 // Control-point solve: per-axis band / cyclic-band substitution over every
 // mesh line (InterpolationTemplate.hpp:448-580, BandLU.hpp:120-143 and
-// :215-259), plus the FP64 residual used by mixed-precision refinement.
+// :215-259), plus the double-float residual of mixed-precision refinement.
 //
 // A mesh of shape N_0 x ... x N_{D-1} is processed one axis at a time. Along
 // axis a the lines are indexed by (outer o, inner t): element k of a line is
@@ -18,11 +18,15 @@
 
 #include "async_copy.cuh"
 #include "launch.hpp"
+#include "refine_df.cuh"
 #include "solve_line.cuh"
 
 namespace intp_gb300 {
 
 namespace {
+
+// 32-bit index math for up to 2^30 values (grid-stride sums stay in range).
+constexpr int64_t kIndex32Max = int64_t{1} << 30;
 
 int grid_for(int64_t n, int block, int max_blocks) {
     int64_t g = (n + block - 1) / block;
@@ -241,81 +245,152 @@ cudaError_t launch_solve_r(R* x, int64_t n, int64_t S, int64_t nlines, int p, in
 // ---- data movement and residual kernels ----
 
 // dst[shift(i)] = (To) src[i]: periodic axes move index i to (i + O/2) mod n
-// (InterpolationTemplate.hpp:451-462).
-template <class Ti, class To>
-__global__ void shift_copy_kernel(const Ti* __restrict__ src, To* __restrict__ dst, ShiftDesc sd) {
-    const int64_t C = sd.channels;
-    for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < sd.total * C;
-         j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        // source element j = point i, channel ch (channel fastest); the
-        // destination holds channel ch's mesh at ch * total
-        const int64_t i = C == 1 ? j : j / C, ch = j - i * C;
-        int64_t r = i, o = ch * sd.total;
+// (InterpolationTemplate.hpp:451-462). With dlo (FP32 destination) the copy
+// is the double-float split of the values, dst = high part (also written to
+// dst2, the solve's working copy) and dlo = the remainder. `identity`: no
+// axis is shifted and there is one channel (destination index = source
+// index). I is the index type (32-bit when the table allows).
+template <class To, class I>
+__global__ void __launch_bounds__(256) shift_copy_kernel(const double* __restrict__ src, To* __restrict__ dst,
+                                                         float* __restrict__ dlo, float* __restrict__ dst2,
+                                                         ShiftDesc sd, int identity) {
+    const I C = static_cast<I>(sd.channels), total = static_cast<I>(sd.total);
+    const I N = total * C;
+    for (I j = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; j < N;
+         j += static_cast<I>(gridDim.x) * blockDim.x) {
+        I o = j;
+        if (!identity) {
+            // source element j = point i, channel ch (channel fastest); the
+            // destination holds channel ch's mesh at ch * total
+            const I i = C == 1 ? j : j / C, ch = j - i * C;
+            I r = i;
+            o = ch * total;
 #pragma unroll
-        for (int d = 3; d >= 0; --d) {
-            if (d < sd.dim) {
-                const int64_t n = sd.n[d];
-                const int64_t q = r / n;
-                int64_t idx = r - q * n;
-                r = q;
-                if (sd.shift[d]) {
-                    idx += sd.shift[d];
-                    if (idx >= n) idx -= n;
+            for (int d = 3; d >= 0; --d) {
+                if (d < sd.dim) {
+                    const I n = static_cast<I>(sd.n[d]);
+                    const I q = r / n;
+                    I idx = r - q * n;
+                    r = q;
+                    if (sd.shift[d]) {
+                        idx += static_cast<I>(sd.shift[d]);
+                        if (idx >= n) idx -= n;
+                    }
+                    o += idx * static_cast<I>(sd.stride[d]);
                 }
-                o += idx * sd.stride[d];
             }
         }
-        dst[o] = static_cast<To>(src[j]);
-    }
-}
-
-// out(line) = A_a in(line) along axis a (FP64 arithmetic), optionally
-// out = rhs - A in for the last pass of a residual.
-template <class Ti>
-__global__ void __launch_bounds__(128) stencil_kernel(const Ti* __restrict__ in, double* __restrict__ out,
-                                                      const double* __restrict__ rhs, int64_t n,
-                                                      int64_t S, int64_t nlines, int width,
-                                                      const int64_t* __restrict__ col,
-                                                      const double* __restrict__ val) {
-    for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
-         l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t o = l / S, t = l - o * S;
-        stencil_line<Ti>(in, out, rhs, o * n * S + t, n, S, width, col, val);
-    }
-}
-
-// Contiguous axis (S = 1): one block per line, threads over its elements
-// (coalesced); each element is the same row product as in stencil_line.
-template <class Ti>
-__global__ void __launch_bounds__(256) stencil_contig_kernel(const Ti* __restrict__ in, double* __restrict__ out,
-                                                             const double* __restrict__ rhs, int64_t n, int64_t nlines,
-                                                             int width, const int64_t* __restrict__ col,
-                                                             const double* __restrict__ val) {
-    for (int64_t l = blockIdx.x; l < nlines; l += gridDim.x) {
-        const int64_t base = l * n;
-        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-            double acc = 0.0;
-            for (int w = 0; w < width; ++w) {
-                const double a = __ldg(val + i * width + w);
-                const int64_t j = __ldg(col + i * width + w);
-                acc = fma(a, static_cast<double>(in[base + j]), acc);
+        const double v = src[j];
+        if constexpr (sizeof(To) == 4) {
+            if (dlo) {
+                // integer split (no FP64 instructions): dst + dlo = v to
+                // about 2^-46 relative
+                float h, l;
+                split_double(v, h, l);
+                dst[o] = h;
+                dst2[o] = h;
+                dlo[o] = l;
+                continue;
             }
-            out[base + i] = rhs ? rhs[base + i] - acc : acc;
+        }
+        dst[o] = static_cast<To>(v);
+    }
+}
+
+bool shift_identity(const ShiftDesc& sd) {
+    if (sd.channels != 1) return false;
+    for (int d = 0; d < sd.dim; ++d)
+        if (sd.shift[d]) return false;
+    return true;
+}
+
+// Position of element e along an axis of n points and stride S: (e / S) % n.
+// (32-bit indices: fast division; 64-bit ones: plain division.)
+struct AxisPos {
+    FastDiv byS, byN;
+    int64_t S64, n64;
+    __device__ __forceinline__ uint32_t operator()(uint32_t e) const {
+        const uint32_t q = byS.div(e);
+        return q - byN.div(q) * byN.d;
+    }
+    __device__ __forceinline__ int64_t operator()(int64_t e) const { return (e / S64) % n64; }
+};
+
+// One residual pass of the mixed form's refinement along an axis of n points
+// and stride S, over all N values (channel blocks included), with Dot2
+// accumulation: out = A_axis in as a double-float, or on the last pass
+// (FINAL) r = rhs - A_axis in rounded to FP32 -- the correction solve's
+// right-hand side. HAS_LO: the input is double-float (else plain FP32). One
+// thread per output element; adjacent threads read adjacent elements of
+// every tap.
+template <class I, bool HAS_LO, bool FINAL>
+__global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restrict__ in_hi,
+                                                            const float* __restrict__ in_lo, float* __restrict__ out_hi,
+                                                            float* __restrict__ out_lo,
+                                                            const float* __restrict__ rhs_hi,
+                                                            const float* __restrict__ rhs_lo, float* __restrict__ r,
+                                                            AxisPos pos, I S, I N, int width,
+                                                            const int32_t* __restrict__ col,
+                                                            const float2* __restrict__ val) {
+    for (I e = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e < N;
+         e += static_cast<I>(gridDim.x) * blockDim.x) {
+        const I i = pos(e);
+        Dot2 acc{0.0f, 0.0f};
+        if (FINAL) acc = Dot2{rhs_hi[e], rhs_lo[e]};
+        dot2_row<HAS_LO, I>(acc, FINAL ? -1.0f : 1.0f, in_hi, in_lo, e - i * S, static_cast<int>(i), S, width, col,
+                            val);
+        if (FINAL) {
+            r[e] = __fadd_rn(acc.s, acc.c);
+        } else {
+            const DF v = dot2_value(acc);
+            out_hi[e] = v.hi;
+            out_lo[e] = v.lo;
         }
     }
 }
 
-template <class Ti, class To>
-__global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        out[i] = static_cast<To>(in[i]);
+template <class I, bool HAS_LO, bool FINAL>
+void launch_residual_t(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
+                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, int width, const int32_t* col,
+                       const float2* val, cudaStream_t s) {
+    AxisPos pos{};
+    if (N <= kIndex32Max) {
+        pos.byS = FastDiv::make(static_cast<uint32_t>(S));
+        pos.byN = FastDiv::make(static_cast<uint32_t>(n));
+    }
+    pos.S64 = S;
+    pos.n64 = n;
+    residual_pass_kernel<I, HAS_LO, FINAL><<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(
+        in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, static_cast<I>(S), static_cast<I>(N), width, col, val);
 }
 
-__global__ void add_kernel(float* __restrict__ x, const float* __restrict__ d, int64_t n) {
+template <class I>
+void launch_residual_i(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
+                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, int width, const int32_t* col,
+                       const float2* val, cudaStream_t s) {
+    const bool lo = in_lo != nullptr, fin = rhs_hi != nullptr;
+    if (lo && fin)
+        launch_residual_t<I, true, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+    else if (lo)
+        launch_residual_t<I, true, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+    else if (fin)
+        launch_residual_t<I, false, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+    else
+        launch_residual_t<I, false, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val,
+                                           s);
+}
+
+// (c, lo) += corr, element-wise in double-float (lo taken as 0 when has_lo
+// is 0: the first refinement step).
+__global__ void __launch_bounds__(256) correct_kernel(float* __restrict__ c, float* __restrict__ lo,
+                                                      const float* __restrict__ corr, int64_t n, int has_lo) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        x[i] += d[i];
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float h = c[i], l = has_lo ? lo[i] : 0.0f;
+        df_correct(h, l, corr[i], has_lo != 0);
+        c[i] = h;
+        lo[i] = l;
+    }
 }
 
 }  // namespace
@@ -347,56 +422,43 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
 
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s) {
-    shift_copy_kernel<double, double><<<grid_for(sd.total * sd.channels, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    const int64_t N = sd.total * sd.channels;
+    const int grid = grid_for(N, 256, 152 * 16);
+    const int id = shift_identity(sd) ? 1 : 0;
+    if (N <= kIndex32Max)
+        shift_copy_kernel<double, uint32_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
+    else
+        shift_copy_kernel<double, int64_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
     note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, const ShiftDesc& sd,
+cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_lo, float* dst2, const ShiftDesc& sd,
                                       cudaStream_t s) {
-    shift_copy_kernel<double, float><<<grid_for(sd.total * sd.channels, 256, 152 * 16), 256, 0, s>>>(src, dst, sd);
+    const int64_t N = sd.total * sd.channels;
+    const int grid = grid_for(N, 256, 152 * 16);
+    const int id = shift_identity(sd) ? 1 : 0;
+    if (N <= kIndex32Max)
+        shift_copy_kernel<float, uint32_t><<<grid, 256, 0, s>>>(src, dst, dst_lo, dst2, sd, id);
+    else
+        shift_copy_kernel<float, int64_t><<<grid, 256, 0, s>>>(src, dst, dst_lo, dst2, sd, id);
     note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_stencil_f32in(const float* in, double* out, const double* rhs, int64_t n, int64_t S,
-                                 int64_t nlines, int width, const int64_t* col, const double* val,
-                                 cudaStream_t s) {
-    if (S == 1) {
-        stencil_contig_kernel<float><<<grid_for(nlines, 1, 152 * 64), 256, 0, s>>>(in, out, rhs, n, nlines, width,
-                                                                                col, val);
-        note_launch();
-        return cudaGetLastError();
-    }
-    stencil_kernel<float><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
-                                                                        width, col, val);
+cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
+                                 const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
+                                 int width, const int32_t* col, const float2* val, cudaStream_t s) {
+    if (N <= kIndex32Max)
+        launch_residual_i<uint32_t>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+    else
+        launch_residual_i<int64_t>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
     note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_stencil_f64in(const double* in, double* out, const double* rhs, int64_t n,
-                                 int64_t S, int64_t nlines, int width, const int64_t* col,
-                                 const double* val, cudaStream_t s) {
-    if (S == 1) {
-        stencil_contig_kernel<double><<<grid_for(nlines, 1, 152 * 64), 256, 0, s>>>(in, out, rhs, n, nlines, width,
-                                                                                 col, val);
-        note_launch();
-        return cudaGetLastError();
-    }
-    stencil_kernel<double><<<grid_for(nlines, 128, 152 * 64), 128, 0, s>>>(in, out, rhs, n, S, nlines,
-                                                                         width, col, val);
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_convert_f64_f32(const double* in, float* out, int64_t n, cudaStream_t s) {
-    convert_kernel<double, float><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(in, out, n);
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_add_f32(float* x, const float* d, int64_t n, cudaStream_t s) {
-    add_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(x, d, n);
+cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s) {
+    correct_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(c, lo, corr, n, has_lo ? 1 : 0);
     note_launch();
     return cudaGetLastError();
 }

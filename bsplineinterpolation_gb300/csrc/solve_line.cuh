@@ -105,24 +105,4 @@ __device__ __forceinline__ void solve_line(const FactorView<R>& f, const Line& l
     }
 }
 
-// One line of out = A in (FP64 arithmetic) along an axis with the collocation
-// rows as a stencil, or out = rhs - A in when rhs is given: the residual step
-// of mixed-precision refinement. `base` is the line's first element, S its
-// stride.
-template <class Ti>
-__device__ __forceinline__ void stencil_line(const Ti* __restrict__ in, double* __restrict__ out,
-                                             const double* __restrict__ rhs, int64_t base, int64_t n,
-                                             int64_t S, int width, const int64_t* __restrict__ col,
-                                             const double* __restrict__ val) {
-    for (int64_t i = 0; i < n; ++i) {
-        double acc = 0.0;
-        for (int w = 0; w < width; ++w) {
-            const double a = __ldg(val + i * width + w);
-            const int64_t j = __ldg(col + i * width + w);
-            acc = fma(a, static_cast<double>(in[base + j * S]), acc);
-        }
-        out[base + i * S] = rhs ? rhs[base + i * S] - acc : acc;
-    }
-}
-
 }  // namespace intp_gb300

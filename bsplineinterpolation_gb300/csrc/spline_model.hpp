@@ -70,7 +70,7 @@ struct LineFactor {
 // Row layout of a factored band matrix (above) for the GPU line solves.
 LineFactor line_factor_from(const BandStore& lu);
 
-// The collocation matrix itself as a row stencil (used for FP64 residuals in
+// The collocation matrix itself as a row stencil (used for the residuals of
 // mixed-precision refinement): row i has nonzeros A(i, col[i*w+k]) =
 // val[i*w+k] for k < w, w = 1+p+q (+p+q in the cyclic case; unused slots
 // have val 0 and col i).

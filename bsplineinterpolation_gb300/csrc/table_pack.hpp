@@ -33,12 +33,13 @@ struct Arena {
 };
 
 // Device pointers of one axis's LU factor (FP64 and FP32 copies) and of its
-// collocation rows as a stencil (FP64 residuals).
+// collocation rows as a stencil (double-float residuals of the mixed form:
+// row i's taps at scol[i * width ..], values as (hi, lo) float pairs).
 struct AxisFactorDev {
     const double *lower, *upper, *dinv, *bottom, *right;
     const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
-    const int64_t* scol;
-    const double* sval;
+    const int32_t* scol;
+    const float2* sval;
     int width;
 };
 
@@ -49,6 +50,10 @@ struct PackedTable {
         size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, scol, sval;
     } ax[kMaxDim];
 };
+
+// Nonzero taps of the widest row of a collocation stencil (the packed
+// stencil's row width).
+int stencil_taps(const RowStencil& st);
 
 // Appends the per-axis arrays of `m` to the arena.
 void pack_table(const TableModel& m, Arena& ar, PackedTable& pt);
@@ -70,8 +75,9 @@ bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv,
 // Sets the message intp_last_error() returns on the calling thread.
 void set_last_error(const std::string& msg);
 
-// Refinement steps that bring a mixed-precision solve of this table to about
-// 1e-6 relative error (0..4), from the per-axis condition estimates.
+// Refinement steps of a mixed-precision solve of this table (1..4): enough
+// to bring the double-float control points to about 1e-12 relative error,
+// from the per-axis condition estimates.
 int auto_refine_steps(const TableModel& m);
 
 }  // namespace intp_gb300

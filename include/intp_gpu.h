@@ -93,6 +93,10 @@ intp_status intp_table_interpolate(intp_table* table, const double* values,
                                    int32_t values_on_device, void* stream);
 
 /* Loads / reads control points (row-major, prod(size) doubles, host memory).
+ * A mixed-precision table that refines its solve keeps every control point
+ * as a double-float (an FP32 value plus its FP32 remainder, about 48
+ * significant bits); a mixed table built without refinement keeps the FP32
+ * value alone.
  * Replaces: BSpline::load_ctrlPts (src/include/BSpline.hpp:230-242) and
  * BSpline::control_points (BSpline.hpp:575-577, plain layout). */
 intp_status intp_table_set_control_points(intp_table* table, const double* ctrl_host);
