@@ -6,6 +6,7 @@ floating-point contraction. Translation units compile in parallel.
 """
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -13,7 +14,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+# objects per host architecture (a tree copied between machines never links
+# another machine's objects)
+BUILD = os.path.join(HERE, "_build", platform.machine() or "host")
 LIB = os.path.join(HERE, "libintp_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -55,13 +58,13 @@ def build(verbose=False, jobs=None):
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if _stale(obj, src):
-            cmds.append([nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            cmds.append(([nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj + ".tmp"], obj))
     for f in cpp:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if _stale(obj, src):
-            cmds.append([os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-c", src, "-o", obj])
+            cmds.append(([os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-c", src, "-o", obj + ".tmp"], obj))
 
     def run(cmd):
         if verbose:
@@ -71,15 +74,23 @@ def build(verbose=False, jobs=None):
             raise RuntimeError("compile failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
         return r.stderr
 
-    # drop objects of sources that no longer exist
+    def compile_one(job):
+        # written under a temporary name: an interrupted compile never leaves
+        # a truncated object that looks up to date
+        cmd, obj = job
+        err = run(cmd)
+        os.replace(obj + ".tmp", obj)
+        return err
+
+    # drop objects of sources that no longer exist, and leftovers
     for f in os.listdir(BUILD):
-        if f.endswith(".o") and f[:-2] not in cu + cpp:
+        if (f.endswith(".o") and f[:-2] not in cu + cpp) or f.endswith(".o.tmp"):
             os.remove(os.path.join(BUILD, f))
     with cf.ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
-        for err in ex.map(run, cmds):
+        for err in ex.map(compile_one, cmds):
             if verbose and err:
                 print(err)
-    if cmds or not os.path.exists(LIB):
+    if cmds or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp%d" % os.getpid()
         run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)

@@ -7,7 +7,7 @@
 // offset off[i]). The control-point solve of all tables runs as one launch
 // per axis pass: pass j solves axis D_i - 1 - j of every table i that has
 // one, as a work list of line groups (one warp per group of up to 32 lines),
-// longest lines first. The arithmetic per line is solve_line, the same as the
+// longest lines first. The arithmetic per line is solve_line_chunked, the same as the
 // single-table solves, so a batched table gets the control points that
 // intp_table_interpolate gives it, bit for bit. Mixed-precision batches
 // refine per table (double-float residual, FP32 correction, double-float
@@ -121,25 +121,28 @@ __device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFact
     return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right};
 }
 
+// Lines are walked in chunks of this many elements (registers per lane).
+constexpr int kBatchChunk = 16;
+
 template <class R, class Line>
 __device__ __forceinline__ void solve_dispatch(int p, bool cyc, const FactorView<R>& fv, const Line& line) {
     if (cyc) {
         switch (p) {
-            case 0: solve_line<R, 0, 0, true>(fv, line); return;
-            case 1: solve_line<R, 1, 1, true>(fv, line); return;
-            case 2: solve_line<R, 2, 2, true>(fv, line); return;
-            case 3: solve_line<R, 3, 3, true>(fv, line); return;
+            case 0: solve_line_chunked<R, 0, 0, true, kBatchChunk>(fv, line); return;
+            case 1: solve_line_chunked<R, 1, 1, true, kBatchChunk>(fv, line); return;
+            case 2: solve_line_chunked<R, 2, 2, true, kBatchChunk>(fv, line); return;
+            case 3: solve_line_chunked<R, 3, 3, true, kBatchChunk>(fv, line); return;
         }
         return;
     }
     switch (p) {
-        case 0: solve_line<R, 0, 0, false>(fv, line); return;
-        case 1: solve_line<R, 1, 1, false>(fv, line); return;
-        case 2: solve_line<R, 2, 2, false>(fv, line); return;
-        case 3: solve_line<R, 3, 3, false>(fv, line); return;
-        case 4: solve_line<R, 4, 4, false>(fv, line); return;
-        case 5: solve_line<R, 5, 5, false>(fv, line); return;
-        case 6: solve_line<R, 6, 6, false>(fv, line); return;
+        case 0: solve_line_chunked<R, 0, 0, false, kBatchChunk>(fv, line); return;
+        case 1: solve_line_chunked<R, 1, 1, false, kBatchChunk>(fv, line); return;
+        case 2: solve_line_chunked<R, 2, 2, false, kBatchChunk>(fv, line); return;
+        case 3: solve_line_chunked<R, 3, 3, false, kBatchChunk>(fv, line); return;
+        case 4: solve_line_chunked<R, 4, 4, false, kBatchChunk>(fv, line); return;
+        case 5: solve_line_chunked<R, 5, 5, false, kBatchChunk>(fv, line); return;
+        case 6: solve_line_chunked<R, 6, 6, false, kBatchChunk>(fv, line); return;
     }
 }
 
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) tile[r * pitch + k] = src[static_cast<int64_t>(r) * ni + k];
         __syncwarp();
-        if (lane < it.rows) solve_dispatch<R>(band.x, band.y != 0, fv, SmemLine<R>{tile + lane * pitch});
+        if (lane < it.rows) solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
         __syncwarp();
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) src[static_cast<int64_t>(r) * ni + k] = tile[r * pitch + k];
@@ -180,14 +183,14 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
     if (lane < it.rows) {
         const int64_t l = it.line0 + lane;
         const int64_t o = l / S, tt = l - o * S;
-        solve_dispatch<R>(band.x, band.y != 0, fv, StridedLine<R>{base + o * n * S + tt, S});
+        solve_dispatch<R>(band.x, band.y != 0, fv, StridedChunks<R>{base + o * n * S + tt, S});
     }
 }
 
 // Residual pass of the refinement with Dot2 accumulation: mid = A_axis in
 // as a double-float, or corr = F - A_axis in (FP32) on the table's last pass
 // (axis 0), for every line of the item. Each output element is an
-// independent sparse row product (dot2_row, the arithmetic of the
+// independent band-row product (dot2_band_row, the operations of the
 // single-table residual), so the lanes spread over the elements of each line
 // of the contiguous axis (coalesced) and over adjacent lines of a strided
 // axis. HAS_LO: the input is double-float (else plain FP32).
@@ -216,7 +219,8 @@ __global__ void __launch_bounds__(32) batch_stencil_kernel(const float* __restri
         const int e = base + i * S;
         Dot2 acc{0.0f, 0.0f};
         if (it.last) acc = Dot2{fhi[o0 + e], flo[o0 + e]};
-        dot2_row<HAS_LO, int>(acc, it.last ? -1.0f : 1.0f, ih, il, base, i, S, f.width, f.scol, f.sval);
+        dot2_band_row<HAS_LO, int>(acc, it.last ? -1.0f : 1.0f, ih, il, base, i, n, S, f.band, ax.periodic != 0,
+                                   f.sval);
         if (it.last) {
             corr[o0 + e] = __fadd_rn(acc.s, acc.c);
         } else {

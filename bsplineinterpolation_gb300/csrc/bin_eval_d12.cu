@@ -13,14 +13,15 @@ cudaError_t launch_do(const TableDev& t, const BinGeom& g, const CUtensorMap* tm
     // the tile, and the remainders' tile when the table keeps them, + the
     // alignment of the TMA destination
     const size_t tile_bytes = (static_cast<size_t>(g.tile_elems) * 4 + 127) & ~size_t(127);
-    const size_t smem = tile_bytes * (t.ctrl_lo ? 2 : 1) + 128;
+    const bool lo = t.ctrl_lo && plan.has_deriv;
+    const size_t smem = tile_bytes * (lo ? 2 : 1) + 128;
     // static + dynamic shared memory may pass 48 KB even when the tile alone
     // does not, so the opt-in limit is set on every launch
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     CUtensorMap none{};
     k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32 ? 1 : 0,
-                                                  tmap ? tmap[0] : none, tmap && t.ctrl_lo ? tmap[1] : none,
+                                                  tmap ? tmap[0] : none, tmap && lo ? tmap[1] : none,
                                                   tmap ? 1 : 0);
     note_launch();
     return cudaGetLastError();

@@ -401,7 +401,8 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
     // their remainders when the table keeps them
     float* tile = reinterpret_cast<float*>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
     float* tile_lo = tile + tile_lo_offset<TS>();
-    const float* __restrict__ cl = t.ctrl_lo;
+    // remainders staged for derivative requests only (as in the direct kernel)
+    const float* __restrict__ cl = plan.has_deriv ? t.ctrl_lo : nullptr;
     __shared__ __align__(8) uint64_t sh_bar;
     __shared__ float sh_cbase;
     __shared__ DerivPlan sh_plan;  // indexed by runtime output / group numbers

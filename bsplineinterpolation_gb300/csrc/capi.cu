@@ -272,8 +272,8 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
         const LineGeom g = line_geom(t, a);
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
-        cudaError_t e = launch_line_solve_f32(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf,
-                                              f.upperf, f.dinvf, f.bottomf, f.rightf, s);
+        cudaError_t e = launch_line_solve_f32(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
+                                              f.dinvf, f.bottomf, f.rightf, s);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -284,8 +284,8 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
         const LineGeom g = line_geom(t, a);
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
-        cudaError_t e = launch_line_solve_f64(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lower,
-                                              f.upper, f.dinv, f.bottom, f.right, s);
+        cudaError_t e = launch_line_solve_f64(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lower, f.upper,
+                                              f.dinv, f.bottom, f.right, s);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -330,7 +330,7 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
                 const bool last = a == 0;
                 cudaError_t e = launch_residual_pass(ih, il, last ? nullptr : ping[pp][0], last ? nullptr : ping[pp][1],
                                                      last ? fhi : nullptr, last ? flo : nullptr, last ? corr : nullptr,
-                                                     g.n, g.S, N, f.width, f.scol, f.sval, s);
+                                                     g.n, g.S, N, f.band, m.axis[a].periodic, f.sval, s);
                 if (e != cudaSuccess) return cuda_fail(e, "residual");
                 ih = ping[pp][0];
                 il = ping[pp][1];
@@ -397,6 +397,10 @@ void group_plan(DerivPlan& plan, int dim) {
     plan.simple = plan.ngroups == 1 ? 1 : 0;
     for (int d = 1; d < dim && plan.simple; ++d)
         if (plan.ord[plan.group_rep[0]][d] != 0) plan.simple = 0;
+    plan.has_deriv = 0;
+    for (int k = 0; k < plan.k; ++k)
+        for (int d = 0; d < dim; ++d)
+            if (plan.ord[k][d] != 0) plan.has_deriv = 1;
 }
 
 bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv, int row_stride, DerivPlan& plan,
@@ -519,16 +523,6 @@ void table_release_scratch(intp_table* t) {
 
 int64_t table_values(const intp_table* t) { return t->values(); }
 
-int stencil_taps(const RowStencil& st) {
-    int taps = 1;
-    for (int64_t i = 0; i < st.n; ++i) {
-        int k = 0;
-        for (int w = 0; w < st.width; ++w) k += st.val[i * st.width + w] != 0.0;
-        taps = std::max(taps, k);
-    }
-    return taps;
-}
-
 void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
     const int O = m.order;
     for (int d = 0; d < m.dim; ++d) {
@@ -571,25 +565,15 @@ void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
         o.dinvf = ar.put(to_f32(f.dinv));
         o.bottomf = ar.put(to_f32(f.bottom));
         o.rightf = ar.put(to_f32(f.right));
-        // stencil rows with their nonzero taps first (column order kept),
-        // trimmed to the widest row; values as double-floats
+        // collocation rows as a band stencil of double-float values (row i,
+        // tap d: column i - band + d, cyclic on a periodic axis)
         const RowStencil& st = ax.stencil;
-        const int taps = stencil_taps(st);
-        std::vector<int32_t> col32(static_cast<size_t>(st.n * taps));
-        std::vector<float2> val2(static_cast<size_t>(st.n * taps), make_float2(0.0f, 0.0f));
-        for (int64_t i = 0; i < st.n; ++i) {
-            int k = 0;
-            for (int w = 0; w < st.width; ++w) {
-                const double v = st.val[i * st.width + w];
-                if (v == 0.0) continue;
-                const float h = static_cast<float>(v);
-                col32[i * taps + k] = static_cast<int32_t>(st.col[i * st.width + w]);
-                val2[i * taps + k] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
-                ++k;
-            }
-            for (; k < taps; ++k) col32[i * taps + k] = static_cast<int32_t>(i);
+        std::vector<float2> val2(st.val.size());
+        for (size_t k = 0; k < val2.size(); ++k) {
+            const double v = st.val[k];
+            const float h = static_cast<float>(v);
+            val2[k] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
         }
-        o.scol = ar.put(col32);
         o.sval = ar.put(val2);
     }
 }
@@ -653,9 +637,8 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
         fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
         fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
-        fd.scol = reinterpret_cast<const int32_t*>(base + o.scol);
         fd.sval = reinterpret_cast<const float2*>(base + o.sval);
-        fd.width = stencil_taps(ax.stencil);
+        fd.band = (ax.stencil.width - 1) / 2;
     }
 }
 

@@ -77,6 +77,7 @@ struct DerivPlan {
     int8_t group_rep[kMaxDeriv];    // an output of each group
     int8_t out_group[kMaxDeriv];    // group of each output
     int32_t simple;                 // one group, all orders on axes 1..D-1 zero
+    int32_t has_deriv;              // some output has a derivative order above 0
 };
 
 // Spans per bucket (log2, per axis) of the binned evaluation, fixed per

@@ -102,6 +102,45 @@ __device__ __forceinline__ int64_t wrap_index(int64_t v, int64_t n, bool periodi
 
 constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
 
+// Mixed-form outputs of one channel of one query (the per-query code of the
+// binned kernel, so results are identical): operands relative to the query's
+// central control point, with (LO) the control points' FP32 remainders
+// added to their offsets from the bucket base cbase.
+template <int D, int O, bool LO>
+__device__ __forceinline__ void mixed_channel(const TableDev& t, const DerivPlan& plan, const int64_t (&cell)[D],
+                                              const float (&xr)[D], const float (&base)[D][O + 1],
+                                              const int64_t (&off)[D][O + 1], const float* __restrict__ cpc,
+                                              const float* __restrict__ loc, void* __restrict__ out, int out_f32,
+                                              int64_t o0, int C, int ch) {
+    const float cbase = LO ? __ldg(cpc + bucket_centre_offset<D, O>(t, cell)) : 0.0f;
+    auto operand = [&](int64_t o) {
+        const float h = __ldg(cpc + o);
+        if constexpr (LO)
+            return (h - cbase) + __ldg(loc + o);
+        else
+            return h;
+    };
+    int64_t oref = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) oref += off[d][ref_tap<O>()];
+    const float cref = operand(oref);
+    mixed_point_outputs<D, O>(
+        t, plan, cell, xr, base, cref, cbase,
+        [&](const int (&ix)[D]) {
+            int64_t o = 0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) o += off[d][ix[d]];
+            return operand(o) - cref;
+        },
+        [out, out_f32, o0, C, ch](int k, float v) {
+            const int64_t e = (o0 + k) * C + ch;
+            if (out_f32)
+                static_cast<float*>(out)[e] = v;
+            else
+                static_cast<double*>(out)[e] = static_cast<double>(v);
+        });
+}
+
 // All outputs of one query point: xp holds its D coordinates, output k goes
 // to out[o0 + k]. Shared by the direct kernel and the batched-table kernel.
 template <int D, int O, bool MIXED>
@@ -144,32 +183,17 @@ __device__ __forceinline__ void eval_point(const TableDev& t, const double* __re
     if constexpr (MIXED) {
         for (int ch = 0; ch < C; ++ch) {
             const R* __restrict__ cpc = cp + ch * t.chan_stride;
-            // same per-query code as the binned kernel (identical results)
-            const float* __restrict__ loc = t.ctrl_lo ? t.ctrl_lo + ch * t.chan_stride : nullptr;
-            const float cbase = loc ? __ldg(cpc + bucket_centre_offset<D, O>(t, cell)) : 0.0f;
-            auto operand = [&](int64_t o) {
-                const float h = __ldg(cpc + o);
-                return loc ? (h - cbase) + __ldg(loc + o) : h;
-            };
-            int64_t oref = 0;
-#pragma unroll
-            for (int d = 0; d < D; ++d) oref += off[d][ref_tap<O>()];
-            const float cref = operand(oref);
-            mixed_point_outputs<D, O>(
-                t, plan, cell, xr, base, cref, cbase,
-                [&](const int (&ix)[D]) {
-                    int64_t o = 0;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) o += off[d][ix[d]];
-                    return operand(o) - cref;
-                },
-                [out, out_f32, o0, C, ch](int k, float v) {
-                    const int64_t e = (o0 + k) * C + ch;
-                    if (out_f32)
-                        static_cast<float*>(out)[e] = v;
-                    else
-                        static_cast<double*>(out)[e] = static_cast<double>(v);
-                });
+            // the remainders matter for derivatives only (a value is within
+            // FP32 rounding of the stored control points either way); 4D
+            // tables contract the stored FP32 control points
+            if constexpr (D <= 3) {
+                if (t.ctrl_lo && plan.has_deriv) {
+                    mixed_channel<D, O, true>(t, plan, cell, xr, base, off, cpc, t.ctrl_lo + ch * t.chan_stride, out,
+                                              out_f32, o0, C, ch);
+                    continue;
+                }
+            }
+            mixed_channel<D, O, false>(t, plan, cell, xr, base, off, cpc, nullptr, out, out_f32, o0, C, ch);
         }
     } else {
         for (int k = 0; k < K; ++k) {

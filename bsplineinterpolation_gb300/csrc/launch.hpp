@@ -61,14 +61,14 @@ cudaError_t launch_range_check(const TableDev& t, const double* coords, int64_t 
                                unsigned long long* first_bad, cudaStream_t s);
 
 // solve (solve_kernels.cu)
-cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                  bool cyclic, const double* lower, const double* upper,
-                                  const double* dinv, const double* bottom, const double* right,
-                                  cudaStream_t s);
-cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                  bool cyclic, const float* lower, const float* upper,
-                                  const float* dinv, const float* bottom, const float* right,
-                                  cudaStream_t s);
+// Band / cyclic-band solves of every line along one axis with the factor's
+// lower / upper bands, inverse diagonal and cyclic corner blocks.
+cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                  const double* lower, const double* upper, const double* dinv, const double* bottom,
+                                  const double* right, cudaStream_t s);
+cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                  const float* lower, const float* upper, const float* dinv, const float* bottom,
+                                  const float* right, cudaStream_t s);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
 // FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),
@@ -76,11 +76,12 @@ cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const Shif
 cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_lo, float* dst2, const ShiftDesc& sd,
                                       cudaStream_t s);
 // One double-float residual pass along an axis (n points, stride S) over N
-// values: out = A in, or r = rhs - A in (FP32) when rhs_hi is given. in_lo
-// may be null (plain FP32 input).
+// values with the axis' band stencil (band half-width `band`, values val):
+// out = A in, or r = rhs - A in (FP32) when rhs_hi is given. in_lo may be
+// null (plain FP32 input).
 cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
                                  const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
-                                 int width, const int32_t* col, const float2* val, cudaStream_t s);
+                                 int band, bool periodic, const float2* val, cudaStream_t s);
 // (c, lo) += corr in double-float (lo read as 0 unless has_lo).
 cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait

@@ -79,20 +79,46 @@ __device__ __forceinline__ void dot2_add(Dot2& acc, float2 a, float xh, float xl
     acc.c = __fadd_rn(acc.c, __fadd_rn(t.lo, q));
 }
 
-// One element of a residual pass along one axis: acc += sign * (row i of
-// the axis' collocation matrix) times the line whose element k sits at
-// hi[base + k * S] (+ lo[...] when HAS_LO). The row has `width` taps,
-// columns col and double-float values val (zero-valued padding taps add
-// exact zeros). Taps are summed in column-list order.
+// One element of a residual pass along one axis, element-parallel form:
+// acc += sign * (row i of the axis' collocation matrix) times the line whose
+// element k sits at hi[base + k * S] (+ lo[...] when HAS_LO). The row is a
+// band of 2*band+1 double-float values (tap d: column i - band + d, cyclic
+// on a periodic axis); zero taps are skipped, the others summed in tap
+// order.
 template <bool HAS_LO, class I>
-__device__ __forceinline__ void dot2_row(Dot2& acc, float sign, const float* __restrict__ hi,
-                                         const float* __restrict__ lo, I base, int i, I S, int width,
-                                         const int32_t* __restrict__ col, const float2* __restrict__ val) {
-    for (int w = 0; w < width; ++w) {
-        float2 a = __ldg(val + i * width + w);
+__device__ __forceinline__ void dot2_band_row(Dot2& acc, float sign, const float* __restrict__ hi,
+                                              const float* __restrict__ lo, I base, int i, int n, I S, int band,
+                                              bool periodic, const float2* __restrict__ val) {
+    const int W = 2 * band + 1;
+    for (int d = 0; d < W; ++d) {
+        float2 a = __ldg(val + i * W + d);
+        if (a.x == 0.0f && a.y == 0.0f) continue;
         a.x *= sign;
         a.y *= sign;
-        const I j = base + static_cast<I>(__ldg(col + i * width + w)) * S;
+        int c = i - band + d;
+        if (periodic) c = c < 0 ? c + n : (c >= n ? c - n : c);
+        const I j = base + static_cast<I>(c) * S;
+        dot2_add<HAS_LO>(acc, a, __ldg(hi + j), HAS_LO ? __ldg(lo + j) : 0.0f);
+    }
+}
+
+// dot2_band_row with the band and the periodicity known at compile time
+// (taps unrolled; the same operations in the same order).
+template <int BAND, bool PERIODIC, bool HAS_LO, class I>
+__device__ __forceinline__ void dot2_band_row_t(Dot2& acc, float sign, const float* __restrict__ hi,
+                                                const float* __restrict__ lo, I base, int i, int n, I S,
+                                                const float2* __restrict__ val) {
+    constexpr int W = 2 * BAND + 1;
+    const float2* __restrict__ row = val + i * W;
+#pragma unroll
+    for (int d = 0; d < W; ++d) {
+        float2 a = __ldg(row + d);
+        if (a.x == 0.0f && a.y == 0.0f) continue;
+        a.x *= sign;
+        a.y *= sign;
+        int c = i - BAND + d;
+        if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
+        const I j = base + static_cast<I>(c) * S;
         dot2_add<HAS_LO>(acc, a, __ldg(hi + j), HAS_LO ? __ldg(lo + j) : 0.0f);
     }
 }

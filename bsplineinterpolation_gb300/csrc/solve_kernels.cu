@@ -4,13 +4,16 @@
 //
 // A mesh of shape N_0 x ... x N_{D-1} is processed one axis at a time. Along
 // axis a the lines are indexed by (outer o, inner t): element k of a line is
-// at o*N_a*S + k*S + t with S = prod_{d>a} N_d. One thread owns one line;
-// adjacent threads own adjacent t, so for S >= 32 every step of the
-// substitution is a coalesced warp-wide access. The contiguous axis (S = 1)
-// is staged through shared memory so it is read and written coalesced too.
-// The reference instead rotates the whole tensor after each axis pass
+// at o*N_a*S + k*S + t with S = prod_{d>a} N_d. One thread owns one line and
+// walks it in register chunks of 32 elements (forward sweep, then back
+// sweep, each chunk written back in place); adjacent threads own adjacent
+// t, so for S >= 32 every chunk access is coalesced. The contiguous axis
+// (S = 1) moves each chunk through a small per-warp shared-memory transpose
+// so it is read and written coalesced too. Nothing holds a whole line, so
+// occupancy is set by registers and long lines need no special path. The
+// reference instead rotates the whole tensor after each axis pass
 // (:537-543); solving in place along strided lines needs no rotation. The
-// substitution itself is solve_line (solve_line.cuh).
+// substitution itself is solve_line_chunked (solve_line.cuh).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,184 +38,59 @@ int grid_for(int64_t n, int block, int max_blocks) {
     return static_cast<int>(g);
 }
 
+// Lines are walked in chunks of elements held in registers: 32 for the
+// contiguous axis (one shared-memory transpose per chunk), fewer on strided
+// axes, where every element of a chunk is a separate global load in flight
+// (register budget).
+constexpr int kChunk = 32;
+template <class R>
+constexpr int strided_chunk() {
+    return sizeof(R) == 4 ? 16 : 8;
+}
+constexpr int kSolveWarps = 4;  // warps per block
+
+// Strided axis (S > 1): one thread per line; adjacent threads own adjacent
+// lines (adjacent t), so every chunk load and store of a warp is a run of
+// contiguous elements. No shared memory: occupancy is set by registers only.
 template <class R, int P, int Q, bool CYC>
-__global__ void __launch_bounds__(128) solve_strided_kernel(R* __restrict__ x, int64_t n, int64_t S,
-                                                            int64_t nlines, FactorView<R> f) {
+__global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R* __restrict__ x, int64_t n,
+                                                                              int64_t S, int64_t nlines,
+                                                                              FactorView<R> f) {
     for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
          l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t o = l / S, t = l - o * S;
-        StridedLine<R> line{x + o * n * S + t, S};
-        solve_line<R, P, Q, CYC>(f, line);
+        solve_line_chunked<R, P, Q, CYC, strided_chunk<R>()>(f, StridedChunks<R>{x + o * n * S + t, S});
     }
 }
 
-// Contiguous lines (S = 1): a block stages 32 lines x n into shared memory
-// (row pitch n+1, conflict-free per-lane access), solves, writes back.
+// Contiguous axis (S = 1): one warp per 32 consecutive lines.
 template <class R, int P, int Q, bool CYC>
-__global__ void __launch_bounds__(32) solve_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
-                                                          FactorView<R> f) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    R* tile = reinterpret_cast<R*>(smem_raw);
-    const int64_t pitch = n + 1;
-    const int lane = threadIdx.x;
-    for (int64_t l0 = blockIdx.x * 32LL; l0 < nlines; l0 += gridDim.x * 32LL) {
+__global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_kernel(R* __restrict__ x, int64_t n,
+                                                                             int64_t nlines, FactorView<R> f) {
+    __shared__ R stage[kSolveWarps][32 * 33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t ngroups = (nlines + 31) / 32;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(kSolveWarps) + warp; g < ngroups;
+         g += static_cast<int64_t>(gridDim.x) * kSolveWarps) {
+        const int64_t l0 = g * 32;
         const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
-        const R* src = x + l0 * n;
-        for (int r = 0; r < rows; ++r)
-            for (int64_t k = lane; k < n; k += 32) tile[r * pitch + k] = src[r * n + k];
-        __syncwarp();
-        if (lane < rows) solve_line<R, P, Q, CYC>(f, SmemLine<R>{tile + lane * pitch});
-        __syncwarp();
-        R* dst = x + l0 * n;
-        for (int r = 0; r < rows; ++r)
-            for (int64_t k = lane; k < n; k += 32) dst[r * n + k] = tile[r * pitch + k];
-        __syncwarp();
+        WarpContigChunks<R> io{x + l0 * n, n, rows, stage[warp], lane};
+        solve_line_chunked<R, P, Q, CYC, strided_chunk<R>()>(f, io);
     }
 }
-
-template <class R, int P, int Q, bool CYC>
-cudaError_t launch_solve_pq_fallback(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
-                                     cudaStream_t s);
-
-// ---- tiled solves: one warp stages 32 lines in shared memory ----
-
-// Column of a [n][32] tile: element k of lane l at base[k*32 + l].
-template <class R>
-struct TileColumn {
-    R* base;
-    __device__ __forceinline__ R load(int64_t k) const { return base[k * 32]; }
-    __device__ __forceinline__ void store(int64_t k, R v) const { base[k * 32] = v; }
-};
-
-// Strided axis (S % (16/sizeof(R)) == 0): the tile holds 32 adjacent lines
-// (t0 .. t0+31 for one outer index o); row k of the tile is the 32 contiguous
-// elements k*S + t0 .. + 31, moved by one TMA bulk copy each way.
-template <class R, int P, int Q, bool CYC>
-__global__ void __launch_bounds__(32) solve_tile_strided_kernel(R* __restrict__ x, int64_t n, int64_t S,
-                                                                int64_t tiles_per_o, int64_t ntiles,
-                                                                FactorView<R> f) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar;
-    R* tile = reinterpret_cast<R*>(smem_raw);
-    const int lane = threadIdx.x;
-    if (lane == 0) mbar_init(&bar, 1);
-    __syncwarp();
-    uint32_t phase = 0;
-    for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
-        const int64_t o = tl / tiles_per_o, t0 = (tl - o * tiles_per_o) * 32;
-        const int w = static_cast<int>(S - t0 < 32 ? S - t0 : 32);
-        const uint32_t row_bytes = static_cast<uint32_t>(w * sizeof(R));
-        R* base = x + o * n * S + t0;
-        if (lane == 0) mbar_expect_tx(&bar, row_bytes * static_cast<uint32_t>(n));
-        __syncwarp();
-        for (int64_t k = lane; k < n; k += 32) bulk_load(tile + k * 32, base + k * S, row_bytes, &bar);
-        if (!mbar_wait(&bar, phase)) {
-            mbar_wait(&bar, phase);  // give the copies in flight a second bounded wait
-            return;
-        }
-        phase ^= 1u;
-        if (lane < w) solve_line<R, P, Q, CYC>(f, TileColumn<R>{tile + lane});
-        __syncwarp();
-        fence_async_smem();
-        __syncwarp();
-        for (int64_t k = lane; k < n; k += 32) bulk_store(base + k * S, tile + k * 32, row_bytes);
-        bulk_store_commit();
-        bulk_store_wait_read();
-        __syncwarp();
-    }
-    bulk_store_wait_all();
-}
-
-// Contiguous axis (S = 1): 32 lines of n elements copied element-wise with
-// cp.async into rows of pitch n+1, so lane l reading element k of line l
-// touches bank (l + k) mod 32: no conflicts.
-template <class R, int P, int Q, bool CYC>
-__global__ void __launch_bounds__(32) solve_tile_contig_kernel(R* __restrict__ x, int64_t n, int64_t nlines,
-                                                               FactorView<R> f) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    R* tile = reinterpret_cast<R*>(smem_raw);
-    const int64_t pitch = n + 1;
-    const int lane = threadIdx.x;
-    for (int64_t l0 = blockIdx.x * 32LL; l0 < nlines; l0 += gridDim.x * 32LL) {
-        const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
-        const R* src = x + l0 * n;
-        for (int r = 0; r < rows; ++r)
-            for (int64_t k = lane; k < n; k += 32) cp_async<sizeof(R)>(tile + r * pitch + k, src + r * n + k);
-        cp_async_wait_all();
-        __syncwarp();
-        if (lane < rows) solve_line<R, P, Q, CYC>(f, SmemLine<R>{tile + lane * pitch});
-        __syncwarp();
-        R* dst = x + l0 * n;
-        for (int r = 0; r < rows; ++r)
-            for (int64_t k = lane; k < n; k += 32) dst[r * n + k] = tile[r * pitch + k];
-        __syncwarp();
-    }
-}
-
-int sm_count_solve() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
-    }
-    return n;
-}
-
-constexpr size_t kTileSmemLimit = 200 * 1024;
 
 template <class R, int P, int Q, bool CYC>
 cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
                             cudaStream_t s) {
-    const size_t tile_bytes = static_cast<size_t>(n) * 32 * sizeof(R);
-    const bool aligned = (S * static_cast<int64_t>(sizeof(R))) % 16 == 0 &&
-                         (reinterpret_cast<uintptr_t>(x) % 16) == 0;
-    if (S >= 32 && aligned && tile_bytes <= kTileSmemLimit) {
-        auto k = solve_tile_strided_kernel<R, P, Q, CYC>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(tile_bytes));
-        if (e != cudaSuccess) return e;
-        const int64_t tiles_per_o = (S + 31) / 32;
-        const int64_t ntiles = (nlines / S) * tiles_per_o;
-        const int per_sm = static_cast<int>(std::max<size_t>(1, 220 * 1024 / (tile_bytes + 1024)));
-        const int grid = static_cast<int>(std::min<int64_t>(ntiles, int64_t{sm_count_solve()} * per_sm));
-        k<<<grid, 32, tile_bytes, s>>>(x, n, S, tiles_per_o, ntiles, f);
-        note_launch();
-        return cudaGetLastError();
+    constexpr int kThreads = kSolveWarps * 32;
+    if (S == 1) {
+        const int64_t groups = (nlines + 31) / 32;
+        const int grid = grid_for(groups, kSolveWarps, 152 * 64);
+        solve_warp_contig_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, nlines, f);
+    } else {
+        const int grid = grid_for(nlines, kThreads, 152 * 64);
+        solve_warp_strided_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, S, nlines, f);
     }
-    const size_t ctile = static_cast<size_t>(32) * static_cast<size_t>(n + 1) * sizeof(R);
-    if (S == 1 && ctile <= kTileSmemLimit) {
-        auto k = solve_tile_contig_kernel<R, P, Q, CYC>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ctile));
-        if (e != cudaSuccess) return e;
-        const int per_sm = static_cast<int>(std::max<size_t>(1, 220 * 1024 / (ctile + 1024)));
-        const int64_t ntiles = (nlines + 31) / 32;
-        const int grid = static_cast<int>(std::min<int64_t>(ntiles, int64_t{sm_count_solve()} * per_sm));
-        k<<<grid, 32, ctile, s>>>(x, n, nlines, f);
-        note_launch();
-        return cudaGetLastError();
-    }
-    return launch_solve_pq_fallback<R, P, Q, CYC>(x, n, S, nlines, f, s);
-}
-
-template <class R, int P, int Q, bool CYC>
-cudaError_t launch_solve_pq_fallback(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
-                                     cudaStream_t s) {
-    const size_t smem = static_cast<size_t>(32) * static_cast<size_t>(n + 1) * sizeof(R);
-    if (S == 1 && smem <= 96 * 1024) {
-        auto k = solve_contig_kernel<R, P, Q, CYC>;
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(smem));
-            if (e != cudaSuccess) return e;
-        }
-        const int grid = grid_for(nlines, 32, 152 * 64);
-        k<<<grid, 32, smem, s>>>(x, n, nlines, f);
-        note_launch();
-        return cudaGetLastError();
-    }
-    const int grid = grid_for(nlines, 128, 152 * 64);
-    solve_strided_kernel<R, P, Q, CYC><<<grid, 128, 0, s>>>(x, n, S, nlines, f);
     note_launch();
     return cudaGetLastError();
 }
@@ -318,66 +196,90 @@ struct AxisPos {
 
 // One residual pass of the mixed form's refinement along an axis of n points
 // and stride S, over all N values (channel blocks included), with Dot2
-// accumulation: out = A_axis in as a double-float, or on the last pass
-// (FINAL) r = rhs - A_axis in rounded to FP32 -- the correction solve's
+// accumulation over the axis' band stencil (dot2_band_row, the operations of
+// the batched residual): out = A_axis in as a double-float, or on the last
+// pass (FINAL) r = rhs - A_axis in rounded to FP32 -- the correction solve's
 // right-hand side. HAS_LO: the input is double-float (else plain FP32). One
-// thread per output element; adjacent threads read adjacent elements of
-// every tap.
-template <class I, bool HAS_LO, bool FINAL>
+// thread per output element, two elements per loop trip (independent loads
+// in flight); the columns are computed, not loaded, and on a strided axis
+// the warp's coefficient loads are broadcasts.
+template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
 __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restrict__ in_hi,
                                                             const float* __restrict__ in_lo, float* __restrict__ out_hi,
                                                             float* __restrict__ out_lo,
                                                             const float* __restrict__ rhs_hi,
                                                             const float* __restrict__ rhs_lo, float* __restrict__ r,
-                                                            AxisPos pos, I S, I N, int width,
-                                                            const int32_t* __restrict__ col,
+                                                            AxisPos pos, I S, I N, int n,
                                                             const float2* __restrict__ val) {
-    for (I e = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e < N;
-         e += static_cast<I>(gridDim.x) * blockDim.x) {
-        const I i = pos(e);
-        Dot2 acc{0.0f, 0.0f};
-        if (FINAL) acc = Dot2{rhs_hi[e], rhs_lo[e]};
-        dot2_row<HAS_LO, I>(acc, FINAL ? -1.0f : 1.0f, in_hi, in_lo, e - i * S, static_cast<int>(i), S, width, col,
-                            val);
-        if (FINAL) {
-            r[e] = __fadd_rn(acc.s, acc.c);
-        } else {
-            const DF v = dot2_value(acc);
-            out_hi[e] = v.hi;
-            out_lo[e] = v.lo;
+    const I stride = static_cast<I>(gridDim.x) * blockDim.x;
+    for (I e0 = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e0 < N; e0 += 2 * stride) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const I e = e0 + u * stride;
+            if (e < N) {
+                const I i = pos(e);
+                Dot2 acc{0.0f, 0.0f};
+                if (FINAL) acc = Dot2{rhs_hi[e], rhs_lo[e]};
+                dot2_band_row_t<BAND, PERIODIC, HAS_LO, I>(acc, FINAL ? -1.0f : 1.0f, in_hi, in_lo, e - i * S,
+                                                            static_cast<int>(i), n, S, val);
+                if (FINAL) {
+                    r[e] = __fadd_rn(acc.s, acc.c);
+                } else {
+                    const DF v = dot2_value(acc);
+                    out_hi[e] = v.hi;
+                    out_lo[e] = v.lo;
+                }
+            }
         }
     }
 }
 
-template <class I, bool HAS_LO, bool FINAL>
+template <int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
 void launch_residual_t(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
-                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, int width, const int32_t* col,
-                       const float2* val, cudaStream_t s) {
+                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, const float2* val,
+                       cudaStream_t s) {
     AxisPos pos{};
+    pos.S64 = S;
+    pos.n64 = n;
+    const int grid = grid_for((N + 1) / 2, 256, 152 * 16);
     if (N <= kIndex32Max) {
         pos.byS = FastDiv::make(static_cast<uint32_t>(S));
         pos.byN = FastDiv::make(static_cast<uint32_t>(n));
+        residual_pass_kernel<uint32_t, BAND, PERIODIC, HAS_LO, FINAL><<<grid, 256, 0, s>>>(
+            in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, static_cast<uint32_t>(S), static_cast<uint32_t>(N),
+            static_cast<int>(n), val);
+    } else {
+        residual_pass_kernel<int64_t, BAND, PERIODIC, HAS_LO, FINAL><<<grid, 256, 0, s>>>(
+            in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, S, N, static_cast<int>(n), val);
     }
-    pos.S64 = S;
-    pos.n64 = n;
-    residual_pass_kernel<I, HAS_LO, FINAL><<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(
-        in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, static_cast<I>(S), static_cast<I>(N), width, col, val);
 }
 
-template <class I>
-void launch_residual_i(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
-                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, int width, const int32_t* col,
-                       const float2* val, cudaStream_t s) {
+template <int BAND, bool PERIODIC>
+void launch_residual_bp(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
+                        const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, const float2* val,
+                        cudaStream_t s) {
     const bool lo = in_lo != nullptr, fin = rhs_hi != nullptr;
     if (lo && fin)
-        launch_residual_t<I, true, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+        launch_residual_t<BAND, PERIODIC, true, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
     else if (lo)
-        launch_residual_t<I, true, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+        launch_residual_t<BAND, PERIODIC, true, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
+                                                       s);
     else if (fin)
-        launch_residual_t<I, false, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+        launch_residual_t<BAND, PERIODIC, false, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
+                                                       s);
     else
-        launch_residual_t<I, false, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val,
-                                           s);
+        launch_residual_t<BAND, PERIODIC, false, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
+                                                        s);
+}
+
+template <int BAND>
+void launch_residual_b(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
+                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, bool periodic,
+                       const float2* val, cudaStream_t s) {
+    if (periodic)
+        launch_residual_bp<BAND, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
+    else
+        launch_residual_bp<BAND, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
 }
 
 // (c, lo) += corr, element-wise in double-float (lo taken as 0 when has_lo
@@ -404,18 +306,16 @@ int take_device_error(cudaStream_t s) {
     return v;
 }
 
-cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                  bool cyclic, const double* lower, const double* upper,
-                                  const double* dinv, const double* bottom, const double* right,
-                                  cudaStream_t s) {
+cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                  const double* lower, const double* upper, const double* dinv, const double* bottom,
+                                  const double* right, cudaStream_t s) {
     FactorView<double> f{n, lower, upper, dinv, bottom, right};
     return launch_solve_r<double>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 
-cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                  bool cyclic, const float* lower, const float* upper,
-                                  const float* dinv, const float* bottom, const float* right,
-                                  cudaStream_t s) {
+cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                  const float* lower, const float* upper, const float* dinv, const float* bottom,
+                                  const float* right, cudaStream_t s) {
     FactorView<float> f{n, lower, upper, dinv, bottom, right};
     return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
 }
@@ -448,11 +348,20 @@ cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_
 
 cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
                                  const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
-                                 int width, const int32_t* col, const float2* val, cudaStream_t s) {
-    if (N <= kIndex32Max)
-        launch_residual_i<uint32_t>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
-    else
-        launch_residual_i<int64_t>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, width, col, val, s);
+                                 int band, bool periodic, const float2* val, cudaStream_t s) {
+#define INTP_RESIDUAL_CASE(B) \
+    case B: launch_residual_b<B>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, periodic, val, s); break;
+    switch (band) {
+        INTP_RESIDUAL_CASE(0)
+        INTP_RESIDUAL_CASE(1)
+        INTP_RESIDUAL_CASE(2)
+        INTP_RESIDUAL_CASE(3)
+        INTP_RESIDUAL_CASE(4)
+        INTP_RESIDUAL_CASE(5)
+        INTP_RESIDUAL_CASE(6)
+        default: return cudaErrorInvalidValue;
+    }
+#undef INTP_RESIDUAL_CASE
     note_launch();
     return cudaGetLastError();
 }

@@ -26,25 +26,110 @@ struct FactorView {
     const R* right;   // [P*n]
 };
 
-// Accessor of one line: element k at base[k*S].
+// a * b + c with one rounding (FP32 or FP64).
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Chunk accessors of one line: load(i0, cnt, buf) fills buf[0 .. cnt-1] with
+// elements i0 .. i0+cnt-1 of the line, store(i0, cnt, buf) writes them back.
+
+// Element k at base[k*S] (global memory; each lane its own line).
 template <class R>
-struct StridedLine {
+struct StridedChunks {
     R* base;
     int64_t S;
-    __device__ __forceinline__ R load(int64_t k) const { return base[k * S]; }
-    __device__ __forceinline__ void store(int64_t k, R v) const { base[k * S] = v; }
+    template <int K>
+    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = base[(i0 + k) * S];
+    }
+    template <int K>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) base[(i0 + k) * S] = buf[k];
+    }
 };
 
 // A line held contiguously (in shared memory).
 template <class R>
-struct SmemLine {
+struct SmemChunks {
     R* base;
-    __device__ __forceinline__ R load(int64_t k) const { return base[k]; }
-    __device__ __forceinline__ void store(int64_t k, R v) const { base[k] = v; }
+    template <int K>
+    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = base[i0 + k];
+    }
+    template <int K>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) base[i0 + k] = buf[k];
+    }
 };
 
-template <class R, int P, int Q, bool CYC, class Line>
-__device__ __forceinline__ void solve_line(const FactorView<R>& f, const Line& line) {
+// 32 consecutive contiguous lines, lane l owning line l0 + l (x = line l0's
+// first element, `rows` lines present), each chunk moved through a per-warp
+// [32][33] shared-memory transpose: the global accesses are runs of one
+// line's elements (lane j touches element i0 + j of every line, all 32
+// loads in flight), and lane l reading element k of its line touches bank
+// (l + k) mod 32. Chunks are at most 32 elements. Warp-collective: every
+// lane calls with the same chunk; lanes past `rows` compute on stale values
+// that are never written back.
+template <class R>
+struct WarpContigChunks {
+    R* x;
+    int64_t n;
+    int rows;
+    R* stage;
+    int lane;
+    template <int K>
+    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
+        static_assert(K <= 32, "chunks of at most 32 elements");
+        __syncwarp();
+        if (lane < cnt) {
+            // rows in groups (32 FP32 / 16 FP64 loads in flight per lane)
+            constexpr int G = sizeof(R) == 4 ? 32 : 16;
+#pragma unroll
+            for (int g = 0; g < 32; g += G) {
+                R v[G];
+#pragma unroll
+                for (int r = 0; r < G; ++r)
+                    if (g + r < rows) v[r] = x[(g + r) * n + i0 + lane];
+#pragma unroll
+                for (int r = 0; r < G; ++r) stage[(g + r) * 33 + lane] = v[r];
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = stage[lane * 33 + k];
+    }
+    template <int K>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const {
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) stage[lane * 33 + k] = buf[k];
+        __syncwarp();
+        if (lane < cnt) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r)
+                if (r < rows) x[r * n + i0 + lane] = stage[r * 33 + lane];
+        }
+    }
+};
+
+// Substitution of one line with the band / cyclic-band factor, walking the
+// line in chunks of K elements (K loads in flight per lane, the values of a
+// chunk held in registers). Every step is the same sequence of roundings as
+// the textbook recurrences written out with explicit FMAs, so all callers
+// (strided lines, transposed contiguous lines, batched items) agree bit for
+// bit.
+template <class R, int P, int Q, bool CYC, int K, class Io>
+__device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const Io& io) {
     const int64_t n = f.n;
     // ---- forward: y = L^{-1} x ----
     R win[P > 0 ? P : 1];  // y_{i-P} .. y_{i-1}
@@ -52,29 +137,39 @@ __device__ __forceinline__ void solve_line(const FactorView<R>& f, const Line& l
     for (int k = 0; k < P; ++k) win[k] = 0;
     R acc[Q > 0 ? Q : 1];  // cyclic: rows n-Q .. n-1 collecting side-band terms
     if (CYC) {
+        R tmp[K];
+        io.load(n - Q, Q, tmp);
 #pragma unroll
-        for (int r = 0; r < Q; ++r) acc[r] = line.load(n - Q + r);
+        for (int r = 0; r < Q; ++r) acc[r] = tmp[r];
     }
-    for (int64_t i = 0; i < n; ++i) {
-        R v;
-        if (CYC && i >= n - Q) {
-            v = acc[0];
+    for (int64_t i0 = 0; i0 < n; i0 += K) {
+        const int cnt = static_cast<int>(n - i0 < K ? n - i0 : K);
+        R buf[K];
+        io.load(i0, cnt, buf);
 #pragma unroll
-            for (int r = 1; r < Q; ++r)
-                if (i == n - Q + r) v = acc[r];
-        } else {
-            v = line.load(i);
+        for (int k = 0; k < K; ++k) {
+            if (k < cnt) {
+                const int64_t i = i0 + k;
+                R v = buf[k];
+                if (CYC && i >= n - Q) {
+                    v = acc[0];
+#pragma unroll
+                    for (int r = 1; r < Q; ++r)
+                        if (i == n - Q + r) v = acc[r];
+                }
+#pragma unroll
+                for (int kk = 0; kk < P; ++kk) v = fma_r(-__ldg(f.lower + i * P + kk), win[kk], v);
+                if (CYC && i < n - P - 1) {
+#pragma unroll
+                    for (int r = 0; r < Q; ++r) acc[r] = fma_r(-__ldg(f.bottom + r * n + i), v, acc[r]);
+                }
+                buf[k] = v;
+#pragma unroll
+                for (int kk = 0; kk + 1 < P; ++kk) win[kk] = win[kk + 1];
+                if (P > 0) win[P - 1] = v;
+            }
         }
-#pragma unroll
-        for (int k = 0; k < P; ++k) v -= __ldg(f.lower + i * P + k) * win[k];
-        if (CYC && i < n - P - 1) {
-#pragma unroll
-            for (int r = 0; r < Q; ++r) acc[r] -= __ldg(f.bottom + r * n + i) * v;
-        }
-        line.store(i, v);
-#pragma unroll
-        for (int k = 0; k + 1 < P; ++k) win[k] = win[k + 1];
-        if (P > 0) win[P - 1] = v;
+        io.store(i0, cnt, buf);
     }
     // ---- back: x = U^{-1} y ----
     R zw[Q > 0 ? Q : 1];  // z_{i+1} .. z_{i+Q}
@@ -83,25 +178,36 @@ __device__ __forceinline__ void solve_line(const FactorView<R>& f, const Line& l
     R tail[P > 0 ? P : 1];  // cyclic: z_{n-P} .. z_{n-1}
 #pragma unroll
     for (int k = 0; k < P; ++k) tail[k] = 0;
-    for (int64_t i = n - 1; i >= 0; --i) {
-        R v = line.load(i);
-        if (CYC) {
+    for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
+        const int cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
+        const int64_t i0 = i1 - cnt + 1;
+        R buf[K];
+        io.load(i0, cnt, buf);
 #pragma unroll
-            for (int r = P - 1; r >= 0; --r)
-                if (n - P + r > i + Q) v -= __ldg(f.right + r * n + i) * tail[r];
+        for (int k = K - 1; k >= 0; --k) {
+            if (k < cnt) {
+                const int64_t i = i0 + k;
+                R v = buf[k];
+                if (CYC) {
+#pragma unroll
+                    for (int r = P - 1; r >= 0; --r)
+                        if (n - P + r > i + Q) v = fma_r(-__ldg(f.right + r * n + i), tail[r], v);
+                }
+#pragma unroll
+                for (int kk = Q - 1; kk >= 0; --kk) v = fma_r(-__ldg(f.upper + i * Q + kk), zw[kk], v);
+                v *= __ldg(f.dinv + i);
+                buf[k] = v;
+                if (CYC) {
+#pragma unroll
+                    for (int r = 0; r < P; ++r)
+                        if (i == n - P + r) tail[r] = v;
+                }
+#pragma unroll
+                for (int kk = Q - 1; kk > 0; --kk) zw[kk] = zw[kk - 1];
+                if (Q > 0) zw[0] = v;
+            }
         }
-#pragma unroll
-        for (int k = Q - 1; k >= 0; --k) v -= __ldg(f.upper + i * Q + k) * zw[k];
-        v *= __ldg(f.dinv + i);
-        line.store(i, v);
-        if (CYC) {
-#pragma unroll
-            for (int r = 0; r < P; ++r)
-                if (i == n - P + r) tail[r] = v;
-        }
-#pragma unroll
-        for (int k = Q - 1; k > 0; --k) zw[k] = zw[k - 1];
-        if (Q > 0) zw[0] = v;
+        io.store(i0, cnt, buf);
     }
 }
 

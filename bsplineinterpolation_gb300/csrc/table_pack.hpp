@@ -33,27 +33,24 @@ struct Arena {
 };
 
 // Device pointers of one axis's LU factor (FP64 and FP32 copies) and of its
-// collocation rows as a stencil (double-float residuals of the mixed form:
-// row i's taps at scol[i * width ..], values as (hi, lo) float pairs).
+// collocation rows as a band stencil (double-float residuals of the mixed
+// form): sval[i * (2 * band + 1) + d] = A(i, i - band + d) as a (hi, lo)
+// float pair, the column taken cyclically on a periodic axis and the value
+// 0 where a non-periodic column falls outside the axis.
 struct AxisFactorDev {
     const double *lower, *upper, *dinv, *bottom, *right;
     const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
-    const int32_t* scol;
     const float2* sval;
-    int width;
+    int band;
 };
 
 // Arena offsets of one table's per-axis arrays.
 struct PackedTable {
     struct Axis {
         size_t knots, keys, rinv, rinvf, kdf, khi, klo;
-        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, scol, sval;
+        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, sval;
     } ax[kMaxDim];
 };
-
-// Nonzero taps of the widest row of a collocation stencil (the packed
-// stencil's row width).
-int stencil_taps(const RowStencil& st);
 
 // Appends the per-axis arrays of `m` to the arena.
 void pack_table(const TableModel& m, Arena& ar, PackedTable& pt);
