@@ -38,13 +38,11 @@ int grid_for(int64_t n, int block, int max_blocks) {
     return static_cast<int>(g);
 }
 
-// Lines are walked in chunks of elements held in registers: 32 for the
-// contiguous axis (one shared-memory transpose per chunk), fewer on strided
-// axes, where every element of a chunk is a separate global load in flight
-// (register budget).
-constexpr int kChunk = 32;
+// Lines are walked in chunks of elements held in registers: 16 FP32 or 8 FP64
+// values per lane (register budget: one wave of line groups per pass at
+// 256^3; longer chunks cost a second wave).
 template <class R>
-constexpr int strided_chunk() {
+constexpr int line_chunk() {
     return sizeof(R) == 4 ? 16 : 8;
 }
 constexpr int kSolveWarps = 4;  // warps per block
@@ -59,7 +57,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R*
     for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
          l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t o = l / S, t = l - o * S;
-        solve_line_chunked<R, P, Q, CYC, strided_chunk<R>()>(f, StridedChunks<R>{x + o * n * S + t, S});
+        solve_line_chunked<R, P, Q, CYC, line_chunk<R>()>(f, StridedChunks<R>{x + o * n * S + t, S});
     }
 }
 
@@ -75,7 +73,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_kernel(
         const int64_t l0 = g * 32;
         const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
         WarpContigChunks<R> io{x + l0 * n, n, rows, stage[warp], lane};
-        solve_line_chunked<R, P, Q, CYC, strided_chunk<R>()>(f, io);
+        solve_line_chunked<R, P, Q, CYC, line_chunk<R>()>(f, io);
     }
 }
 
