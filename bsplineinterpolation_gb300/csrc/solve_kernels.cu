@@ -77,6 +77,24 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_kernel(
     }
 }
 
+// Contiguous FP32 lines of a length divisible by 4, 16-byte aligned: the
+// chunks move as float4 vectors (WarpContigChunksV4).
+template <int P, int Q, bool CYC>
+__global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_v4_kernel(float* __restrict__ x, int64_t n,
+                                                                                int64_t nlines,
+                                                                                FactorView<float> f) {
+    __shared__ __align__(16) float stage[kSolveWarps][32 * WarpContigChunksV4::kPitch];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t ngroups = (nlines + 31) / 32;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(kSolveWarps) + warp; g < ngroups;
+         g += static_cast<int64_t>(gridDim.x) * kSolveWarps) {
+        const int64_t l0 = g * 32;
+        const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
+        WarpContigChunksV4 io{x + l0 * n, n, rows, stage[warp], lane};
+        solve_line_chunked<float, P, Q, CYC, line_chunk<float>()>(f, io);
+    }
+}
+
 template <class R, int P, int Q, bool CYC>
 cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
                             cudaStream_t s) {
@@ -84,7 +102,12 @@ cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const Fa
     if (S == 1) {
         const int64_t groups = (nlines + 31) / 32;
         const int grid = grid_for(groups, kSolveWarps, 152 * 64);
-        solve_warp_contig_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, nlines, f);
+        bool vec = false;
+        if constexpr (sizeof(R) == 4) vec = n % 4 == 0 && reinterpret_cast<uintptr_t>(x) % 16 == 0;
+        if constexpr (sizeof(R) == 4) {
+            if (vec) solve_warp_contig_v4_kernel<P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, nlines, f);
+        }
+        if (!vec) solve_warp_contig_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, nlines, f);
     } else {
         const int grid = grid_for(nlines, kThreads, 152 * 64);
         solve_warp_strided_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, S, nlines, f);

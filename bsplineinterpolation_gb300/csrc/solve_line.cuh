@@ -122,6 +122,89 @@ struct WarpContigChunks {
     }
 };
 
+// WarpContigChunks for FP32 lines whose length is a multiple of 4 (every line
+// starts 16-byte aligned): chunks of 16 elements move as float4 vectors
+// through a per-warp [32][20] stage. Lane l = 4 * row_sub + q loads column
+// group q (elements 4q .. 4q+3 of the chunk) of rows row_sub, +8, +16, +24;
+// lane l then reads its own row as four float4 (16-byte units 5l + j: the
+// eight lanes of a phase hit distinct bank groups). A chunk that does not
+// start on a multiple of 4 (the cyclic corner read) takes per-element
+// copies. Only data moves: results equal those of WarpContigChunks.
+struct WarpContigChunksV4 {
+    float* x;  // first element of line l0
+    int64_t n;
+    int rows;
+    float* stage;  // 32 * 20 floats
+    int lane;
+    static constexpr int kPitch = 20;
+    template <int K>
+    __device__ __forceinline__ void load(int64_t i0, int cnt, float (&buf)[K]) const {
+        static_assert(K <= 16, "chunks of at most 16 elements");
+        __syncwarp();
+        const int q = lane & 3;
+        const bool vec = (i0 & 3) == 0;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const int r = (lane >> 2) + 8 * g;
+            if (r < rows && 4 * q < cnt) {
+                const float* src = x + r * n + i0 + 4 * q;
+                float4 v;
+                if (vec && 4 * q + 4 <= cnt) {
+                    v = *reinterpret_cast<const float4*>(src);
+                } else {
+                    v.x = src[0];
+                    v.y = 4 * q + 1 < cnt ? src[1] : 0.0f;
+                    v.z = 4 * q + 2 < cnt ? src[2] : 0.0f;
+                    v.w = 4 * q + 3 < cnt ? src[3] : 0.0f;
+                }
+                *reinterpret_cast<float4*>(stage + r * kPitch + 4 * q) = v;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < (K + 3) / 4; ++j) {
+            const float4 v = *reinterpret_cast<const float4*>(stage + lane * kPitch + 4 * j);
+            if (4 * j < K) buf[4 * j] = v.x;
+            if (4 * j + 1 < K) buf[4 * j + 1] = v.y;
+            if (4 * j + 2 < K) buf[4 * j + 2] = v.z;
+            if (4 * j + 3 < K) buf[4 * j + 3] = v.w;
+        }
+    }
+    template <int K>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const float (&buf)[K]) const {
+        static_assert(K <= 16, "chunks of at most 16 elements");
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < (K + 3) / 4; ++j) {
+            float4 v;
+            v.x = 4 * j < K ? buf[4 * j] : 0.0f;
+            v.y = 4 * j + 1 < K ? buf[4 * j + 1] : 0.0f;
+            v.z = 4 * j + 2 < K ? buf[4 * j + 2] : 0.0f;
+            v.w = 4 * j + 3 < K ? buf[4 * j + 3] : 0.0f;
+            *reinterpret_cast<float4*>(stage + lane * kPitch + 4 * j) = v;
+        }
+        __syncwarp();
+        const int q = lane & 3;
+        const bool vec = (i0 & 3) == 0;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const int r = (lane >> 2) + 8 * g;
+            if (r < rows && 4 * q < cnt) {
+                float* dst = x + r * n + i0 + 4 * q;
+                const float4 v = *reinterpret_cast<const float4*>(stage + r * kPitch + 4 * q);
+                if (vec && 4 * q + 4 <= cnt) {
+                    *reinterpret_cast<float4*>(dst) = v;
+                } else {
+                    dst[0] = v.x;
+                    if (4 * q + 1 < cnt) dst[1] = v.y;
+                    if (4 * q + 2 < cnt) dst[2] = v.z;
+                    if (4 * q + 3 < cnt) dst[3] = v.w;
+                }
+            }
+        }
+    }
+};
+
 // Substitution of one line with the band / cyclic-band factor, walking the
 // line in chunks of K elements (K loads in flight per lane, the values of a
 // chunk held in registers). Every step is the same sequence of roundings as
