@@ -102,20 +102,24 @@ __device__ __forceinline__ void dot2_band_row(Dot2& acc, float sign, const float
     }
 }
 
-// dot2_band_row with the band and the periodicity known at compile time
-// (taps unrolled; the same operations in the same order).
-template <int BAND, bool PERIODIC, bool HAS_LO, class I>
-__device__ __forceinline__ void dot2_band_row_t(Dot2& acc, float sign, const float* __restrict__ hi,
-                                                const float* __restrict__ lo, I base, int i, int n, I S,
-                                                const float2* __restrict__ val) {
+// dot2_band_row with the band, the periodicity and the sign (NEG: -1) known
+// at compile time: taps unrolled, the negation folded into the products,
+// the same values in the same order. (A zero high part implies a zero low
+// part: the low part is the rounding of the coefficient minus its high
+// part.)
+template <int BAND, bool PERIODIC, bool HAS_LO, bool NEG, class I>
+__device__ __forceinline__ void dot2_band_row_t(Dot2& acc, const float* __restrict__ hi, const float* __restrict__ lo,
+                                                I base, int i, int n, I S, const float2* __restrict__ val) {
     constexpr int W = 2 * BAND + 1;
     const float2* __restrict__ row = val + i * W;
 #pragma unroll
     for (int d = 0; d < W; ++d) {
         float2 a = __ldg(row + d);
-        if (a.x == 0.0f && a.y == 0.0f) continue;
-        a.x *= sign;
-        a.y *= sign;
+        if (a.x == 0.0f) continue;
+        if (NEG) {
+            a.x = -a.x;
+            a.y = -a.y;
+        }
         int c = i - BAND + d;
         if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
         const I j = base + static_cast<I>(c) * S;

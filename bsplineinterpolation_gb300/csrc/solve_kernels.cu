@@ -241,8 +241,8 @@ __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restr
                 const I i = pos(e);
                 Dot2 acc{0.0f, 0.0f};
                 if (FINAL) acc = Dot2{rhs_hi[e], rhs_lo[e]};
-                dot2_band_row_t<BAND, PERIODIC, HAS_LO, I>(acc, FINAL ? -1.0f : 1.0f, in_hi, in_lo, e - i * S,
-                                                            static_cast<int>(i), n, S, val);
+                dot2_band_row_t<BAND, PERIODIC, HAS_LO, FINAL, I>(acc, in_hi, in_lo, e - i * S, static_cast<int>(i), n,
+                                                                   S, val);
                 if (FINAL) {
                     r[e] = __fadd_rn(acc.s, acc.c);
                 } else {
