@@ -221,9 +221,11 @@ struct AxisPos {
 // the batched residual): out = A_axis in as a double-float, or on the last
 // pass (FINAL) r = rhs - A_axis in rounded to FP32 -- the correction solve's
 // right-hand side. HAS_LO: the input is double-float (else plain FP32). One
-// thread per output element, two elements per loop trip (independent loads
+// thread per output element, kResidualIlp elements per loop trip (independent loads
 // in flight); the columns are computed, not loaded, and on a strided axis
 // the warp's coefficient loads are broadcasts.
+constexpr int kResidualIlp = 4;
+
 template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
 __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restrict__ in_hi,
                                                             const float* __restrict__ in_lo, float* __restrict__ out_hi,
@@ -233,9 +235,9 @@ __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restr
                                                             AxisPos pos, I S, I N, int n,
                                                             const float2* __restrict__ val) {
     const I stride = static_cast<I>(gridDim.x) * blockDim.x;
-    for (I e0 = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e0 < N; e0 += 2 * stride) {
+    for (I e0 = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e0 < N; e0 += kResidualIlp * stride) {
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kResidualIlp; ++u) {
             const I e = e0 + u * stride;
             if (e < N) {
                 const I i = pos(e);
@@ -262,7 +264,7 @@ void launch_residual_t(const float* in_hi, const float* in_lo, float* out_hi, fl
     AxisPos pos{};
     pos.S64 = S;
     pos.n64 = n;
-    const int grid = grid_for((N + 1) / 2, 256, 152 * 16);
+    const int grid = grid_for((N + kResidualIlp - 1) / kResidualIlp, 256, 152 * 16);
     if (N <= kIndex32Max) {
         pos.byS = FastDiv::make(static_cast<uint32_t>(S));
         pos.byN = FastDiv::make(static_cast<uint32_t>(n));
