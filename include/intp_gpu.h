@@ -40,7 +40,7 @@ typedef enum intp_status {
 
 typedef enum intp_precision {
     INTP_PRECISION_FP64 = 0,  /* FP64 end to end (parity form) */
-    INTP_PRECISION_MIXED = 1  /* FP32 solve + refinement, FP32 basis/contraction */
+    INTP_PRECISION_MIXED = 1  /* FP32 solve + double-float refinement, FP32 basis/contraction */
 } intp_precision;
 
 typedef enum intp_dtype { INTP_F64 = 0, INTP_F32 = 1 } intp_dtype;
@@ -53,7 +53,7 @@ typedef struct intp_table_desc {
     int32_t dim;           /* 1..INTP_GPU_MAX_DIM */
     int32_t order;         /* 0..INTP_GPU_MAX_ORDER */
     int32_t precision;     /* intp_precision */
-    int32_t refine_steps;  /* mixed only: -1 = automatic, else 0..4 */
+    int32_t refine_steps;  /* mixed only: -1 = automatic (at least 1), else 0..4 */
     int32_t periodic[INTP_GPU_MAX_DIM];
     int64_t size[INTP_GPU_MAX_DIM];     /* samples per axis (mesh dim sizes) */
     double range_lo[INTP_GPU_MAX_DIM];  /* uniform axis: x_min */
