@@ -40,7 +40,7 @@ namespace {
 constexpr int kBatchMaxDim = 3;
 constexpr int32_t kChunkElems = 8192;
 constexpr int64_t kEvalRun = 2048;           // query points per evaluation CTA
-constexpr size_t kStageBytes = 34 * 1024;     // shared memory per warp for contiguous lines
+constexpr size_t kStageBytes = 16 * 1024;     // shared memory per warp for contiguous lines
 constexpr size_t kStageMaxBytes = 200 * 1024;  // longest contiguous line staged
 
 intp_status bfail(intp_status s, const std::string& msg);
