@@ -15,8 +15,15 @@ through the C-ABI host-buffer path (values and coordinates copied from
 pinned host memory, results copied back, inside the timed region).
 Multi-GPU runs are independent replicas (the path does not exchange data):
 `value` sums the points of all ranks over the slowest rank's time.
-`--impl reference` times the reference algorithm on the host cores (the C
-restatement of the reference, multithreaded) on a bounded sample.
+`--impl reference` times the reference's own CPU code on the host cores:
+its headers compiled with g++ -O3 INTP_MULTITHREAD (oracle/_ref, from the
+reference install staged under baseline/_ref), over whole steps.
+
+Besides the headline, the line carries the 2D cubic 64^2 workload
+(`plain_2d_64`) and the periodic order-7 512^2 workload (`periodic_o7_512`),
+each timed on the GPU in both forms and on the reference CPU path, with the
+GPU's error against the reference outputs, and the headline's error against
+the reference on the CPU baseline's sample (`max_rel_err_vs_reference`).
 """
 import argparse
 import ctypes as C
@@ -57,6 +64,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-tables workload")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop workload")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 2D cubic and periodic order-7 workloads")
+    ap.add_argument("--cpu-sample", type=int, default=20_000_000,
+                    help="points of the CPU baseline's bounded sample (our arm)")
+    ap.add_argument("--ref-seconds", type=float, default=90.0,
+                    help="reference arm: time budget of the timed whole steps")
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--batched-tables", type=int, default=4096)
     ap.add_argument("--batched-only", action="store_true",
@@ -177,37 +189,191 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (reference algorithm on the host cores)
+# CPU baseline: the reference's own code on the host cores
 # ---------------------------------------------------------------------------
-def cpu_baseline(npts_step, mesh_n, sample_pts, gpu_check=None):
-    """Times the reference algorithm (C restatement, all host threads) on a
-    bounded sample: the full mesh solve plus `sample_pts` evaluations of
-    value and d/dx; the step time is extrapolated to npts_step points."""
-    from oracle import oracle
+def _reference_available():
+    from oracle import reference
+    return all(reference.available(lay) for lay in reference.LAYOUTS)
+
+
+def _pick_layout(order, periodic, vals, lo, hi, pts, derivs, threads, npts_step):
+    """Builds the reference in both control-point layouts (INTP_CELL_LAYOUT
+    and plain) and keeps the one with the shorter projected step (build +
+    npts_step evaluations at the rate measured on `pts`)."""
+    from oracle import reference
+    best = None
+    for layout in reference.LAYOUTS:
+        f = reference.RefFunction(order, periodic, vals, lo, hi, layout=layout)
+        t0 = time.perf_counter()
+        f.outputs(pts, derivs, nthreads=threads)
+        rate = pts.shape[0] / (time.perf_counter() - t0)
+        step = f.build_seconds + npts_step / rate
+        if best is None or step < best[0]:
+            best = (step, layout, f, rate)
+        else:
+            del f
+    return best[1], best[2]
+
+
+def cpu_baseline(npts_step, mesh_n, sample_pts):
+    """Times the reference CPU path on a bounded sample of the 3D cubic
+    workload, all host threads: the reference headers (INTP_MULTITHREAD, the
+    faster of the cell and plain layouts) when oracle/_ref is built, else the
+    C restatement. The sample is the full 256^3 build plus `sample_pts` of the
+    npts_step points (value and d/dx); the step time is build + npts_step /
+    measured rate. Returns (result, (values, points, outputs)) so that the GPU
+    outputs can be checked against the same reference outputs."""
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(SEED)
     vals = make_values_np(mesh_n, rng)
     pts = make_points_np(sample_pts, rng)
-    s = oracle.Spline(3, 3, [0, 0, 0], [mesh_n] * 3, [-1.0] * 3, [1.0] * 3)
-    t0 = time.perf_counter()
-    s.interpolate(vals, nthreads=threads)
-    t1 = time.perf_counter()
-    out = s.derivative(pts, DERIVS, nthreads=threads)
-    t2 = time.perf_counter()
-    solve_s = t1 - t0
-    eval_s = (t2 - t1) * npts_step / sample_pts
+    lo, hi = [-1.0] * 3, [1.0] * 3
+    if _reference_available():
+        layout, f = _pick_layout(3, [False] * 3, vals, lo, hi, pts[:1_000_000], DERIVS, threads, npts_step)
+        build_s = f.build_seconds
+        t0 = time.perf_counter()
+        out = f.outputs(pts, DERIVS, nthreads=threads)
+        eval_s = time.perf_counter() - t0
+        kind = "reference"
+        what = "reference headers (g++ -O3 INTP_MULTITHREAD, %s layout)" % layout
+    else:
+        from oracle import oracle
+        s = oracle.Spline(3, 3, [0, 0, 0], [mesh_n] * 3, lo, hi)
+        t0 = time.perf_counter()
+        s.interpolate(vals, nthreads=threads)
+        t1 = time.perf_counter()
+        out = s.derivative(pts, DERIVS, nthreads=threads)
+        build_s, eval_s = t1 - t0, time.perf_counter() - t1
+        kind = "port"
+        what = "C restatement of the reference (reference build unavailable)"
+    rate = sample_pts / eval_s
     res = {
-        "value": npts_step / (solve_s + eval_s),
+        "value": npts_step / (build_s + npts_step / rate),
         "unit": "points/s",
         "cores": threads,
-        "kind": "port",
-        "sample": "full %d^3 solve + %d of %d points (value and d/dx), step time extrapolated"
-                  % (mesh_n, sample_pts, npts_step),
-        "solve_ms": solve_s * 1e3,
-        "eval_points_per_s": sample_pts / (t2 - t1),
+        "kind": kind,
+        "sample": "%s: full %d^3 build + %d of %d points (value and d/dx); step time = build + %d / measured rate"
+                  % (what, mesh_n, sample_pts, npts_step, npts_step),
+        "build_ms": build_s * 1e3,
+        "eval_points_per_s": rate,
     }
-    if gpu_check is not None:
-        res["_check"] = (vals, pts, out)
+    return res, (vals, pts, out)
+
+
+def max_rel_err(got, want):
+    """max |got - want| / max |want| per output column."""
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    return [float(np.max(np.abs(got[:, k] - want[:, k])) / max(np.max(np.abs(want[:, k])), 1e-300))
+            for k in range(want.shape[1])]
+
+
+# ---------------------------------------------------------------------------
+# configs 1 and 4: plain 2D cubic 64^2, periodic order 7 512^2
+# ---------------------------------------------------------------------------
+CFG1 = dict(name="plain_2d_64", order=3, n=(64, 64), periodic=[False, False], lo=[0.0, 0.0], hi=[1.0, 2.0],
+            npts=100_000, derivs=[[0, 0]], seed=20261203 + 0,
+            workload="2D order 3 non-periodic 64x64 on [0,1]x[0,2], z = sin(3x)cos(2y) + N(0,0.01^2); "
+                     "1e5 uniform points, value")
+CFG4 = dict(name="periodic_o7_512", order=7, n=(512, 512), periodic=[True, True], lo=[0.0, 0.0],
+            hi=[2 * np.pi, 2 * np.pi], npts=10_000_000, derivs=[[1, 0], [0, 1], [2, 0], [1, 1], [0, 2]],
+            seed=20261203 + 3,
+            workload="2D order 7 periodic x periodic 512x512, sum of 16 random sinusoids (wavenumbers 1-20); "
+                     "cyclic-band solve, then 1e7 uniform points: d/dx, d/dy, d2/dx2, d2/dxdy, d2/dy2")
+
+
+def config_inputs(cfg):
+    rng = np.random.default_rng(cfg["seed"])
+    n0, n1 = cfg["n"]
+    if cfg["name"] == "plain_2d_64":
+        x = np.linspace(0.0, 1.0, n0)
+        y = np.linspace(0.0, 2.0, n1)
+        vals = np.sin(3 * x)[:, None] * np.cos(2 * y)[None, :] + rng.normal(0.0, 0.01, (n0, n1))
+    else:
+        g0 = np.arange(n0) * (2 * np.pi / n0)  # one period over the axis range
+        g1 = np.arange(n1) * (2 * np.pi / n1)
+        X, Y = np.meshgrid(g0, g1, indexing="ij")
+        vals = np.zeros((n0, n1))
+        for _ in range(16):
+            kx, ky = rng.integers(1, 21, 2)
+            vals += np.sin(kx * X + ky * Y + rng.uniform(0, 2 * np.pi))
+    pts = rng.uniform(cfg["lo"], cfg["hi"], (cfg["npts"], 2))
+    return vals, pts
+
+
+def config_cpu(cfg, vals, pts):
+    """The reference CPU path on one whole step of a config (build + every
+    point), all host threads; returns (timing, outputs)."""
+    threads = os.cpu_count() or 1
+    if _reference_available():
+        sel = pts[:min(pts.shape[0], 200_000)]
+        layout, f = _pick_layout(cfg["order"], cfg["periodic"], vals, cfg["lo"], cfg["hi"], sel, cfg["derivs"],
+                                 threads, pts.shape[0])
+        # the selection built both layouts; the timed step builds again
+        from oracle import reference
+        f = reference.RefFunction(cfg["order"], cfg["periodic"], vals, cfg["lo"], cfg["hi"], layout=layout)
+        build_s = f.build_seconds
+        t0 = time.perf_counter()
+        out = f.outputs(pts, cfg["derivs"], nthreads=threads)
+        eval_s = time.perf_counter() - t0
+        kind = "reference (%s layout)" % layout
+    else:
+        from oracle import oracle
+        s = oracle.Spline(2, cfg["order"], cfg["periodic"], list(cfg["n"]), cfg["lo"], cfg["hi"])
+        t0 = time.perf_counter()
+        s.interpolate(vals, nthreads=threads)
+        t1 = time.perf_counter()
+        out = s.derivative(pts, cfg["derivs"], nthreads=threads)
+        build_s, eval_s = t1 - t0, time.perf_counter() - t1
+        kind = "port"
+    npts = pts.shape[0]
+    return {"points_per_s": npts / (build_s + eval_s), "build_ms": build_s * 1e3, "eval_ms": eval_s * 1e3,
+            "cores": threads, "kind": kind, "steps": 1}, out
+
+
+def config_gpu(cfg, vals, pts, torch, precision, steps=10, warmup=3):
+    """One step = the table's build (control-point solve) + evaluation of
+    every point; CUDA events on the launching stream, inputs in HBM."""
+    import bsplineinterpolation_gb300 as bi
+    r0, r1 = (cfg["lo"][0], cfg["hi"][0]), (cfg["lo"][1], cfg["hi"][1])
+    v = torch.tensor(vals, device="cuda")
+    p = torch.tensor(pts, device="cuda")
+    f = bi.InterpolationFunction(cfg["order"], cfg["periodic"], v, r0, r1, precision=precision)
+    out = torch.empty((pts.shape[0], len(cfg["derivs"])), device="cuda",
+                      dtype=torch.float32 if precision == "mixed" else torch.float64)
+    tpl = f._template
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        tpl._solve(v)
+        f.evaluate(p, derivs=cfg["derivs"], out=out)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1, e2 in ev:
+        e0.record(stream)
+        tpl._solve(v)
+        e1.record(stream)
+        f.evaluate(p, derivs=cfg["derivs"], out=out)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    total = ev[0][0].elapsed_time(ev[-1][2]) / steps
+    res = {"points_per_s": pts.shape[0] / (total / 1e3),
+           "build_ms": float(np.median([a.elapsed_time(b) for a, b, _ in ev])),
+           "eval_ms": float(np.median([b.elapsed_time(c) for _, b, c in ev])),
+           "steps": steps, "warmup": warmup}
+    return res, out.double().cpu().numpy()
+
+
+def run_config(cfg, torch):
+    vals, pts = config_inputs(cfg)
+    cpu, want = config_cpu(cfg, vals, pts)
+    res = {"workload": cfg["workload"], "points": int(pts.shape[0]), "cpu_reference": cpu}
+    for prec in ("fp64", "mixed"):
+        g, got = config_gpu(cfg, vals, pts, torch, prec)
+        errs = max_rel_err(got, want)
+        g["max_rel_err_vs_reference"] = dict(zip([str(d) for d in cfg["derivs"]], errs))
+        res[prec] = g
+    res["norm"] = "max|err| / max|reference| per output, over every point"
     return res
 
 
@@ -343,6 +509,16 @@ def run_ours(args, rank, world):
                           "frac": ach / peak, "traffic": traffic,
                           "kernel": "evaluation", "algorithmic_bytes": alg_bytes,
                           "peak_source": peak_kind}
+    # the solve: the separable algorithm's own traffic, one read and one write
+    # of the mesh per axis pass (3 passes) in the working precision
+    solve_bytes = 3 * 2 * n ** 3 * out_b
+    solve_ms_med = float(np.median(solve_ms))
+    sach = solve_bytes / (solve_ms_med / 1e3) / 1e9
+    result["solve_roofline"] = {"bound": "hbm", "achieved": sach, "peak": peak, "unit": "GB/s",
+                                "frac": sach / peak, "algorithmic_bytes": solve_bytes,
+                                "compulsory_bytes": 2 * n ** 3 * out_b, "peak_source": peak_kind,
+                                "note": "algorithmic bytes: 3 passes x (read + write) x N^3 x %d B; the mixed "
+                                        "build also runs its refinement inside solve_ms" % out_b}
     if clock_info:
         result["clocks"] = clock_info
 
@@ -355,8 +531,10 @@ def run_ours(args, rank, world):
         for k in range(K):
             den = ref64[:, k].abs().max().item()
             errs.append((out[:, k].double() - ref64[:, k]).abs().max().item() / den)
+        s64m = float(np.median(s64))
         result["fp64_plain"] = {"points_per_s": npts * 2 / (tot64 / 1e3),
-                                "solve_ms": float(np.median(s64)), "eval_ms": float(np.median(e64))}
+                                "solve_ms": s64m, "eval_ms": float(np.median(e64)),
+                                "solve_roofline_frac": 3 * 2 * n ** 3 * 8 / (s64m / 1e3) / 1e9 / peak}
         result["mixed_max_rel_err_vs_fp64"] = {"value": errs[0], "d/dx": errs[1],
                                                "norm": "max|err| / max|fp64| over all queries"}
         del f64, out64
@@ -368,11 +546,33 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.no_serve:
         result["serving"] = run_serving(args, torch)
     if rank == 0 and not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline(npts, n, min(npts, 20_000_000))
+        base, check = cpu_baseline(npts, n, min(npts, args.cpu_sample))
+        result["cpu_baseline"] = base
+        result["max_rel_err_vs_reference"] = oracle_check(check, torch)
+    if rank == 0 and not args.no_configs:
+        result["plain_2d_64"] = run_config(CFG1, torch)
+        result["periodic_o7_512"] = run_config(CFG4, torch)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def oracle_check(check, torch):
+    """Both GPU forms built from the CPU sample's value mesh and evaluated at
+    its points, against the reference CPU path's outputs on them."""
+    import bsplineinterpolation_gb300 as bi
+    vals, pts, want = check
+    v = torch.tensor(vals, device="cuda")
+    p = torch.tensor(pts, device="cuda")
+    res = {"points": int(pts.shape[0]), "norm": "max|err| / max|reference| per output over the sample"}
+    for prec in ("fp64", "mixed"):
+        f = bi.InterpolationFunction(3, [False] * 3, v, (-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0), precision=prec)
+        got = f.evaluate(p, derivs=DERIVS).double().cpu().numpy()
+        errs = max_rel_err(got, want)
+        res[prec] = {"value": errs[0], "d/dx": errs[1]}
+        del f
+    return res
 
 
 def e2e(args, f, vals, pts, lib, torch):
@@ -584,24 +784,73 @@ def run_serving(args, torch, rate=2000.0, seed=SEED + 4):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's own CPU code (headers compiled with
+    g++ -O3 INTP_MULTITHREAD; the faster of its two control-point layouts) on
+    whole steps of the 3D cubic workload, all host threads. A step is the
+    reference constructor at 256^3 (knots, factors, solve on its thread pool)
+    plus value and d/dx at every one of the 1e8 points (operator() and
+    derivative(), the points split over the host threads). Warm-up steps run
+    on a 1e6-point sample. Timed steps stop once --ref-seconds have passed
+    (at least one); `steps` reports how many were timed."""
     if rank != 0:
         return None
-    base = cpu_baseline(args.npts, args.mesh, min(args.npts, 10_000_000))
-    steps = max(1, args.steps)
-    return {
-        "metric": METRIC, "value": base["value"], "unit": "points/s", "n_gpus": world,
-        "steps": steps, "warmup": args.warmup,
-        "ms_per_step": args.npts / base["value"] * 1e3, "higher_is_better": True,
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(SEED)
+    n, npts = args.mesh, args.npts
+    vals = make_values_np(n, rng)
+    pts = make_points_np(npts, rng)
+    lo, hi = [-1.0] * 3, [1.0] * 3
+    out = np.empty((npts, len(DERIVS)), np.float64)
+    if _reference_available():
+        from oracle import reference
+        layout, _ = _pick_layout(3, [False] * 3, vals, lo, hi, pts[:1_000_000], DERIVS, threads, npts)
+        kind, what = "reference", "reference headers (g++ -O3 INTP_MULTITHREAD, %s layout)" % layout
+
+        def step(m):
+            t0 = time.perf_counter()
+            f = reference.RefFunction(3, [False] * 3, vals, lo, hi, layout=layout)
+            f.outputs(pts[:m], DERIVS, nthreads=threads, out=out[:m])
+            return time.perf_counter() - t0
+    else:
+        from oracle import oracle
+        kind, what = "port", "C restatement of the reference (reference build unavailable)"
+
+        def step(m):
+            t0 = time.perf_counter()
+            s = oracle.Spline(3, 3, [0, 0, 0], [n] * 3, lo, hi)
+            s.interpolate(vals, nthreads=threads)
+            out[:m] = s.derivative(pts[:m], DERIVS, nthreads=threads)
+            return time.perf_counter() - t0
+    for _ in range(max(0, args.warmup)):
+        step(min(npts, 1_000_000))
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max(1, args.steps):
+        times.append(step(npts))
+        if time.perf_counter() - t_start > args.ref_seconds:
+            break
+    steps = len(times)
+    total = sum(times)
+    res = {
+        "metric": METRIC, "value": npts * steps / total, "unit": "points/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": total / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded; shapes and distributions of the 3D cubic workload)",
-        "config": {"workload": "3D cubic 256^3 build + 1e8 queries value+d/dx", "mesh": [args.mesh] * 3,
-                   "order": 3, "queries": args.npts, "precision": "fp64",
-                   "parallelism": "host threads"},
+        "config": {"workload": "3D cubic 256^3 build + 1e8 queries value+d/dx", "mesh": [n] * 3,
+                   "order": 3, "queries": npts, "precision": "fp64", "parallelism": "host threads",
+                   "steps_requested": args.steps},
         "impl": "reference",
-        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": base["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
     }
+    res["cpu_baseline"] = {"value": res["value"], "unit": "points/s", "cores": threads, "kind": kind,
+                           "sample": "%s: %d whole steps (build + all %d points), warm-up steps on 1e6 points"
+                                     % (what, steps, npts)}
+    res["e2e"] = {"value": res["value"], "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    if not args.no_configs:
+        for cfg in (CFG1, CFG4):
+            v, p = config_inputs(cfg)
+            timing, _ = config_cpu(cfg, v, p)
+            res[cfg["name"]] = dict(workload=cfg["workload"], points=int(p.shape[0]), **timing)
+    return res
 
 
 def main():

@@ -289,6 +289,18 @@ class InterpolationFunction:
                                    _stream_ptr(stream)))
         return cells, wrapped
 
+    def locate_binned(self, points, stream=None):
+        """Knot-span indices (N x D int64) as the binned evaluation path
+        computes them (its own locate kernel, records decoded); mixed scalar
+        tables of dimension 1..3 only."""
+        torch = _torch()
+        lib = _lib.load()
+        pts = points.to(torch.float64).contiguous().reshape(-1, self.dim)
+        cells = torch.empty(pts.shape, dtype=torch.int64, device=pts.device)
+        _lib.check(lib.intp_locate_binned(self._h, C.c_void_p(pts.data_ptr()), pts.shape[0],
+                                          C.c_void_p(cells.data_ptr()), _stream_ptr(stream)))
+        return cells
+
     def check_range(self, points, stream=None):
         """Index of the first point outside a non-periodic axis range, or -1."""
         torch = _torch()

@@ -94,6 +94,7 @@ SIGNATURES = {
     "intp_eval_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int32, _P, C.c_int32, _P]),
     "intp_check_range": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_locate": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P]),
+    "intp_locate_binned": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_stream_synchronize": (C.c_int, [_P]),
     "intp_last_error": (C.c_char_p, []),
     "intp_launch_count": (C.c_uint64, []),

@@ -87,6 +87,29 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const uint32_t
         }
 }
 
+// Knot spans of the queries in input order, decoded from the records the
+// locate kernel wrote: the bucket in the tag's high bits, the span within the
+// bucket in its low kCellBits bits (the inverse of locate_kernel's packing).
+template <int D>
+__global__ void decode_spans_kernel(BinGeom g, int order, const uint32_t* __restrict__ in_rec, int64_t n,
+                                    int64_t* __restrict__ cells) {
+    constexpr int RW = rec_words<D>();
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < n;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t w[RW];
+        rec_load<D>(in_rec, p, w);
+        const uint32_t tag = w[RW - 1];
+        uint32_t b = tag >> kCellBits;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+            const uint32_t bc = b % static_cast<uint32_t>(g.nb[d]);
+            b /= static_cast<uint32_t>(g.nb[d]);
+            const uint32_t local = (tag >> g.shift[d]) & ((1u << g.lb[d]) - 1u);
+            cells[p * D + d] = static_cast<int64_t>((bc << g.lb[d]) | local) + order;
+        }
+    }
+}
+
 }  // namespace bin_detail
 
 namespace {
@@ -134,6 +157,26 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
 
 }  // namespace
 
+template <int D>
+cudaError_t launch_span_readout(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
+                                uint32_t* blkcount, uint32_t* in_rec, int64_t* cells, cudaStream_t s) {
+    using namespace bin_detail;
+    const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
+    auto kl = locate_kernel<D>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    const int64_t slice = (n + nblk - 1) / nblk;
+    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, blkcount);
+    note_launch();
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, int64_t{sm_count()} * 8);
+    decode_spans_kernel<D><<<static_cast<int>(blocks), 256, 0, s>>>(g, t.order, in_rec, n, cells);
+    note_launch();
+    return cudaGetLastError();
+}
+
 int bin_record_words(int dim) { return dim == 1 ? bin_detail::rec_words<1>() : bin_detail::rec_words<2>(); }
 
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
@@ -149,6 +192,36 @@ cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* co
         case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t binned_span_readout(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
+                                int64_t* cells, cudaStream_t s) {
+    if (npts <= 0) return cudaSuccess;
+    const int D = t.dim;
+    if (D > 3) return cudaErrorInvalidValue;
+    const int nblk = sm_count() * 2;
+    // the production chunk bound: a sort CTA's slice stays below kMaxSlice
+    const int64_t cap = std::min<int64_t>(npts, int64_t{nblk} * (bin_detail::kMaxSlice - 1));
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t b_m = up(static_cast<size_t>(g.nbuckets * nblk) * 4);
+    const size_t total = b_m + up(static_cast<size_t>(cap) * 4 * bin_record_words(D));
+    void* mem = nullptr;
+    cudaError_t e = cudaMallocAsync(&mem, total, s);
+    if (e != cudaSuccess) return e;
+    uint32_t* blkcount = static_cast<uint32_t*>(mem);
+    uint32_t* in_rec = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(mem) + b_m);
+    for (int64_t p0 = 0; p0 < npts && e == cudaSuccess; p0 += cap) {
+        const int64_t n = std::min(cap, npts - p0);
+        const double* c = coords + p0 * D;
+        int64_t* o = cells + p0 * D;
+        switch (D) {
+            case 1: e = launch_span_readout<1>(t, g, c, n, nblk, blkcount, in_rec, o, s); break;
+            case 2: e = launch_span_readout<2>(t, g, c, n, nblk, blkcount, in_rec, o, s); break;
+            default: e = launch_span_readout<3>(t, g, c, n, nblk, blkcount, in_rec, o, s); break;
+        }
+    }
+    const cudaError_t e2 = cudaFreeAsync(mem, s);
+    return e != cudaSuccess ? e : e2;
 }
 
 BinGeom make_bin_geom(const TableDev& t) {

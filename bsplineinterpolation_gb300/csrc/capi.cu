@@ -913,6 +913,17 @@ intp_status intp_locate(const intp_table* t, const double* coords, int64_t npts,
     return INTP_OK;
 }
 
+intp_status intp_locate_binned(const intp_table* t, const double* coords, int64_t npts, int64_t* cells,
+                               void* stream) {
+    if (!t || (npts > 0 && (!coords || !cells))) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (npts < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "npts must be >= 0");
+    if (!(t->mixed() && t->model.dim <= 3 && t->channels == 1 && t->bins.smem_buckets > 0))
+        return fail(INTP_ERR_UNSUPPORTED, "the table does not take the binned evaluation path");
+    INTP_CUDA(binned_span_readout(t->dev, t->bins, coords, npts, cells, static_cast<cudaStream_t>(stream)),
+              "binned span read-out");
+    return INTP_OK;
+}
+
 intp_status intp_stream_synchronize(void* stream) {
     INTP_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -993,30 +1004,32 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     if (dev != t->device) return fail(INTP_ERR_INVALID_ARGUMENT, "make the table's device current first");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const bool out_f32 = out_dtype == INTP_F32;
-    if (!(t->mixed() && t->model.dim <= 3 && t->bins.smem_buckets > 0)) {
-        // tables the binned path does not take evaluate with the direct
-        // kernel, which needs no scratch
-        if (npts == 0) return INTP_OK;
-        INTP_CUDA(launch_eval_direct(t->dev, t->mixed(), coords, npts, plan, out, out_f32, s), "evaluation kernel");
-        return INTP_OK;
-    }
+    // the array's address first, whatever the table: any first call on a
+    // device (npts = 0 included) does the set-up
     void* base = nullptr;
     const intp_status st = noalloc_scratch_address(dev, &base);
     if (st != INTP_OK) return st;
+    const bool bins = t->mixed() && t->model.dim <= 3 && t->channels == 1 && t->bins.smem_buckets > 0;
     // carve the fixed area: per-(bucket, CTA) counts and offsets, scan tile
     // sums, then as many query records as fit
     const int D = t->model.dim;
     const BinGeom& g = t->bins;
-    const int64_t m = g.nbuckets * kNoAllocSortBlocks;
+    const int64_t m = bins ? g.nbuckets * kNoAllocSortBlocks : 0;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
     // two records per query in flight: in input order and in bucket order
     const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D)) * 2;
-    if (fixed + 1024 * per_rec + 512 > kNoAllocScratchBytes)
+    if (bins && fixed + 1024 * per_rec + 512 > kNoAllocScratchBytes)
         return fail(INTP_ERR_INVALID_ARGUMENT,
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
                         ") for the 8 MiB scratch of the allocation-free evaluation; use intp_eval");
     if (npts == 0) return INTP_OK;
+    if (!bins || npts < kBinnedMinPoints) {
+        // the direct kernel needs no scratch: tables the binned path does not
+        // take, and batches too small to be worth binning (as intp_eval)
+        INTP_CUDA(launch_eval_direct(t->dev, t->mixed(), coords, npts, plan, out, out_f32, s), "evaluation kernel");
+        return INTP_OK;
+    }
     int64_t cap = static_cast<int64_t>((kNoAllocScratchBytes - fixed - 512) / per_rec);
     cap &= ~int64_t{63};
     unsigned char* p = static_cast<unsigned char*>(base);

@@ -41,6 +41,10 @@ cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* co
                            uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
                            uint32_t* rec, int64_t* slice, cudaStream_t s);
 int bin_record_words(int dim);
+// Knot spans (npts x D int64, device memory) of the binned path: the locate
+// kernel of the binned evaluation, its records decoded (diagnostics).
+cudaError_t binned_span_readout(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
+                                int64_t* cells, cudaStream_t s);
 cudaError_t launch_bin_eval_d12(const TableDev&, const BinGeom&, const CUtensorMap* tmap, const uint32_t* blkoffset,
                                 int nblk, int64_t slice, const uint32_t* rec, int64_t n, const DerivPlan&, void* out,
                                 bool out_f32, int grid, cudaStream_t);

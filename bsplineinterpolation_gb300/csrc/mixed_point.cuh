@@ -61,7 +61,11 @@ __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const Der
             }
         }
         float Pz[W];
-#pragma unroll
+        // a stencil above 1024 operands (4D at orders 6 and 7) keeps the
+        // axis-0 loop rolled: the same operations in the same order, with
+        // compile time bounded
+        constexpr int kUnrollI0 = W * ROWS1 * W <= 1024 ? W : 1;
+#pragma unroll kUnrollI0
         for (int i0 = 0; i0 < W; ++i0) {
             float acc = 0.0f;
 #pragma unroll

@@ -385,6 +385,10 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
                 ist = e == cudaErrorMemoryAllocation ? INTP_ERR_OUT_OF_MEMORY : INTP_ERR_CUDA;
                 msg = std::string("evaluation: ") + cudaGetErrorString(e);
             }
+            // copies already queued for earlier requests of the unit may still
+            // be writing their outputs: the requests are reported done only
+            // once the slot's stream has drained
+            cudaStreamSynchronize(st);
             for (Request* q : u.reqs) fail_request(q, ist, msg);
             return true;
         }

@@ -146,9 +146,10 @@ intp_status intp_eval_host(const intp_table* table, const double* coords_host, i
  *
  * Requirements and limits:
  *  - The table's device must be current.
- *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress), which may run the CUDA runtime's module set-up.
- *    Make that first call (npts = 0 will do) before any stream capture.
+ *  - The first call on a device, whatever its table and point count,
+ *    looks up the array's device address (cudaGetSymbolAddress), which may
+ *    run the CUDA runtime's module set-up. Make that first call (npts = 0
+ *    will do) before any stream capture.
  *  - The array is shared by every call on a device. Calls whose work
  *    overlaps on the device (several streams or host threads) race on it, so
  *    issue them on one stream. Its contents between calls do not matter:
@@ -157,8 +158,9 @@ intp_status intp_eval_host(const intp_table* table, const double* coords_host, i
  *    records in the 8 MiB is rejected with INTP_ERR_INVALID_ARGUMENT (about
  *    32k buckets, e.g. a 512^3 cubic table); use intp_eval for it.
  *  - The number of points is not limited: they are taken in chunks that fit.
- *  - Tables outside the binned path (FP64 precision, dim 4) run the direct
- *    kernel, which needs no scratch. */
+ *  - Tables outside the binned path (FP64 precision, dim 4, vector-valued
+ *    tables) and batches below 2^18 points run the direct kernel, which
+ *    needs no scratch. */
 intp_status intp_eval_noalloc(const intp_table* table, const double* coords, int64_t npts,
                               const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype,
                               void* stream);
@@ -175,6 +177,15 @@ intp_status intp_check_range(const intp_table* table, const double* coords, int6
  * Replaces BSpline::get_knot_iter (BSpline.hpp:125-157). */
 intp_status intp_locate(const intp_table* table, const double* coords, int64_t npts,
                         int64_t* cells, double* wrapped, void* stream);
+
+/* Knot-span index per point and axis (npts x dim int64, device memory) as the
+ * binned evaluation computes it: the binned path's own locate kernel runs on
+ * the points and its sort records are decoded. Mixed-precision scalar tables
+ * of dimension 1..3 only (the tables intp_eval bins); INTP_ERR_UNSUPPORTED
+ * otherwise. Diagnostics: it lets a caller check the binned path's spans
+ * against BSpline::get_knot_iter (BSpline.hpp:125-157) point for point. */
+intp_status intp_locate_binned(const intp_table* table, const double* coords, int64_t npts,
+                               int64_t* cells, void* stream);
 
 /* Waits for `stream`. */
 intp_status intp_stream_synchronize(void* stream);

@@ -13,6 +13,7 @@
 #include <BandMatrix.hpp>
 
 #include <array>
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -24,6 +25,9 @@
 namespace {
 
 thread_local std::string g_err;
+// seconds spent in the last InterpolationFunction constructor (knots, factors
+// and the control-point solve), without the driver's own mesh copy
+thread_local double g_build_seconds = 0.0;
 
 struct Handle {
     virtual ~Handle() = default;
@@ -38,6 +42,11 @@ struct Handle {
     virtual int64_t nctrl() const = 0;
     virtual void ctrl(double* out) const = 0;
     virtual int at_check(const double* c) const = 0;
+    // outputs as a user of the reference computes them: operator() for a row
+    // of all-zero orders, derivative() otherwise
+    virtual void eval_user(const double* c, int64_t n, const int* k, int nk, double* out, int nthreads) const {
+        eval_deriv(c, n, k, nk, out, nthreads);
+    }
 };
 
 template <typename F>
@@ -78,6 +87,26 @@ struct FnHandle : Handle {
                     for (std::size_t d = 0; d < D; ++d) kk[d] = (std::size_t)k[r * (int)D + (int)d];
                     out[p * nk + r] = fn.derivative(x, kk);
                 }
+            }
+        });
+    }
+    void eval_user(const double* c, int64_t n, const int* k, int nk, double* out,
+                   int nthreads) const override {
+        parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+            std::array<std::size_t, D> kk[16];
+            bool value[16];
+            for (int r = 0; r < nk && r < 16; ++r) {
+                value[r] = true;
+                for (std::size_t d = 0; d < D; ++d) {
+                    kk[r][d] = (std::size_t)k[r * (int)D + (int)d];
+                    value[r] = value[r] && kk[r][d] == 0;
+                }
+            }
+            for (int64_t p = b; p < e; ++p) {
+                std::array<double, D> x;
+                for (std::size_t d = 0; d < D; ++d) x[d] = c[p * (int64_t)D + (int64_t)d];
+                for (int r = 0; r < nk && r < 16; ++r)
+                    out[p * nk + r] = value[r] ? fn(x) : fn.derivative(x, kk[r]);
             }
         });
     }
@@ -143,7 +172,10 @@ intp::Mesh<double, D> make_mesh(const int64_t* sizes, const double* values) {
 
 template <std::size_t D, std::size_t O, typename... A>
 Handle* construct(const std::array<bool, D>& per, const intp::Mesh<double, D>& m, A... a) {
-    return new FnHandle<D, O>(intp::InterpolationFunction<double, D, O>(per, m, a...));
+    const auto t0 = std::chrono::steady_clock::now();
+    intp::InterpolationFunction<double, D, O> fn(per, m, a...);
+    g_build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return new FnHandle<D, O>(std::move(fn));
 }
 
 template <std::size_t O>
@@ -302,6 +334,12 @@ void ref_eval_deriv(void* h, const double* c, int64_t n, const int* k, int nk, d
                     int nthreads) {
     static_cast<Handle*>(h)->eval_deriv(c, n, k, nk, out, nthreads);
 }
+
+void ref_eval_user(void* h, const double* c, int64_t n, const int* k, int nk, double* out, int nthreads) {
+    static_cast<Handle*>(h)->eval_user(c, n, k, nk, out, nthreads);
+}
+
+double ref_last_build_seconds() { return g_build_seconds; }
 
 int64_t ref_num_knots(void* h, int axis) { return static_cast<Handle*>(h)->nknots(axis); }
 void ref_knots(void* h, int axis, double* out) { static_cast<Handle*>(h)->knots(axis, out); }

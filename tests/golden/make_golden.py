@@ -2,7 +2,9 @@
 
 Run where the reference source tree is available (it is read, never copied):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <reference root>
+
+(or with INTP_REFERENCE_ROOT=<reference root> in the environment).
 
 It writes two files:
 
@@ -384,8 +386,11 @@ def ref_outputs(path):
 def main():
     global REF_ROOT
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("INTP_REFERENCE_ROOT"),
+                    help="root of the reference source tree (or INTP_REFERENCE_ROOT)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("the reference root is required (--reference or INTP_REFERENCE_ROOT)")
     REF_ROOT = os.path.abspath(args.reference)
     cases = reference_tests()
     with open(os.path.join(HERE, "reference_tests.json"), "w") as fh:
@@ -396,7 +401,7 @@ def main():
     print("wrote", os.path.join(HERE, "reference_tests.json"), "and ref_outputs.npz")
 
 
-REF_ROOT = "/root/reference"
+REF_ROOT = None  # set by main()
 
 if __name__ == "__main__":
     sys.exit(main())

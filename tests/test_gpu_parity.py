@@ -136,3 +136,23 @@ def test_mixed_workload_shapes_within_1e6(meta):
         f = _table(meta, precision="mixed", refine_steps=steps)
         val = f.evaluate(torch.tensor(pts_np, device="cuda")).double().cpu().numpy()[inside, 0]
         assert norm_rel_err(val, want) < 1e-6, steps
+
+
+@pytest.mark.parametrize("meta", [m for m in INDEX if m["dim"] <= 3], ids=lambda m: m["name"])
+def test_binned_spans_match_reference(meta):
+    """The binned evaluation path locates queries with its own kernel (exact
+    integer knot keys, a 32-bit FP32 hint, the span packed into its sort
+    records). Its spans, read back from those records, equal the reference's
+    get_knot_iter (BSpline.hpp:125-157) bit for bit on every case: points on
+    knots, at both ends of non-periodic ranges, outside them, and wrapped
+    around periodic axes."""
+    name = meta["name"]
+    f = _table(meta, precision="mixed")
+    pts = torch.tensor(Z[name + "/points"], device="cuda")
+    got = f.locate_binned(pts).cpu().numpy()
+    assert np.array_equal(got, Z[name + "/cells"])
+    # the same spans in a batch large enough for intp_eval to bin it
+    reps = (1 << 18) // pts.shape[0] + 1
+    big = pts.repeat(reps, 1)
+    got = f.locate_binned(big).cpu().numpy()
+    assert np.array_equal(got, np.tile(Z[name + "/cells"], (reps, 1)))
