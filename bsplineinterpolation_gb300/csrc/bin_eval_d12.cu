@@ -10,17 +10,25 @@ cudaError_t launch_do(const TableDev& t, const BinGeom& g, const CUtensorMap* tm
                       int64_t slice, const uint32_t* rec,
                       int64_t n, const DerivPlan& plan, void* out, bool out_f32, int grid, cudaStream_t s) {
     auto k = bin_detail::eval_kernel<D, O>;
-    // the tile, and the remainders' tile when the table keeps them, + the
-    // alignment of the TMA destination
-    const size_t tile_bytes = (static_cast<size_t>(g.tile_elems) * 4 + 127) & ~size_t(127);
+    // the tile, the remainders' tile / sorted records, the records' cells and
+    // the cell counters (bin_detail::EvalSmem)
+    const size_t smem = bin_detail::EvalSmem<D, O>::kBytes;
     const bool lo = t.ctrl_lo && plan.has_deriv;
-    const size_t smem = tile_bytes * (lo ? 2 : 1) + 128;
     // static + dynamic shared memory may pass 48 KB even when the tile alone
     // does not, so the opt-in limit is set on every launch
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+    // FP32 outputs: 1, or 3 when pairs of outputs may leave as 8-byte stores
+    const int out_mode = out_f32 ? ((reinterpret_cast<uintptr_t>(out) & 7u) == 0 ? 3 : 1) : 0;
+    // a full wave: every SM holds as many evaluation CTAs as fit
+    static int per_sm = 0;
+    if (per_sm == 0 &&
+        (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, bin_detail::kBinThreads, smem) != cudaSuccess ||
+         per_sm < 1))
+        per_sm = 1;
+    grid *= per_sm;  // grid: the SM count
     CUtensorMap none{};
-    k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_f32 ? 1 : 0,
+    k<<<grid, bin_detail::kBinThreads, smem, s>>>(t, g, offsets, nblk, slice, rec, n, plan, out, out_mode,
                                                   tmap ? tmap[0] : none, tmap && lo ? tmap[1] : none,
                                                   tmap ? 1 : 0);
     note_launch();

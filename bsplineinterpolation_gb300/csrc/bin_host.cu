@@ -128,8 +128,8 @@ int sm_count() {
 
 template <int D>
 cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec, uint32_t* rec,
-                        int64_t slice, cudaStream_t s) {
+                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec, uint32_t* rank,
+                        uint32_t* rec, int64_t slice, cudaStream_t s) {
     using namespace bin_detail;
     const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
     auto kl = locate_kernel<D>;
@@ -140,7 +140,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
             e = cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, blkcount);
+    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
     note_launch();
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -150,7 +150,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    kp<<<nblk, kSortThreads, smem, s>>>(g, n, slice, in_rec, blkoffset, rec);
+    kp<<<nblk, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }
@@ -169,7 +169,7 @@ cudaError_t launch_span_readout(const TableDev& t, const BinGeom& g, const doubl
         if (e != cudaSuccess) return e;
     }
     const int64_t slice = (n + nblk - 1) / nblk;
-    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, blkcount);
+    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, nullptr, blkcount);
     note_launch();
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, int64_t{sm_count()} * 8);
     decode_spans_kernel<D><<<static_cast<int>(blocks), 256, 0, s>>>(g, t.order, in_rec, n, cells);
@@ -181,15 +181,15 @@ int bin_record_words(int dim) { return dim == 1 ? bin_detail::rec_words<1>() : b
 
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
                            uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
-                           uint32_t* rec, int64_t* slice, cudaStream_t s) {
+                           uint32_t* rank, uint32_t* rec, int64_t* slice, cudaStream_t s) {
     if (nblk < 1 || nblk > bin_detail::kMaxSortBlocks) return cudaErrorInvalidValue;
     const int64_t sl = (n + nblk - 1) / nblk;
     if (sl >= bin_detail::kMaxSlice) return cudaErrorInvalidValue;
     *slice = sl;
     switch (t.dim) {
-        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
-        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
-        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, sl, s);
+        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
+        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
+        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -240,7 +240,9 @@ BinGeom make_bin_geom(const TableDev& t) {
         // rows of the last axis are padded to a multiple of 4 floats
         stride *= d == D - 1 ? ((g.P[d] + 3) & ~3) : g.P[d];
     }
-    for (int d = 0; d < D; ++d) {
+    // the span within the bucket packs row-major, the last axis in the low
+    // bits: ordering records by it orders them as the tile lies in memory
+    for (int d = D - 1; d >= 0; --d) {
         g.shift[d] = shift;
         shift += g.lb[d];
         g.nbuckets *= g.nb[d];
@@ -260,15 +262,18 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     if (npts <= 0) return cudaSuccess;
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
-    const int64_t cap = std::min<int64_t>(chunk, npts);
     const int nblk = sm_count() * 2;  // count/scatter CTAs of kSortThreads (one pair per SM)
+    // a record names its query by its index within a sort CTA's slice
+    // (below kMaxSlice)
+    const int64_t cap = std::min<int64_t>(std::min<int64_t>(chunk, npts), int64_t{nblk} * (bin_detail::kMaxSlice - 1));
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + bin_detail::kScanTile - 1) / bin_detail::kScanTile;
     if (ntiles > bin_detail::kScanThreads * bin_detail::kScanItems) return cudaErrorInvalidValue;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t b_m = up(static_cast<size_t>(m) * 4), b_t = up(static_cast<size_t>(ntiles) * 4);
     const size_t b_r = up(static_cast<size_t>(cap) * 4 * bin_record_words(D));
-    const size_t total = b_m * 2 + b_t + b_r * 2;
+    const size_t b_k = up(static_cast<size_t>(cap) * 4);  // ranks
+    const size_t total = b_m * 2 + b_t + b_r * 2 + b_k;
     void* mem = nullptr;
     cudaError_t e = cudaMallocAsync(&mem, total, s);
     if (e != cudaSuccess) return e;
@@ -282,14 +287,16 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
     p += b_r;
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
+    p += b_r;
+    uint32_t* rank = reinterpret_cast<uint32_t*>(p);
     const int K = plan.k;
     const size_t ob = out_f32 ? 4 : 8;
-    const int grid_eval = sm_count() * 2;
+    const int grid_eval = sm_count();  // the launchers fill each SM
     for (int64_t p0 = 0; p0 < npts && e == cudaSuccess; p0 += cap) {
         const int64_t n = std::min(cap, npts - p0);
         const double* c = coords + p0 * D;
         int64_t slice = 0;
-        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rec, &slice, s);
+        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, &slice, s);
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
         e = D <= 2 ? launch_bin_eval_d12(t, g, tmap, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s)

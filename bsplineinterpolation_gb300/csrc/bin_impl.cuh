@@ -11,7 +11,8 @@
 //            one 8- or 16-byte record per query in input order, and
 //            per-(bucket, CTA) counts
 //   scan:    exclusive prefix sum over (bucket, CTA) -> first slot of each pair
-//   permute: every record moves to its pair's next slot (one vector store)
+//   permute: every record moves to its pair's first slot plus its rank in the
+//            pair (counted by locate): one vector store, no atomics
 //   eval:    CTA j takes the j-th equal slice of the sorted records, stages the
 //            tile of each bucket it meets with asynchronous copies, evaluates,
 //            writes out[index]
@@ -21,10 +22,10 @@
 // consecutive slots with a single atomic, so clustered queries neither
 // serialise on a counter nor scatter their records.
 //
-// Queries are processed in chunks of the input. A chunk is large (millions of
-// queries) so each bucket's tile is staged a few times per chunk only; its
-// output writes land in a region small enough to stay in L2 until its
-// sectors are complete.
+// Queries are processed in chunks of the input, as large as a record's
+// 20-bit slice index allows (up to 2^28 queries): each bucket's tile is staged
+// once per evaluation CTA that meets the bucket, so the more queries one sort
+// holds, the more of them share each staged tile.
 #pragma once
 
 #include <cuda.h>
@@ -41,7 +42,7 @@ namespace intp_gb300 {
 namespace bin_detail {
 
 constexpr int kBinThreads = 256;   // evaluation CTA
-constexpr int kSortThreads = 512;  // count / scatter CTA
+constexpr int kSortThreads = 768;  // count / scatter CTA (two per SM at up to 42 registers)
 
 // Exact span and FP32 local offset of one coordinate on axis a (mixed form),
 // with 32-bit span indices (binned tables have fewer than 2^31 knots per
@@ -72,7 +73,7 @@ __device__ __forceinline__ uint32_t bucket_of(const BinGeom& g, const int (&cl)[
 // order) or the query's index within its sort CTA's input slice (records in
 // bucket order).
 constexpr int kCellBits = 12;
-constexpr int kMaxSortBlocks = 1024;
+constexpr int kMaxSortBlocks = 512;
 constexpr int64_t kMaxSlice = int64_t{1} << (32 - kCellBits);
 
 template <int D>
@@ -126,13 +127,14 @@ __device__ __forceinline__ void rec_load(const uint32_t* rec, int64_t slot, uint
 //            per-bucket counts in blkcount[b * nblk + blk] (bucket-major);
 //   scan:    exclusive prefix sum over (bucket, CTA): the first slot of every
 //            pair (the first slot of bucket b is scan[b * nblk]);
-//   permute: moves every record of the slice to its pair's next slot
-//            (shared-memory cursors).
+//   permute: moves every record of the slice to its pair's first slot plus
+//            the record's rank within the pair (written by locate).
 // Shared-memory atomics are aggregated per warp (__match_any_sync), and every
 // thread runs the same number of loop trips so the match sees all lanes.
 template <int D>
-__global__ void __launch_bounds__(kSortThreads) locate_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
+__global__ void __launch_bounds__(kSortThreads, 2) locate_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
                                                              int64_t n, int64_t slice, uint32_t* __restrict__ in_rec,
+                                                             uint32_t* __restrict__ rank,
                                                              uint32_t* __restrict__ blkcount) {
     extern __shared__ uint32_t sh_count[];
     const int nblk = gridDim.x, blk = blockIdx.x;
@@ -156,48 +158,59 @@ __global__ void __launch_bounds__(kSortThreads) locate_kernel(TableDev t, BinGeo
             b = bucket_of<D>(g, cl);
             rec_store<D>(in_rec, p, u, (b << kCellBits) | cell);
         }
+        // the query's rank among its CTA's queries of the bucket: one atomic
+        // per group of lanes with the same bucket
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
-        if (valid && lane == __ffs(peers) - 1) atomicAdd(&sh_count[b], static_cast<uint32_t>(__popc(peers)));
+        const int leader = __ffs(peers) - 1;
+        uint32_t first = 0;
+        if (valid && lane == leader) first = atomicAdd(&sh_count[b], static_cast<uint32_t>(__popc(peers)));
+        first = __shfl_sync(0xFFFFFFFFu, first, leader);
+        if (valid && rank) rank[p] = first + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
     }
     __syncthreads();
     for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) blkcount[b * nblk + blk] = sh_count[b];
 }
 
+// Every record of the slice to slot = (first slot of its (bucket, CTA) pair)
+// + (its rank there, from the locate kernel): independent streaming copies,
+// four records per thread and trip with all loads in flight.
 template <int D>
-__global__ void __launch_bounds__(kSortThreads) permute_kernel(BinGeom g, int64_t n, int64_t slice,
+__global__ void __launch_bounds__(kSortThreads, 2) permute_kernel(BinGeom g, int64_t n, int64_t slice,
                                                               const uint32_t* __restrict__ in_rec,
+                                                              const uint32_t* __restrict__ rank,
                                                               const uint32_t* __restrict__ blkoffset,
                                                               uint32_t* __restrict__ rec) {
-    extern __shared__ uint32_t sh_cursor[];
+    extern __shared__ uint32_t sh_first[];
     constexpr int RW = rec_words<D>();
+    constexpr int U = 4;
     const int nblk = gridDim.x, blk = blockIdx.x;
-    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_cursor[b] = blkoffset[b * nblk + blk];
+    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_first[b] = __ldg(blkoffset + b * nblk + blk);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const uint32_t lt_mask = (1u << lane) - 1u;
     const int64_t p0 = blk * slice, p1 = (p0 + slice < n) ? p0 + slice : n;
     constexpr uint32_t cell_mask = (1u << kCellBits) - 1u;
-    for (int64_t base = p0; base < p1; base += blockDim.x) {
-        const int64_t p = base + threadIdx.x;
-        const bool valid = p < p1;
-        uint32_t w[RW];
-        uint32_t b = 0xFFFFFFFFu;
-        if (valid) {
-            rec_load<D>(in_rec, p, w);
-            b = w[RW - 1] >> kCellBits;
+    for (int64_t base = p0; base < p1; base += U * static_cast<int64_t>(blockDim.x)) {
+        uint32_t w[U][RW];
+        uint32_t rk[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+            const int64_t p = base + j * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+            if (p < p1) {
+                rec_load<D>(in_rec, p, w[j]);
+                rk[j] = __ldg(rank + p);
+            }
         }
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
-        const int leader = __ffs(peers) - 1;
-        uint32_t first = 0;
-        if (valid && lane == leader) first = atomicAdd(&sh_cursor[b], static_cast<uint32_t>(__popc(peers)));
-        first = __shfl_sync(0xFFFFFFFFu, first, leader);
-        if (valid) {
-            const uint32_t slot = first + static_cast<uint32_t>(__popc(peers & lt_mask));
-            w[RW - 1] = (static_cast<uint32_t>(p - p0) << kCellBits) | (w[RW - 1] & cell_mask);
-            if constexpr (D == 1)
-                reinterpret_cast<uint2*>(rec)[slot] = make_uint2(w[0], w[1]);
-            else
-                reinterpret_cast<uint4*>(rec)[slot] = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+            const int64_t p = base + j * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+            if (p < p1) {
+                const uint32_t tag = w[j][RW - 1];
+                const uint32_t slot = sh_first[tag >> kCellBits] + rk[j];
+                w[j][RW - 1] = (static_cast<uint32_t>(p - p0) << kCellBits) | (tag & cell_mask);
+                if constexpr (D == 1)
+                    reinterpret_cast<uint2*>(rec)[slot] = make_uint2(w[j][0], w[j][1]);
+                else
+                    reinterpret_cast<uint4*>(rec)[slot] = make_uint4(w[j][0], w[j][1], w[j][2], w[j][3]);
+            }
         }
     }
 }
@@ -288,91 +301,159 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
     }
 }
 
-// Evaluation of the records of one bucket [r, end) against its staged tile.
-// seg[j] is the first slot of the bucket's records from sort CTA j (nblk
-// entries); a record's query index is j * slice + its local index.
-// LEAN: a DerivPlan::simple plan.
+// Shared-memory plan of the evaluation CTA for one (D, O): the control
+// points' tile; a second region of the same size that holds the remainders'
+// tile while a bucket is staged and then a piece of the bucket's records
+// sorted by cell; the cell of every sorted record; and the per-cell counters
+// of the piece (two 16-bit counts per word).
+template <int D, int O>
+struct EvalSmem {
+    using TS = TileShape<D, O>;
+    static constexpr int kRecBytes = rec_words<D>() * 4;
+    static constexpr int kTileBytes = (TS::elems() * 4 + 127) & ~127;
+    static constexpr int kPiece = (kTileBytes / kRecBytes) / kBinThreads * kBinThreads;
+    static constexpr int kPerThread = kPiece / kBinThreads;
+    static constexpr int kCellofBytes = (kPiece * 2 + 127) & ~127;
+    static constexpr int kCountWords = (1 << kCellBits) / 2;
+    static constexpr int kBytes = 2 * kTileBytes + kCellofBytes + kCountWords * 4 + 128;
+    static_assert(kPiece >= kBinThreads && kPiece < 65536, "piece of the in-CTA sort");
+};
+
+// Exclusive scan, in place, of the 2^kCellBits 16-bit cell counts packed two
+// per word (cell 2w in the low half of word w): afterwards each half holds
+// the first sorted position of its cell's records in the piece (< 2^16).
+__device__ __forceinline__ void scan_cell_counts(uint32_t* cnt, uint32_t* warp_sums) {
+    constexpr int kWords = (1 << kCellBits) / 2;
+    constexpr int kPer = kWords / kBinThreads;  // words per thread
+    static_assert(kPer * kBinThreads == kWords && kPer % 4 == 0, "cell counter layout");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t v[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; j += 4) {
+        const uint4 q = reinterpret_cast<const uint4*>(cnt + tid * kPer)[j / 4];
+        v[j] = q.x;
+        v[j + 1] = q.y;
+        v[j + 2] = q.z;
+        v[j + 3] = q.w;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) sum += (v[j] & 0xFFFFu) + (v[j] >> 16);
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t run = incl - sum;
+    for (int w = 0; w < warp; ++w) run += warp_sums[w];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const uint32_t lo = v[j] & 0xFFFFu, hi = v[j] >> 16;
+        v[j] = run | ((run + lo) << 16);
+        run += lo + hi;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; j += 4)
+        reinterpret_cast<uint4*>(cnt + tid * kPer)[j / 4] = make_uint4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+}
+
+// Outputs of one sorted record: w = (u_0 .. u_{D-1} as FP32, query index),
+// cell = its span within the bucket (packed as in the tag).
 template <int D, int O, bool LEAN, class TS>
-__device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
-                                             const float* tile, const int (&org)[D], float cbase,
-                                             const uint32_t* seg, int nblk, int64_t slice,
-                                             const uint32_t* __restrict__ rec, int64_t r, int64_t end,
-                                             void* __restrict__ out, int out_f32) {
+__device__ __forceinline__ void eval_record(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
+                                            const float* tile, const int (&org)[D], float cbase,
+                                            const uint32_t (&w)[rec_words<D>()], uint32_t cell,
+                                            void* __restrict__ out, int out_f32) {
     constexpr int RW = rec_words<D>();
     constexpr int W = O + 1;
     const int K = plan.k;
-    // records are software-pipelined: the next one loads while the current
-    // one is evaluated
-    uint32_t nx[RW];
-    int64_t rr = r + threadIdx.x;
-    if (rr < end) rec_load<D>(rec, rr, nx);
-    for (; rr < end; rr += blockDim.x) {
-        uint32_t cur[RW];
+    const int64_t idx = static_cast<int64_t>(w[RW - 1]);
+    int tb = 0;
+    int cl[D];
 #pragma unroll
-        for (int j = 0; j < RW; ++j) cur[j] = nx[j];
-        const int64_t nr = rr + blockDim.x;
-        if (nr < end) rec_load<D>(rec, nr, nx);
-        const uint32_t tag = cur[RW - 1];
-        // sort CTA of the record: the last segment starting at or before rr
-        int lo = 0, hi = nblk;
-        const uint32_t slot = static_cast<uint32_t>(rr);
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (seg[mid] <= slot)
-                lo = mid;
+    for (int d = 0; d < D; ++d) {
+        cl[d] = static_cast<int>((cell >> g.shift[d]) & ((1u << bucket_log2(D, d)) - 1u));
+        tb += cl[d] * TS::S(d);
+    }
+    const float* tl = tile + tb;
+    // the query's reference: its central control point
+    int tref = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) tref += ref_tap<O>() * TS::S(d);
+    const float cref = tl[tref];
+    const int64_t o0 = idx * K;
+    // value and one derivative (the common request) leave as one 8-byte store
+    float first = 0.0f;
+    const bool pair = out_f32 == 3 && K == 2;
+    auto emit = [out, out_f32, o0, pair, &first](int k, float v) {
+        if (pair) {
+            if (k == 0)
+                first = v;
             else
-                hi = mid;
+                reinterpret_cast<float2*>(static_cast<float*>(out) + o0)[0] = make_float2(first, v);
+        } else if (out_f32) {
+            static_cast<float*>(out)[o0 + k] = v;
+        } else {
+            static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
         }
-        const int64_t idx = static_cast<int64_t>(lo) * slice + (tag >> kCellBits);
-        int tb = 0;
-        int cl[D];
+    };
+    if constexpr (LEAN) {
+        float u[D];
+        int c[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            cl[d] = static_cast<int>((tag >> g.shift[d]) & ((1u << bucket_log2(D, d)) - 1u));
-            tb += cl[d] * TS::S(d);
+            u[d] = __uint_as_float(w[d]);
+            c[d] = org[d] + cl[d] + O;
         }
-        const float* tl = tile + tb;
-        // the query's reference: its central control point
-        int tref = 0;
+        lean_point<D, O, TS>(t, c, u, tl, plan, cref, cbase, emit);
+    } else {
+        float u[D];
+        int64_t c[D];
+        float base[D][W];
 #pragma unroll
-        for (int d = 0; d < D; ++d) tref += ref_tap<O>() * TS::S(d);
-        const float cref = tl[tref];
-        const int64_t o0 = idx * K;
-        auto emit = [out, out_f32, o0](int k, float v) {
-            if (out_f32)
-                static_cast<float*>(out)[o0 + k] = v;
-            else
-                static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
-        };
-        if constexpr (LEAN) {
-            float u[D];
-            int c[D];
+        for (int d = 0; d < D; ++d) {
+            u[d] = __uint_as_float(w[d]);
+            c[d] = org[d] + cl[d] + O;
+            axis_weights32<O>(t.ax[d], c[d], u[d], 0, base[d]);
+        }
+        mixed_point_outputs<D, O>(
+            t, plan, c, u, base, cref, cbase,
+            [tl, cref](const int (&ix)[D]) {
+                int off = 0;
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                u[d] = __uint_as_float(cur[d]);
-                c[d] = org[d] + cl[d] + O;
-            }
-            lean_point<D, O, TS>(t, c, u, tl, plan, cref, cbase, emit);
+                for (int d = 0; d < D; ++d) off += ix[d] * TS::S(d);
+                return tl[off] - cref;
+            },
+            emit);
+    }
+}
+
+// Evaluation of the n records of a piece, in cell order (sorted positions
+// tid, tid + kBinThreads, ...: the lanes of a warp read the same or
+// neighbouring cells of the tile).
+template <int D, int O, bool LEAN, class TS>
+__device__ __forceinline__ void eval_sorted(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
+                                            const float* tile, const int (&org)[D], float cbase,
+                                            const uint32_t* sbuf, const uint16_t* cellof, int n,
+                                            void* __restrict__ out, int out_f32) {
+    constexpr int RW = rec_words<D>();
+    for (int q = threadIdx.x; q < n; q += kBinThreads) {
+        uint32_t w[RW];
+        if constexpr (RW == 2) {
+            const uint2 v = reinterpret_cast<const uint2*>(sbuf)[q];
+            w[0] = v.x;
+            w[1] = v.y;
         } else {
-            float u[D];
-            int64_t c[D];
-            float base[D][W];
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                u[d] = __uint_as_float(cur[d]);
-                c[d] = org[d] + cl[d] + O;
-                axis_weights32<O>(t.ax[d], c[d], u[d], 0, base[d]);
-            }
-            mixed_point_outputs<D, O>(
-                t, plan, c, u, base, cref, cbase,
-                [tl, cref](const int (&ix)[D]) {
-                    int off = 0;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) off += ix[d] * TS::S(d);
-                    return tl[off] - cref;
-                },
-                emit);
+            const uint4 v = reinterpret_cast<const uint4*>(sbuf)[q];
+            w[0] = v.x;
+            w[1] = v.y;
+            w[2] = v.z;
+            w[3] = v.w;
         }
+        eval_record<D, O, LEAN, TS>(t, g, plan, tile, org, cbase, w, cellof[q], out, out_f32);
     }
 }
 
@@ -380,27 +461,40 @@ __device__ __forceinline__ void eval_records(const TableDev& t, const BinGeom& g
 // plans, table-driven weights at clamped or non-uniform spans) stays out of
 // the lean path's allocation.
 template <int D, int O, class TS>
-__device__ __noinline__ void eval_records_general(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
-                                                  const float* tile, const int (&org)[D], float cbase,
-                                                  const uint32_t* seg, int nblk, int64_t slice,
-                                                  const uint32_t* __restrict__ rec, int64_t r, int64_t end,
-                                                  void* __restrict__ out, int out_f32) {
-    eval_records<D, O, false, TS>(t, g, plan, tile, org, cbase, seg, nblk, slice, rec, r, end, out, out_f32);
+__device__ __noinline__ void eval_sorted_general(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
+                                                 const float* tile, const int (&org)[D], float cbase,
+                                                 const uint32_t* sbuf, const uint16_t* cellof, int n,
+                                                 void* __restrict__ out, int out_f32) {
+    eval_sorted<D, O, false, TS>(t, g, plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
 }
 
+// Evaluation CTA. CTA j takes the j-th equal slice of the records in bucket
+// order. For each bucket it meets it stages the bucket's tile (one TMA box,
+// or element copies where the tile wraps around a periodic axis), then takes
+// the bucket's records in pieces of kPiece: each piece is counting-sorted by
+// cell in shared memory (16-bit counters, warp-aggregated atomics) and then
+// evaluated in cell order. The cell packs row-major (last axis lowest), so
+// lanes with neighbouring sorted records read neighbouring tile words.
 template <int D, int O>
-__global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeom g, const uint32_t* __restrict__ blkoffset,
+__global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeom g, const uint32_t* __restrict__ blkoffset,
                                                            int nblk, int64_t slice, const uint32_t* __restrict__ rec,
                                                            int64_t nrec, DerivPlan plan, void* __restrict__ out,
                                                            int out_f32, const __grid_constant__ CUtensorMap tmap,
                                                            const __grid_constant__ CUtensorMap tmap_lo,
                                                            int use_tma) {
     using TS = TileShape<D, O>;
+    using SM = EvalSmem<D, O>;
+    constexpr int RW = rec_words<D>();
+    constexpr int RPT = SM::kPerThread;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    // 128-byte aligned tiles (TMA destinations): the control points, then
-    // their remainders when the table keeps them
-    float* tile = reinterpret_cast<float*>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
-    float* tile_lo = tile + tile_lo_offset<TS>();
+    // 128-byte aligned regions: the tile (a TMA destination), the remainders'
+    // tile / sorted records, the cells of the sorted records, the counters
+    unsigned char* sm = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    float* tile = reinterpret_cast<float*>(sm);
+    float* tile_lo = reinterpret_cast<float*>(sm + SM::kTileBytes);
+    uint32_t* sbuf = reinterpret_cast<uint32_t*>(sm + SM::kTileBytes);
+    uint16_t* cellof = reinterpret_cast<uint16_t*>(sm + 2 * SM::kTileBytes);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(sm + 2 * SM::kTileBytes + SM::kCellofBytes);
     // remainders staged for derivative requests only (as in the direct kernel)
     const float* __restrict__ cl = plan.has_deriv ? t.ctrl_lo : nullptr;
     __shared__ __align__(8) uint64_t sh_bar;
@@ -409,11 +503,14 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
     __shared__ TableDev sh_t;      // passed by reference to the out-of-line path
     __shared__ int sh_last[TS::P(D - 1)];                          // last-axis control-point indices
     __shared__ int64_t sh_outer[D > 1 ? D - 1 : 1][D > 1 ? TS::P(0) : 1];  // outer-axis offsets
-    __shared__ uint32_t sh_seg[kMaxSortBlocks];                    // the bucket's per-CTA first slots
+    __shared__ uint32_t sh_seg[kMaxSortBlocks];                    // the bucket's per-sort-CTA first slots
+    __shared__ uint32_t sh_warp[kBinThreads / 32];
     const float* __restrict__ cp = static_cast<const float*>(t.ctrl);
     const int64_t r0 = nrec * blockIdx.x / gridDim.x, r1 = nrec * (blockIdx.x + 1) / gridDim.x;
     if (r0 >= r1) return;
-    if (threadIdx.x == 0) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    if (tid == 0) {
         sh_plan = plan;
         sh_t = t;
         mbar_init(&sh_bar, 1);
@@ -450,8 +547,8 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
             }
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < nblk; j += kBinThreads) sh_seg[j] = __ldg(blkoffset + b * nblk + j);
-        if (threadIdx.x == 0 && cl) {
+        for (int j = tid; j < nblk; j += kBinThreads) sh_seg[j] = __ldg(blkoffset + b * nblk + j);
+        if (tid == 0 && cl) {
             // the operands' base: the control point at the tile's centre
             // (clamped at the end of a non-periodic axis, as in the direct
             // kernel)
@@ -467,7 +564,7 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
         for (int d = 0; d < D; ++d)
             if (t.ax[d].periodic && org[d] + TS::P(d) > t.ax[d].n) tma = false;
         if (tma) {
-            if (threadIdx.x == 0) {
+            if (tid == 0) {
                 fence_async_smem();  // the tiles' earlier generic-proxy accesses before the async write
                 mbar_expect_tx(&sh_bar, static_cast<uint32_t>(TS::elems() * 4 * (cl ? 2 : 1)));
                 if constexpr (D == 3) tma_load_3d(tile, &tmap, org[2], org[1], org[0], &sh_bar);
@@ -486,18 +583,18 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
         } else {
             // per-axis global offsets of the tile positions (periodic wrap,
             // clamp at the end of a non-periodic axis)
-            for (int i = threadIdx.x; i < PL; i += kBinThreads) sh_last[i] = tile_index(t.ax[D - 1], org[D - 1] + i);
+            for (int i = tid; i < PL; i += kBinThreads) sh_last[i] = tile_index(t.ax[D - 1], org[D - 1] + i);
             if constexpr (D >= 2) {
-                for (int i = threadIdx.x; i < TS::P(0); i += kBinThreads)
+                for (int i = tid; i < TS::P(0); i += kBinThreads)
                     sh_outer[0][i] = static_cast<int64_t>(tile_index(t.ax[0], org[0] + i)) * t.ax[0].stride;
             }
             if constexpr (D >= 3) {
-                for (int i = threadIdx.x; i < TS::P(1); i += kBinThreads)
+                for (int i = tid; i < TS::P(1); i += kBinThreads)
                     sh_outer[1][i] = static_cast<int64_t>(tile_index(t.ax[1], org[1] + i)) * t.ax[1].stride;
             }
             __syncthreads();
             // asynchronous element copies, all in flight at once
-            for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) {
+            for (int e = tid; e < TS::elems(); e += kBinThreads) {
                 int rem = e;
                 const int il = rem % PLP;
                 rem /= PLP;
@@ -517,19 +614,92 @@ __global__ void __launch_bounds__(kBinThreads, 2) eval_kernel(TableDev t, BinGeo
         __syncthreads();
         // operands, once per tile element: the stored FP32 control point, or
         // with remainders (ctrl - cbase) + ctrl_lo; each query then reads them
-        // relative to its own central tap
+        // relative to its own central tap. The remainders' region is free
+        // afterwards: it holds the sorted records of each piece.
         float cbase = 0.0f;
         if (cl) {
             cbase = sh_cbase;
-            for (int e = threadIdx.x; e < TS::elems(); e += kBinThreads) tile[e] = (tile[e] - cbase) + tile_lo[e];
+            for (int e = tid; e < TS::elems(); e += kBinThreads) tile[e] = (tile[e] - cbase) + tile_lo[e];
+        }
+        int seg = 0;  // sort CTA of the thread's current record
+        for (int64_t p0 = r; p0 < end; p0 += SM::kPiece) {
+            const int n = static_cast<int>(end - p0 < SM::kPiece ? end - p0 : SM::kPiece);
+            for (int wd = tid * 4; wd < SM::kCountWords; wd += kBinThreads * 4)
+                *reinterpret_cast<uint4*>(cnt + wd) = make_uint4(0u, 0u, 0u, 0u);
+            __syncthreads();
+            // this thread's records: slots p0 + tid * RPT + i, in order. Their
+            // tags first (all loads in flight); the whole records are read
+            // again when they are placed (from L1: the tag's sector holds
+            // the record)
+            uint32_t key[RPT];   // cell | rank << 16
+            uint32_t qidx[RPT];  // query index within the chunk
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int li = tid * RPT + i;
+                qidx[i] = li < n ? __ldg(rec + (p0 + li) * RW + (RW - 1)) : 0u;
+            }
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int li = tid * RPT + i;
+                const bool valid = li < n;
+                uint32_t cell = 0xFFFFFFFFu;
+                if (valid) {
+                    const uint32_t tag = qidx[i];
+                    cell = tag & ((1u << kCellBits) - 1u);
+                    // the record's sort CTA: the last segment starting at or
+                    // before its slot (binary search once, then forward steps)
+                    const uint32_t slot = static_cast<uint32_t>(p0 + li);
+                    if (i == 0) {
+                        int a = 0, z = nblk;
+                        while (z - a > 1) {
+                            const int mid = (a + z) >> 1;
+                            if (sh_seg[mid] <= slot)
+                                a = mid;
+                            else
+                                z = mid;
+                        }
+                        seg = a;
+                    }
+                    while (seg + 1 < nblk && sh_seg[seg + 1] <= slot) ++seg;
+                    qidx[i] = static_cast<uint32_t>(static_cast<int64_t>(seg) * slice + (tag >> kCellBits));
+                }
+                // rank within the cell: one atomic per group of lanes with the
+                // same cell
+                const uint32_t peers = __match_any_sync(0xFFFFFFFFu, cell);
+                const int leader = __ffs(peers) - 1;
+                const uint32_t sh = (cell & 1u) * 16u;
+                uint32_t old = 0;
+                if (valid && lane == leader) old = atomicAdd(cnt + (cell >> 1), static_cast<uint32_t>(__popc(peers)) << sh);
+                old = __shfl_sync(0xFFFFFFFFu, old, leader);
+                const uint32_t rank = ((old >> sh) & 0xFFFFu) + static_cast<uint32_t>(__popc(peers & lt_mask));
+                key[i] = (cell & 0xFFFFu) | (rank << 16);
+            }
+            __syncthreads();
+            scan_cell_counts(cnt, sh_warp);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int li = tid * RPT + i;
+                if (li < n) {
+                    uint32_t w[RW];
+                    rec_load<D>(rec, p0 + li, w);
+                    w[RW - 1] = qidx[i];
+                    const uint32_t cell = key[i] & 0xFFFFu;
+                    const uint32_t q = ((cnt[cell >> 1] >> ((cell & 1u) * 16u)) & 0xFFFFu) + (key[i] >> 16);
+                    if constexpr (RW == 2)
+                        reinterpret_cast<uint2*>(sbuf)[q] = make_uint2(w[0], w[1]);
+                    else
+                        reinterpret_cast<uint4*>(sbuf)[q] = make_uint4(w[0], w[1], w[2], w[3]);
+                    cellof[q] = static_cast<uint16_t>(cell);
+                }
+            }
+            __syncthreads();
+            if (sh_plan.simple)
+                eval_sorted<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
+            else
+                eval_sorted_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
             __syncthreads();
         }
-        if (sh_plan.simple)
-            eval_records<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cbase, sh_seg, nblk, slice, rec, r, end, out,
-                                         out_f32);
-        else
-            eval_records_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cbase, sh_seg, nblk, slice, rec, r, end, out,
-                                           out_f32);
         r = end;
     }
 }

@@ -25,8 +25,11 @@ namespace {
 
 std::atomic<unsigned long long> g_launches{0};
 
-// binned evaluation: queries per chunk, smallest batch worth binning
-constexpr int64_t kDefaultChunk = int64_t{1} << 24;
+// binned evaluation: queries per chunk (one sort of up to 2^28 queries: each
+// bucket's tile is staged once per evaluation CTA that meets the bucket, and
+// more queries per sort means more of them per staged tile), smallest batch
+// worth binning
+constexpr int64_t kDefaultChunk = int64_t{1} << 28;
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
 // INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
@@ -36,6 +39,13 @@ int eval_mode() {
     if (std::strcmp(v, "direct") == 0) return 1;
     if (std::strcmp(v, "binned") == 0) return 2;
     return 0;
+}
+
+// INTP_GB300_RESIDUAL = passes: the per-axis residual passes for 3D tables
+// too (the fused kernel is the default; both give the same bits)
+bool fused_residual_enabled() {
+    const char* v = std::getenv("INTP_GB300_RESIDUAL");
+    return !(v && std::strcmp(v, "passes") == 0);
 }
 
 int64_t eval_chunk() {
@@ -279,6 +289,31 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
     return cudaSuccess;
 }
 
+// The correction solve of one refinement step and the update of (c, lo):
+// the last axis pass (axis 0, strided when D > 1) adds its solution to the
+// control points in its back sweep; a 1D table solves, then corrects.
+cudaError_t correction_solve(intp_table* t, float* corr, float* c, bool has_lo, cudaStream_t s) {
+    const int D = t->model.dim;
+    if (D == 1) {
+        cudaError_t e = solve_f32_all(t, corr, s);
+        if (e == cudaSuccess) e = launch_correct(c, t->ctrl_lo, corr, t->values(), has_lo, s);
+        return e;
+    }
+    for (int a = D - 1; a >= 1; --a) {
+        const LineGeom g = line_geom(t, a);
+        const AxisFactorDev& f = t->fac[a];
+        const LineFactor& lf = t->model.axis[a].factor;
+        cudaError_t e = launch_line_solve_f32(corr, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
+                                              f.dinvf, f.bottomf, f.rightf, s);
+        if (e != cudaSuccess) return e;
+    }
+    const LineGeom g = line_geom(t, 0);
+    const AxisFactorDev& f = t->fac[0];
+    const LineFactor& lf = t->model.axis[0].factor;
+    return launch_line_solve_f32_correct(corr, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
+                                         f.dinvf, f.bottomf, f.rightf, c, t->ctrl_lo, has_lo, s);
+}
+
 cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
     for (int a = t->model.dim - 1; a >= 0; --a) {
         const LineGeom g = line_geom(t, a);
@@ -320,9 +355,25 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
         float* ping[2][2] = {{b + 2 * N, b + 3 * N}, {b + 4 * N, b + 5 * N}};
         INTP_CUDA(launch_shift_copy_f64_f32(values_dev, fhi, flo, c, sd, s), "shift copy");
         INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
+        // 3D tables: all residual passes in one launch (the same arithmetic)
+        int n3[3] = {}, band3[3] = {}, per3[3] = {};
+        const float2* val3[3] = {};
+        for (int d = 0; d < 3 && d < m.dim; ++d) {
+            n3[d] = static_cast<int>(m.axis[d].n);
+            band3[d] = t->fac[d].band;
+            per3[d] = m.axis[d].periodic ? 1 : 0;
+            val3[d] = t->fac[d].sval;
+        }
+        const bool fused = m.dim == 3 && fused_residual_enabled() && residual3d_supported(n3, band3, t->channels);
         for (int it = 0; it < steps; ++it) {
             // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass
             const float *ih = c, *il = it > 0 ? t->ctrl_lo : nullptr;
+            if (fused) {
+                INTP_CUDA(launch_residual3d(ih, il, fhi, flo, corr, n3, band3, per3, val3, t->channels, s),
+                          "residual");
+                INTP_CUDA(correction_solve(t, corr, c, it > 0, s), "line solve (correction)");
+                continue;
+            }
             int pp = 0;
             for (int a = m.dim - 1; a >= 0; --a) {
                 const LineGeom g = line_geom(t, a);
@@ -336,8 +387,7 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
                 il = ping[pp][1];
                 pp ^= 1;
             }
-            INTP_CUDA(solve_f32_all(t, corr, s), "line solve (correction)");
-            INTP_CUDA(launch_correct(c, t->ctrl_lo, corr, N, it > 0, s), "correction");
+            INTP_CUDA(correction_solve(t, corr, c, it > 0, s), "line solve (correction)");
         }
     }
     t->has_ctrl = true;
@@ -1017,8 +1067,9 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     const int64_t m = bins ? g.nbuckets * kNoAllocSortBlocks : 0;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    // two records per query in flight: in input order and in bucket order
-    const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D)) * 2;
+    // per query: two records (in input order and in bucket order) and its
+    // rank within its (bucket, sort CTA) pair
+    const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D)) * 2 + 4;
     if (bins && fixed + 1024 * per_rec + 512 > kNoAllocScratchBytes)
         return fail(INTP_ERR_INVALID_ARGUMENT,
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
@@ -1039,9 +1090,12 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     p += up(static_cast<size_t>(m) * 4);
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += up(static_cast<size_t>((m + 4095) / 4096) * 4);
+    const size_t rec_bytes = static_cast<size_t>(cap) * 4 * bin_record_words(D);
     uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
-    p += up(static_cast<size_t>(cap) * per_rec / 2);
+    p += up(rec_bytes);
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
+    p += up(rec_bytes);
+    uint32_t* rank = reinterpret_cast<uint32_t*>(p);
     // every word the kernels read is written earlier in the same chunk (counts
     // by the locate kernel, offsets by the scan, records by locate and
     // permute), so nothing in the area has to be cleared between calls
@@ -1052,14 +1106,14 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
         const int64_t n = std::min(cap, npts - p0);
         int64_t slice = 0;
         INTP_CUDA(bin_sort_chunk(t->dev, g, coords + p0 * D, n, kNoAllocSortBlocks, blkcount, blkoffset, tile_sum,
-                                 in_rec, rec, &slice, s),
+                                 in_rec, rank, rec, &slice, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
         const CUtensorMap* tm = t->has_tile_map ? t->tile_map : nullptr;
         INTP_CUDA(D <= 2 ? launch_bin_eval_d12(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
-                                               out_f32, sms * 2, s)
+                                               out_f32, sms, s)
                          : launch_bin_eval_d3(t->dev, g, tm, blkoffset, kNoAllocSortBlocks, slice, rec, n, plan, o,
-                                              out_f32, sms * 2, s),
+                                              out_f32, sms, s),
                   "binned evaluation");
     }
     return INTP_OK;

@@ -60,7 +60,7 @@ struct BinGeom {
     int32_t lb[kDevMaxDim];
     int32_t nb[kDevMaxDim];
     int32_t P[kDevMaxDim];
-    int32_t shift[kDevMaxDim];   // bit offset of l_d & (B_d - 1) in the packed span
+    int32_t shift[kDevMaxDim];   // bit offset of l_d & (B_d - 1) in the packed span (row-major: last axis lowest)
     int32_t tstride[kDevMaxDim];
     int64_t nbuckets;
     int32_t tile_elems;

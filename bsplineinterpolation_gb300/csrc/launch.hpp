@@ -35,12 +35,15 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
 // One chunk's counting sort by bucket into caller-provided scratch: blkcount
 // and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096);
 // in_rec and rec hold n records of bin_record_words(D) words each (queries
-// in input order, then in bucket order). Needs n <= nblk * 2^20. Returns the
+// in input order, then in bucket order), rank n words (each query's rank
+// within its (bucket, sort CTA) pair). Needs n <= nblk * 2^20. Returns the
 // slice of input queries each sort CTA took (for the evaluation).
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
                            uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
-                           uint32_t* rec, int64_t* slice, cudaStream_t s);
+                           uint32_t* rank, uint32_t* rec, int64_t* slice, cudaStream_t s);
 int bin_record_words(int dim);
+// (launch_bin_eval_*: `grid` is the SM count; the launchers place as many
+// evaluation CTAs per SM as fit.)
 // Knot spans (npts x D int64, device memory) of the binned path: the locate
 // kernel of the binned evaluation, its records decoded (diagnostics).
 cudaError_t binned_span_readout(const TableDev& t, const BinGeom& g, const double* coords, int64_t npts,
@@ -86,6 +89,21 @@ cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_
 cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
                                  const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
                                  int band, bool periodic, const float2* val, cudaStream_t s);
+// All residual passes of a 3D table in one launch (residual3d.cu):
+// r = rhs - (A_0 x A_1 x A_2) (c_hi + c_lo), bit-identical to the three
+// launch_residual_pass calls (axis 2, 1, then 0). n, band, periodic, val per
+// axis; c_lo may be null; `channels` blocks of prod(n) values.
+bool residual3d_supported(const int* n, const int* band, int channels);
+cudaError_t launch_residual3d(const float* c_hi, const float* c_lo, const float* rhs_hi, const float* rhs_lo, float* r,
+                              const int* n, const int* band, const int* periodic, const float2* const* val,
+                              int channels, cudaStream_t s);
+// The refinement's last correction pass along a strided axis (S > 1): the
+// FP32 line solve of corr whose back sweep adds each solution value to
+// (c, lo) as a double-float (the correction kernel's update, fused).
+cudaError_t launch_line_solve_f32_correct(float* corr, int64_t n, int64_t S, int64_t nlines, int p, int q,
+                                          bool cyclic, const float* lower, const float* upper, const float* dinv,
+                                          const float* bottom, const float* right, float* c, float* lo, bool has_lo,
+                                          cudaStream_t s);
 // (c, lo) += corr in double-float (lo read as 0 unless has_lo).
 cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait

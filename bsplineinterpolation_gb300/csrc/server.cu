@@ -51,9 +51,9 @@ constexpr int kMaxSlots = 64;
 constexpr uint64_t kDefaultBudget = uint64_t{150} << 30;
 constexpr int64_t kDefaultMaxBatchPoints = int64_t{1} << 24;
 // transient bytes of the binned evaluation (batches of at least
-// kBinnedPoints queries): sort records per query plus an allowance for the
-// per-bucket bookkeeping
-constexpr size_t kEvalScratchPerPoint = 20;
+// kBinnedPoints queries): per query two 16-byte sort records and a 4-byte
+// rank, plus an allowance for the per-bucket bookkeeping
+constexpr size_t kEvalScratchPerPoint = 36;
 constexpr size_t kEvalScratchFixed = size_t{16} << 20;
 constexpr int64_t kBinnedPoints = int64_t{1} << 18;
 
