@@ -179,4 +179,24 @@ __device__ __forceinline__ void axis_weights32(const AxisDev& a, int64_t c, floa
     }
 }
 
+// Weights of the precise mixed path (mixed_point.cuh precise_point_outputs):
+// value weights as axis_weights32; derivative weights on uniform interior
+// spans from the Cox-de Boor recursion on unit knots (uniform_basis, a
+// sequence of convex combinations) followed by the transposed differencing,
+// instead of the monomial (Horner) form, whose coefficients grow and
+// alternate in sign with the degree: at order 7 the Horner second-derivative
+// weights carry errors of several FP32 ulps of the largest weight. On
+// uniform knots every differencing factor k' / (t_{a+k'} - t_a) is 1/dx.
+template <int O>
+__device__ __forceinline__ void axis_weights32_precise(const AxisDev& a, int64_t c, float u, int k,
+                                                       float (&w)[O + 1]) {
+    if (k == 0 || !(a.uniform && c >= a.int_lo && c <= a.int_hi)) {
+        axis_weights32<O>(a, c, u, k, w);
+        return;
+    }
+    uniform_basis<O>(u * a.inv_dxf, O - k, w);
+    const float inv = a.inv_dxf;
+    transpose_difference<O>(k, w, [inv](int, int) { return inv; });
+}
+
 }  // namespace intp_gb300

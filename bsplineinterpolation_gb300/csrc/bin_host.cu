@@ -140,7 +140,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
             e = cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
+    kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
     note_launch();
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -150,7 +150,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    kp<<<nblk, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
+    kp<<<nblk * kPermuteParts, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }
@@ -169,7 +169,7 @@ cudaError_t launch_span_readout(const TableDev& t, const BinGeom& g, const doubl
         if (e != cudaSuccess) return e;
     }
     const int64_t slice = (n + nblk - 1) / nblk;
-    kl<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, in_rec, nullptr, blkcount);
+    kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, nullptr, blkcount);
     note_launch();
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, int64_t{sm_count()} * 8);
     decode_spans_kernel<D><<<static_cast<int>(blocks), 256, 0, s>>>(g, t.order, in_rec, n, cells);
@@ -199,7 +199,7 @@ cudaError_t binned_span_readout(const TableDev& t, const BinGeom& g, const doubl
     if (npts <= 0) return cudaSuccess;
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;
-    const int nblk = sm_count() * 2;
+    const int nblk = sm_count();
     // the production chunk bound: a sort CTA's slice stays below kMaxSlice
     const int64_t cap = std::min<int64_t>(npts, int64_t{nblk} * (bin_detail::kMaxSlice - 1));
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
@@ -262,7 +262,10 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     if (npts <= 0) return cudaSuccess;
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
-    const int nblk = sm_count() * 2;  // count/scatter CTAs of kSortThreads (one pair per SM)
+    // count CTAs, one per SM: fewer slices mean fewer (bucket, slice)
+    // segments that the scatter fills at once, so that more of its partly
+    // written lines stay in L2 until they are complete
+    const int nblk = sm_count();
     // a record names its query by its index within a sort CTA's slice
     // (below kMaxSlice)
     const int64_t cap = std::min<int64_t>(std::min<int64_t>(chunk, npts), int64_t{nblk} * (bin_detail::kMaxSlice - 1));

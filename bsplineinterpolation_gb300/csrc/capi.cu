@@ -289,29 +289,11 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
     return cudaSuccess;
 }
 
-// The correction solve of one refinement step and the update of (c, lo):
-// the last axis pass (axis 0, strided when D > 1) adds its solution to the
-// control points in its back sweep; a 1D table solves, then corrects.
+// The correction solve of one refinement step and the update of (c, lo).
 cudaError_t correction_solve(intp_table* t, float* corr, float* c, bool has_lo, cudaStream_t s) {
-    const int D = t->model.dim;
-    if (D == 1) {
-        cudaError_t e = solve_f32_all(t, corr, s);
-        if (e == cudaSuccess) e = launch_correct(c, t->ctrl_lo, corr, t->values(), has_lo, s);
-        return e;
-    }
-    for (int a = D - 1; a >= 1; --a) {
-        const LineGeom g = line_geom(t, a);
-        const AxisFactorDev& f = t->fac[a];
-        const LineFactor& lf = t->model.axis[a].factor;
-        cudaError_t e = launch_line_solve_f32(corr, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
-                                              f.dinvf, f.bottomf, f.rightf, s);
-        if (e != cudaSuccess) return e;
-    }
-    const LineGeom g = line_geom(t, 0);
-    const AxisFactorDev& f = t->fac[0];
-    const LineFactor& lf = t->model.axis[0].factor;
-    return launch_line_solve_f32_correct(corr, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
-                                         f.dinvf, f.bottomf, f.rightf, c, t->ctrl_lo, has_lo, s);
+    cudaError_t e = solve_f32_all(t, corr, s);
+    if (e == cudaSuccess) e = launch_correct(c, t->ctrl_lo, corr, t->values(), has_lo, s);
+    return e;
 }
 
 cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
@@ -477,6 +459,11 @@ bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv,
             plan.ord[k][d] = static_cast<int8_t>(std::min<int32_t>(v, order + 1));
         }
     group_plan(plan, dim);
+    // second and higher derivatives of high-order tables: the precise mixed
+    // contraction (the plain FP32 one leaves them near 2e-6 of their scale)
+    for (int k = 0; k < plan.k; ++k)
+        for (int d = 0; d < dim; ++d)
+            if (order >= 4 && plan.ord[k][d] >= 2 && plan.ord[k][d] <= order) plan.precise = 1;
     return true;
 }
 
@@ -806,8 +793,10 @@ intp_status intp_eval(const intp_table* t, const double* coords, int64_t npts, c
     std::string err;
     if (!make_plan(t, derivs, nderiv, plan, err)) return fail(INTP_ERR_INVALID_ARGUMENT, err);
     const int mode = eval_mode();
-    // binned needs the per-bucket counters to fit in shared memory
-    const bool binned = t->mixed() && t->model.dim <= 3 && t->bins.smem_buckets > 0 &&
+    // binned needs the per-bucket counters to fit in shared memory; plans
+    // that take the precise contraction read the control points' remainders
+    // per query and evaluate with the direct kernel
+    const bool binned = t->mixed() && t->model.dim <= 3 && t->bins.smem_buckets > 0 && !plan.precise &&
                         (mode == 2 || (mode == 0 && npts >= kBinnedMinPoints));
     if (binned) {
         retain_pool_memory();
@@ -1075,7 +1064,7 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
                         ") for the 8 MiB scratch of the allocation-free evaluation; use intp_eval");
     if (npts == 0) return INTP_OK;
-    if (!bins || npts < kBinnedMinPoints) {
+    if (!bins || npts < kBinnedMinPoints || plan.precise) {
         // the direct kernel needs no scratch: tables the binned path does not
         // take, and batches too small to be worth binning (as intp_eval)
         INTP_CUDA(launch_eval_direct(t->dev, t->mixed(), coords, npts, plan, out, out_f32, s), "evaluation kernel");

@@ -78,6 +78,9 @@ struct DerivPlan {
     int8_t out_group[kMaxDeriv];    // group of each output
     int32_t simple;                 // one group, all orders on axes 1..D-1 zero
     int32_t has_deriv;              // some output has a derivative order above 0
+    // mixed form: a derivative of order >= 2 on a table of order >= 4, which
+    // takes the precise per-query contraction (mixed_point.cuh)
+    int32_t precise;
 };
 
 // Spans per bucket (log2, per axis) of the binned evaluation, fixed per

@@ -112,6 +112,34 @@ __device__ __forceinline__ void mixed_channel(const TableDev& t, const DerivPlan
                                               const int64_t (&off)[D][O + 1], const float* __restrict__ cpc,
                                               const float* __restrict__ loc, void* __restrict__ out, int out_f32,
                                               int64_t o0, int C, int ch) {
+    if (plan.precise) {
+        // operands relative to the query's central control point, in
+        // double-float (its FP32 value and remainder)
+        int64_t oref = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) oref += off[d][ref_tap<O>()];
+        const float rh = __ldg(cpc + oref), rl = LO ? __ldg(loc + oref) : 0.0f;
+        precise_point_outputs<D, O>(
+            t, plan, cell, xr, base, rh, rl,
+            [&](const int (&ix)[D]) {
+                int64_t o = 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) o += off[d][ix[d]];
+                const float dh = __ldg(cpc + o) - rh;
+                if constexpr (LO)
+                    return dh + (__ldg(loc + o) - rl);
+                else
+                    return dh;
+            },
+            [out, out_f32, o0, C, ch](int k, float v) {
+                const int64_t e = (o0 + k) * C + ch;
+                if (out_f32)
+                    static_cast<float*>(out)[e] = v;
+                else
+                    static_cast<double*>(out)[e] = static_cast<double>(v);
+            });
+        return;
+    }
     const float cbase = LO ? __ldg(cpc + bucket_centre_offset<D, O>(t, cell)) : 0.0f;
     auto operand = [&](int64_t o) {
         const float h = __ldg(cpc + o);

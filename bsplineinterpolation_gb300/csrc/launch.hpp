@@ -97,13 +97,6 @@ bool residual3d_supported(const int* n, const int* band, int channels);
 cudaError_t launch_residual3d(const float* c_hi, const float* c_lo, const float* rhs_hi, const float* rhs_lo, float* r,
                               const int* n, const int* band, const int* periodic, const float2* const* val,
                               int channels, cudaStream_t s);
-// The refinement's last correction pass along a strided axis (S > 1): the
-// FP32 line solve of corr whose back sweep adds each solution value to
-// (c, lo) as a double-float (the correction kernel's update, fused).
-cudaError_t launch_line_solve_f32_correct(float* corr, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                          bool cyclic, const float* lower, const float* upper, const float* dinv,
-                                          const float* bottom, const float* right, float* c, float* lo, bool has_lo,
-                                          cudaStream_t s);
 // (c, lo) += corr in double-float (lo read as 0 unless has_lo).
 cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait

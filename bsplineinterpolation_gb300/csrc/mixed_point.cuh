@@ -23,6 +23,7 @@
 
 #include "basis32.cuh"
 #include "device_common.cuh"
+#include "refine_df.cuh"
 
 namespace intp_gb300 {
 
@@ -112,6 +113,107 @@ __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const Der
 #pragma unroll
                 for (int d = 1; d < D; ++d) value_out = value_out && plan.ord[k][d] == 0;
                 if (value_out) v = (v + cref) + cbase;
+            }
+            emit(k, v);
+        }
+    }
+}
+
+// Outputs of one query in the precise mixed form (DerivPlan::precise: a
+// derivative of order >= 2 on a table of order >= 4). Three changes from
+// mixed_point_outputs, each needed to hold such outputs within 1e-6 of
+// their scale (an FP32 emulation of the periodic order-7 workload put the
+// plain form's second derivatives at 2e-6 and this form's at 6e-7):
+//  - operands relative to the query's own central control point in
+//    double-float, (c_hi - ref_hi) + (c_lo - ref_lo), so their rounding
+//    scales with the variation across the stencil, not across a tile;
+//  - derivative weights from the basis recursion (axis_weights32_precise);
+//  - compensated accumulation (Dot2, refine_df.cuh) of every partial sum
+//    of the separable contraction, carried as double-floats between axes.
+// fetch(idx) returns the FP32 operand of control point (c_d - O + idx_d)_d;
+// ref = ref_hi + ref_lo is the central control point, added back to values.
+template <int D, int O, class Fetch, class Emit>
+__device__ __forceinline__ void precise_point_outputs(const TableDev& t, const DerivPlan& plan,
+                                                      const int64_t (&c)[D], const float (&u)[D],
+                                                      const float (&base)[D][O + 1], float ref_hi, float ref_lo,
+                                                      const Fetch& fetch, const Emit& emit) {
+    constexpr int W = O + 1;
+    constexpr int ROWS1 = D >= 2 ? ipow_i(W, D - 2) : 1;  // rows over axes 1..D-2
+    const int K = plan.k;
+    for (int grp = 0; grp < plan.ngroups; ++grp) {
+        const int rep = plan.group_rep[grp];
+        float w[D][W];
+        bool zero = false;
+#pragma unroll
+        for (int d = 1; d < D; ++d) {
+            const int kd = plan.ord[rep][d];
+            if (kd > O) {
+                zero = true;
+            } else if (kd == 0) {
+#pragma unroll
+                for (int i = 0; i < W; ++i) w[d][i] = base[d][i];
+            } else {
+                axis_weights32_precise<O>(t.ax[d], c[d], u[d], kd, w[d]);
+            }
+        }
+        float Ph[W], Pl[W];
+        constexpr int kUnrollI0 = W * ROWS1 * W <= 1024 ? W : 1;
+#pragma unroll kUnrollI0
+        for (int i0 = 0; i0 < W; ++i0) {
+            Dot2 acc{0.0f, 0.0f};
+#pragma unroll
+            for (int rw = 0; rw < ROWS1; ++rw) {
+                int idx[D];
+                idx[0] = i0;
+                float wr = 1.0f;
+                int rem = rw;
+#pragma unroll
+                for (int d = D - 2; d >= 1; --d) {
+                    idx[d] = rem % W;
+                    rem /= W;
+                    wr *= w[d][idx[d]];
+                }
+                if constexpr (D == 1) {
+                    acc.s = fetch(idx);
+                } else {
+                    Dot2 row{0.0f, 0.0f};
+#pragma unroll
+                    for (int i = 0; i < W; ++i) {
+                        idx[D - 1] = i;
+                        dot2_add<false>(row, make_float2(w[D - 1][i], 0.0f), fetch(idx), 0.0f);
+                    }
+                    const DF rv = dot2_value(row);
+                    if constexpr (D == 2) {
+                        acc = Dot2{rv.hi, rv.lo};
+                    } else {
+                        dot2_add<true>(acc, make_float2(wr, 0.0f), rv.hi, rv.lo);
+                    }
+                }
+            }
+            const DF pv = dot2_value(acc);
+            Ph[i0] = pv.hi;
+            Pl[i0] = pv.lo;
+        }
+        for (int k = 0; k < K; ++k) {
+            if (plan.out_group[k] != grp) continue;
+            const int k0 = plan.ord[k][0];
+            float v = 0.0f;
+            if (!zero && k0 <= O) {
+                float wl[W];
+                if (k0 == 0) {
+#pragma unroll
+                    for (int i = 0; i < W; ++i) wl[i] = base[0][i];
+                } else {
+                    axis_weights32_precise<O>(t.ax[0], c[0], u[0], k0, wl);
+                }
+                Dot2 fin{0.0f, 0.0f};
+#pragma unroll
+                for (int i = 0; i < W; ++i) dot2_add<true>(fin, make_float2(wl[i], 0.0f), Ph[i], Pl[i]);
+                v = __fadd_rn(fin.s, fin.c);
+                bool value_out = k0 == 0;
+#pragma unroll
+                for (int d = 1; d < D; ++d) value_out = value_out && plan.ord[k][d] == 0;
+                if (value_out) v = ref_hi + (v + ref_lo);
             }
             emit(k, v);
         }

@@ -51,6 +51,22 @@ struct R3Axis {
     const float2* val;
 };
 
+// Stencil row of one output index in registers: the taps, zero taps as
+// zeros (skipped by the accumulation, as the per-axis passes skip them).
+template <int BMAX>
+struct R3Row {
+    float2 a[2 * BMAX + 1];
+    __device__ __forceinline__ void load(const R3Axis& ax, int i, bool valid) {
+        const int w = 2 * ax.band + 1;
+#pragma unroll
+        for (int d = 0; d < 2 * BMAX + 1; ++d)
+            a[d] = (valid && d < w) ? __ldg(ax.val + static_cast<int64_t>(i) * w + d) : make_float2(0.0f, 0.0f);
+    }
+};
+
+// Lane = axis-2 position within the block's 32 columns; warp w owns rows
+// w, w + 8, ... of each pass. The axis-2 and axis-1 stencil rows of a
+// thread's outputs do not change along the march and stay in registers.
 template <int BMAX, bool HAS_LO>
 __global__ void __launch_bounds__(kR3Threads) residual3d_kernel(const float* __restrict__ c_hi,
                                                                 const float* __restrict__ c_lo,
@@ -58,8 +74,11 @@ __global__ void __launch_bounds__(kR3Threads) residual3d_kernel(const float* __r
                                                                 const float* __restrict__ rhs_lo,
                                                                 float* __restrict__ r, R3Axis az, R3Axis ay,
                                                                 R3Axis ax, int zsegs) {
-    constexpr int W = 2 * BMAX + 1;  // ring slots (>= 2 b_0 + 1)
+    constexpr int W = 2 * BMAX + 1;  // ring slots (>= 2 b_0 + 1) and taps per row
     constexpr int IY = kR3TY + 2 * BMAX, IX = kR3TX + 2 * BMAX;
+    constexpr int kWarps = kR3Threads / 32;
+    constexpr int kYRows = kR3TY / kWarps;  // y-pass rows per warp
+    static_assert(kR3TX == 32 && kR3TY % kWarps == 0, "lane = column, warps share the rows");
     __shared__ float2 inp[IY][IX];
     __shared__ float2 s1[IY][kR3TX];
     __shared__ float2 ring[W][kR3TY][kR3TX];
@@ -69,8 +88,15 @@ __global__ void __launch_bounds__(kR3Threads) residual3d_kernel(const float* __r
     const int64_t cbase = static_cast<int64_t>(ch) * nz * sz;  // channel block (channel-major storage)
     const int x0 = blockIdx.x * kR3TX, y0 = blockIdx.y * kR3TY, z0 = zseg * kR3ZS;
     const int z1 = z0 + kR3ZS < nz ? z0 + kR3ZS : nz;
-    const int tid = threadIdx.x;
-    const int wx = 2 * ax.band + 1, wy = 2 * ay.band + 1, wz = 2 * az.band + 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gx = x0 + lane;
+    const bool xin = gx < nx;
+    R3Row<BMAX> rx;
+    rx.load(ax, gx, xin);
+    R3Row<BMAX> ry[kYRows];
+#pragma unroll
+    for (int k = 0; k < kYRows; ++k) ry[k].load(ay, y0 + warp + k * kWarps, y0 + warp + k * kWarps < ny);
+    const int xo = BMAX - ax.band, yo = BMAX - ay.band;  // tap d reads halo column / row (out + offset + d)
     for (int zz = z0 - az.band; zz < z1 + az.band; ++zz) {
         // the slice: wrapped on a periodic axis; outside a non-periodic one it
         // is never read (its taps are zero) and is not computed
@@ -84,19 +110,19 @@ __global__ void __launch_bounds__(kR3Threads) residual3d_kernel(const float* __r
             const int64_t zoff = cbase + static_cast<int64_t>(zg) * sz;
             for (int e = tid; e < IY * IX; e += kR3Threads) {
                 const int iy = e / IX, ix = e - iy * IX;
-                int gy = y0 - BMAX + iy, gx = x0 - BMAX + ix;
+                int gy = y0 - BMAX + iy, gxx = x0 - BMAX + ix;
                 bool ok = true;
                 if (ay.periodic)
                     gy = wrap_mod(gy, ny);
                 else
                     ok = ok && gy >= 0 && gy < ny;
                 if (ax.periodic)
-                    gx = wrap_mod(gx, nx);
+                    gxx = wrap_mod(gxx, nx);
                 else
-                    ok = ok && gx >= 0 && gx < nx;
+                    ok = ok && gxx >= 0 && gxx < nx;
                 float2 v = make_float2(0.0f, 0.0f);
                 if (ok) {
-                    const int64_t j = zoff + static_cast<int64_t>(gy) * nx + gx;
+                    const int64_t j = zoff + static_cast<int64_t>(gy) * nx + gxx;
                     v.x = __ldg(c_hi + j);
                     if (HAS_LO) v.y = __ldg(c_lo + j);
                 }
@@ -104,75 +130,55 @@ __global__ void __launch_bounds__(kR3Threads) residual3d_kernel(const float* __r
             }
             __syncthreads();
             // axis 2 on every row of the block
-            for (int e = tid; e < IY * kR3TX; e += kR3Threads) {
-                const int iy = e / kR3TX, x = e - iy * kR3TX;
-                const int gx = x0 + x;
-                float2 out = make_float2(0.0f, 0.0f);
-                if (gx < nx) {
-                    Dot2 acc{0.0f, 0.0f};
-                    const float2* __restrict__ row = ax.val + static_cast<int64_t>(gx) * wx;
+            for (int iy = warp; iy < IY; iy += kWarps) {
+                Dot2 acc{0.0f, 0.0f};
 #pragma unroll
-                    for (int d = 0; d < W; ++d) {
-                        if (d < wx) {
-                            const float2 a = __ldg(row + d);
-                            if (a.x != 0.0f) {
-                                const float2 v = inp[iy][x + BMAX - ax.band + d];
-                                dot2_add<HAS_LO>(acc, a, v.x, v.y);
-                            }
-                        }
+                for (int d = 0; d < W; ++d) {
+                    if (rx.a[d].x != 0.0f) {
+                        const float2 v = inp[iy][lane + xo + d];
+                        dot2_add<HAS_LO>(acc, rx.a[d], v.x, v.y);
                     }
-                    const DF dv = dot2_value(acc);
-                    out = make_float2(dv.hi, dv.lo);
                 }
-                s1[iy][x] = out;
+                const DF dv = dot2_value(acc);
+                s1[iy][lane] = make_float2(dv.hi, dv.lo);
             }
             __syncthreads();
             // axis 1 -> the slice's ring slot
             float2(*slot)[kR3TX] = ring[wrap_mod(zz, W)];
-            for (int e = tid; e < kR3TY * kR3TX; e += kR3Threads) {
-                const int y = e / kR3TX, x = e - y * kR3TX;
-                const int gy = y0 + y;
-                float2 out = make_float2(0.0f, 0.0f);
-                if (gy < ny && x0 + x < nx) {
-                    Dot2 acc{0.0f, 0.0f};
-                    const float2* __restrict__ row = ay.val + static_cast<int64_t>(gy) * wy;
 #pragma unroll
-                    for (int d = 0; d < W; ++d) {
-                        if (d < wy) {
-                            const float2 a = __ldg(row + d);
-                            if (a.x != 0.0f) {
-                                const float2 v = s1[y + BMAX - ay.band + d][x];
-                                dot2_add<true>(acc, a, v.x, v.y);
-                            }
-                        }
+            for (int k = 0; k < kYRows; ++k) {
+                const int y = warp + k * kWarps;
+                Dot2 acc{0.0f, 0.0f};
+#pragma unroll
+                for (int d = 0; d < W; ++d) {
+                    if (ry[k].a[d].x != 0.0f) {
+                        const float2 v = s1[y + yo + d][lane];
+                        dot2_add<true>(acc, ry[k].a[d], v.x, v.y);
                     }
-                    const DF dv = dot2_value(acc);
-                    out = make_float2(dv.hi, dv.lo);
                 }
-                slot[y][x] = out;
+                const DF dv = dot2_value(acc);
+                slot[y][lane] = make_float2(dv.hi, dv.lo);
             }
         }
         __syncthreads();
         // axis 0 for the output whose last slice this was
         const int z = zz - az.band;
         if (z >= z0 && z < z1) {
-            const float2* __restrict__ row = az.val + static_cast<int64_t>(z) * wz;
-            for (int e = tid; e < kR3TY * kR3TX; e += kR3Threads) {
-                const int y = e / kR3TX, x = e - y * kR3TX;
-                const int gy = y0 + y, gx = x0 + x;
-                if (gy < ny && gx < nx) {
+            R3Row<BMAX> rz;
+            rz.load(az, z, true);
+            const int zo = z - az.band;  // slice of tap 0
+#pragma unroll
+            for (int k = 0; k < kYRows; ++k) {
+                const int y = warp + k * kWarps, gy = y0 + y;
+                if (gy < ny && xin) {
                     const int64_t j = cbase + static_cast<int64_t>(z) * sz + static_cast<int64_t>(gy) * nx + gx;
                     Dot2 acc{__ldg(rhs_hi + j), __ldg(rhs_lo + j)};
 #pragma unroll
                     for (int d = 0; d < W; ++d) {
-                        if (d < wz) {
-                            float2 a = __ldg(row + d);
-                            if (a.x != 0.0f) {
-                                a.x = -a.x;
-                                a.y = -a.y;
-                                const float2 v = ring[wrap_mod(z - az.band + d, W)][y][x];
-                                dot2_add<true>(acc, a, v.x, v.y);
-                            }
+                        if (rz.a[d].x != 0.0f) {
+                            const float2 a = make_float2(-rz.a[d].x, -rz.a[d].y);
+                            const float2 v = ring[wrap_mod(zo + d, W)][y][lane];
+                            dot2_add<true>(acc, a, v.x, v.y);
                         }
                     }
                     r[j] = __fadd_rn(acc.s, acc.c);

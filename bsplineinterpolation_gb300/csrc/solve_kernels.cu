@@ -61,25 +61,6 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R*
     }
 }
 
-// The refinement's last correction pass on a strided axis: the same line
-// solve, with the back sweep adding its solution to (c, lo) as a
-// double-float (CorrectStridedChunks) in place of the separate correction
-// kernel.
-template <int P, int Q, bool CYC>
-__global__ void __launch_bounds__(kSolveWarps * 32) solve_strided_correct_kernel(float* __restrict__ corr, int64_t n,
-                                                                                 int64_t S, int64_t nlines,
-                                                                                 FactorView<float> f,
-                                                                                 float* __restrict__ c,
-                                                                                 float* __restrict__ lo, int has_lo) {
-    for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
-         l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t o = l / S, t = l - o * S;
-        const int64_t base = o * n * S + t;
-        solve_line_chunked<float, P, Q, CYC, line_chunk<float>()>(
-            f, CorrectStridedChunks{corr + base, c + base, lo + base, S, has_lo != 0});
-    }
-}
-
 // Contiguous axis (S = 1): one warp per 32 consecutive lines.
 template <class R, int P, int Q, bool CYC>
 __global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_kernel(R* __restrict__ x, int64_t n,
@@ -158,16 +139,6 @@ cudaError_t launch_solve_r(R* x, int64_t n, int64_t S, int64_t nlines, int p, in
         case 6: return launch_solve_pq<R, 6, 6, false>(x, n, S, nlines, f, s);
     }
     return cudaErrorInvalidValue;
-}
-
-template <int P, int Q, bool CYC>
-cudaError_t launch_correct_pq(float* corr, int64_t n, int64_t S, int64_t nlines, const FactorView<float>& f, float* c,
-                              float* lo, bool has_lo, cudaStream_t s) {
-    constexpr int kThreads = kSolveWarps * 32;
-    const int grid = grid_for(nlines, kThreads, 152 * 64);
-    solve_strided_correct_kernel<P, Q, CYC><<<grid, kThreads, 0, s>>>(corr, n, S, nlines, f, c, lo, has_lo ? 1 : 0);
-    note_launch();
-    return cudaGetLastError();
 }
 
 // ---- data movement and residual kernels ----
@@ -370,33 +341,6 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
                                   const float* right, cudaStream_t s) {
     FactorView<float> f{n, lower, upper, dinv, bottom, right};
     return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
-}
-
-cudaError_t launch_line_solve_f32_correct(float* corr, int64_t n, int64_t S, int64_t nlines, int p, int q,
-                                          bool cyclic, const float* lower, const float* upper, const float* dinv,
-                                          const float* bottom, const float* right, float* c, float* lo, bool has_lo,
-                                          cudaStream_t s) {
-    if (p != q || S <= 1) return cudaErrorInvalidValue;
-    FactorView<float> f{n, lower, upper, dinv, bottom, right};
-    if (cyclic) {
-        switch (p) {
-            case 0: return launch_correct_pq<0, 0, true>(corr, n, S, nlines, f, c, lo, has_lo, s);
-            case 1: return launch_correct_pq<1, 1, true>(corr, n, S, nlines, f, c, lo, has_lo, s);
-            case 2: return launch_correct_pq<2, 2, true>(corr, n, S, nlines, f, c, lo, has_lo, s);
-            case 3: return launch_correct_pq<3, 3, true>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        }
-        return cudaErrorInvalidValue;
-    }
-    switch (p) {
-        case 0: return launch_correct_pq<0, 0, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 1: return launch_correct_pq<1, 1, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 2: return launch_correct_pq<2, 2, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 3: return launch_correct_pq<3, 3, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 4: return launch_correct_pq<4, 4, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 5: return launch_correct_pq<5, 5, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-        case 6: return launch_correct_pq<6, 6, false>(corr, n, S, nlines, f, c, lo, has_lo, s);
-    }
-    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,

@@ -14,8 +14,6 @@
 
 #include <cstdint>
 
-#include "refine_df.cuh"
-
 namespace intp_gb300 {
 
 template <class R>
@@ -52,11 +50,6 @@ struct StridedChunks {
         for (int k = 0; k < K; ++k)
             if (k < cnt) base[(i0 + k) * S] = buf[k];
     }
-    // the back sweep's stores: the line's solution
-    template <int K>
-    __device__ __forceinline__ void store_back(int64_t i0, int cnt, const R (&buf)[K]) const {
-        store(i0, cnt, buf);
-    }
 };
 
 // A line held contiguously (in shared memory).
@@ -74,11 +67,6 @@ struct SmemChunks {
 #pragma unroll
         for (int k = 0; k < K; ++k)
             if (k < cnt) base[i0 + k] = buf[k];
-    }
-    // the back sweep's stores: the line's solution
-    template <int K>
-    __device__ __forceinline__ void store_back(int64_t i0, int cnt, const R (&buf)[K]) const {
-        store(i0, cnt, buf);
     }
 };
 
@@ -131,11 +119,6 @@ struct WarpContigChunks {
             for (int r = 0; r < 32; ++r)
                 if (r < rows) x[r * n + i0 + lane] = stage[r * 33 + lane];
         }
-    }
-    // the back sweep's stores: the line's solution
-    template <int K>
-    __device__ __forceinline__ void store_back(int64_t i0, int cnt, const R (&buf)[K]) const {
-        store(i0, cnt, buf);
     }
 };
 
@@ -217,49 +200,6 @@ struct WarpContigChunksV4 {
                     if (4 * q + 2 < cnt) dst[2] = v.z;
                     if (4 * q + 3 < cnt) dst[3] = v.w;
                 }
-            }
-        }
-    }
-    // the back sweep's stores: the line's solution
-    template <int K>
-    __device__ __forceinline__ void store_back(int64_t i0, int cnt, const float (&buf)[K]) const {
-        store(i0, cnt, buf);
-    }
-};
-
-// StridedChunks over a correction line (the refinement's last solve pass on
-// a strided axis) whose back sweep, instead of storing the correction, adds
-// it to the refined control points (c, lo) as a double-float: the element-
-// wise df_correct of the separate correction kernel on the same values,
-// without the correction's round trip through memory.
-struct CorrectStridedChunks {
-    float* corr;
-    float* c;
-    float* lo;
-    int64_t S;
-    bool has_lo;
-    template <int K>
-    __device__ __forceinline__ void load(int64_t i0, int cnt, float (&buf)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) buf[k] = corr[(i0 + k) * S];
-    }
-    template <int K>
-    __device__ __forceinline__ void store(int64_t i0, int cnt, const float (&buf)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) corr[(i0 + k) * S] = buf[k];
-    }
-    template <int K>
-    __device__ __forceinline__ void store_back(int64_t i0, int cnt, const float (&buf)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            if (k < cnt) {
-                const int64_t j = (i0 + k) * S;
-                float h = c[j], l = has_lo ? lo[j] : 0.0f;
-                df_correct(h, l, buf[k], has_lo);
-                c[j] = h;
-                lo[j] = l;
             }
         }
     }
@@ -350,7 +290,7 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
                 if (Q > 0) zw[0] = v;
             }
         }
-        io.store_back(i0, cnt, buf);
+        io.store(i0, cnt, buf);
     }
 }
 

@@ -7,8 +7,8 @@ of the reference, pinned bit-exact to the reference's build).
 - Periodic high order: 2D, order 7, periodic in both axes, 512 x 512 of a
   sum of 16 random sinusoids (integer wavenumbers 1..20). Value, first and
   second derivatives: the FP64 form to 1e-12; the mixed form (FP32 cyclic
-  solve with a double-float residual refinement, FP32 weights) to 1e-6 on
-  values and first derivatives and 5e-6 on second derivatives.
+  solve with a double-float residual refinement, FP32 weights, the precise
+  contraction for second derivatives) to 1e-6 on every output.
 - 3D cubic (the headline workload at 64^3): FP64 to 1e-12; the mixed form's
   value and d/dx within 1e-6 of max |.|, its control points (double-floats
   after refinement) within 1e-11 of the FP64 form's.
@@ -79,14 +79,15 @@ def test_periodic_order7_fp64_matches_reference(periodic_o7):
 def test_periodic_order7_mixed_within_stated_error(periodic_o7):
     """Mixed form on the periodic order-7 table: the automatic refinement
     policy refines the FP32 cyclic solve with double-float residuals until the
-    control points are near 1e-12; the contraction reads them relative to
-    each query's central control point. Values and first derivatives within
-    1e-6 of each output's max magnitude; second derivatives, whose FP32
-    weights are amplified by (1/dx)^2, within 5e-6 (measured about 2e-6)."""
+    control points are near 1e-12. A request with second derivatives takes
+    the precise contraction (operands relative to each query's central
+    control point in double-float, recursion-based derivative weights,
+    compensated sums). Every output, values through second derivatives,
+    within 1e-6 of its max magnitude."""
     f, rng_, pts, want, _ = periodic_o7
     t = bi.InterpolationFunction(7, [True, True], torch.tensor(f, device="cuda"), rng_, rng_, precision="mixed")
     got = t.evaluate(torch.tensor(pts, device="cuda"), derivs=DERIVS_2ND).double().cpu().numpy()
-    tol = [1e-6, 1e-6, 1e-6, 5e-6, 5e-6, 5e-6]
+    tol = [1e-6] * 6
     for k in range(len(DERIVS_2ND)):
         assert norm_rel_err(got[:, k], want[:, k]) < tol[k], (DERIVS_2ND[k], norm_rel_err(got[:, k], want[:, k]))
 
