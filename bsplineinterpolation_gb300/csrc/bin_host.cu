@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "bin_impl.cuh"
 
@@ -115,6 +116,16 @@ __global__ void decode_spans_kernel(BinGeom g, int order, const uint32_t* __rest
 namespace {
 
 constexpr int32_t kSmemBucketLimit = 48 * 1024;
+
+int sort_ctas_per_sm() {
+    static int v = 0;
+    if (v == 0) {
+        const char* e = std::getenv("INTP_GB300_SORT_CTAS_PER_SM");
+        v = e ? std::atoi(e) : 2;
+        if (v < 1 || v > 3) v = 2;
+    }
+    return v;
+}
 
 int sm_count() {
     static int n = 0;
@@ -262,10 +273,10 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     if (npts <= 0) return cudaSuccess;
     const int D = t.dim;
     if (D > 3) return cudaErrorInvalidValue;  // D = 4 evaluates with the direct kernel
-    // count CTAs, one per SM: fewer slices mean fewer (bucket, slice)
-    // segments that the scatter fills at once, so that more of its partly
-    // written lines stay in L2 until they are complete
-    const int nblk = sm_count();
+    // count CTAs per SM (INTP_GB300_SORT_CTAS_PER_SM, 1..3; default 2):
+    // fewer slices mean fewer (bucket, slice) segments that the scatter
+    // fills at once, more of them a better spread of the count work
+    const int nblk = sm_count() * sort_ctas_per_sm();
     // a record names its query by its index within a sort CTA's slice
     // (below kMaxSlice)
     const int64_t cap = std::min<int64_t>(std::min<int64_t>(chunk, npts), int64_t{nblk} * (bin_detail::kMaxSlice - 1));

@@ -30,6 +30,9 @@ std::atomic<unsigned long long> g_launches{0};
 // more queries per sort means more of them per staged tile), smallest batch
 // worth binning
 constexpr int64_t kDefaultChunk = int64_t{1} << 28;
+// host-buffer evaluation (intp_eval_host): points per copy-in / evaluate /
+// copy-out stage of its pipeline
+constexpr int64_t kHostPipelineChunk = int64_t{1} << 24;
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
 // INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
@@ -39,13 +42,6 @@ int eval_mode() {
     if (std::strcmp(v, "direct") == 0) return 1;
     if (std::strcmp(v, "binned") == 0) return 2;
     return 0;
-}
-
-// INTP_GB300_RESIDUAL = passes: the per-axis residual passes for 3D tables
-// too (the fused kernel is the default; both give the same bits)
-bool fused_residual_enabled() {
-    const char* v = std::getenv("INTP_GB300_RESIDUAL");
-    return !(v && std::strcmp(v, "passes") == 0);
 }
 
 int64_t eval_chunk() {
@@ -289,13 +285,6 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
     return cudaSuccess;
 }
 
-// The correction solve of one refinement step and the update of (c, lo).
-cudaError_t correction_solve(intp_table* t, float* corr, float* c, bool has_lo, cudaStream_t s) {
-    cudaError_t e = solve_f32_all(t, corr, s);
-    if (e == cudaSuccess) e = launch_correct(c, t->ctrl_lo, corr, t->values(), has_lo, s);
-    return e;
-}
-
 cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
     for (int a = t->model.dim - 1; a >= 0; --a) {
         const LineGeom g = line_geom(t, a);
@@ -337,25 +326,9 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
         float* ping[2][2] = {{b + 2 * N, b + 3 * N}, {b + 4 * N, b + 5 * N}};
         INTP_CUDA(launch_shift_copy_f64_f32(values_dev, fhi, flo, c, sd, s), "shift copy");
         INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
-        // 3D tables: all residual passes in one launch (the same arithmetic)
-        int n3[3] = {}, band3[3] = {}, per3[3] = {};
-        const float2* val3[3] = {};
-        for (int d = 0; d < 3 && d < m.dim; ++d) {
-            n3[d] = static_cast<int>(m.axis[d].n);
-            band3[d] = t->fac[d].band;
-            per3[d] = m.axis[d].periodic ? 1 : 0;
-            val3[d] = t->fac[d].sval;
-        }
-        const bool fused = m.dim == 3 && fused_residual_enabled() && residual3d_supported(n3, band3, t->channels);
         for (int it = 0; it < steps; ++it) {
             // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass
             const float *ih = c, *il = it > 0 ? t->ctrl_lo : nullptr;
-            if (fused) {
-                INTP_CUDA(launch_residual3d(ih, il, fhi, flo, corr, n3, band3, per3, val3, t->channels, s),
-                          "residual");
-                INTP_CUDA(correction_solve(t, corr, c, it > 0, s), "line solve (correction)");
-                continue;
-            }
             int pp = 0;
             for (int a = m.dim - 1; a >= 0; --a) {
                 const LineGeom g = line_geom(t, a);
@@ -369,7 +342,8 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
                 il = ping[pp][1];
                 pp ^= 1;
             }
-            INTP_CUDA(correction_solve(t, corr, c, it > 0, s), "line solve (correction)");
+            INTP_CUDA(solve_f32_all(t, corr, s), "line solve (correction)");
+            INTP_CUDA(launch_correct(c, t->ctrl_lo, corr, N, it > 0, s), "correction");
         }
     }
     t->has_ctrl = true;
@@ -822,7 +796,9 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     const int D = t->model.dim;
     const int K = (derivs ? nderiv : 1) * t->channels;  // output values per point
     const size_t osz = out_dtype == INTP_F32 ? 4 : 8;
-    const int64_t chunk = eval_chunk();
+    // pipeline chunks: the copies of one chunk overlap the evaluation of the
+    // next, so they stay well below the sort's own chunk
+    const int64_t chunk = std::min<int64_t>(eval_chunk(), kHostPipelineChunk);
     if (npts <= chunk) {
         const size_t cb = static_cast<size_t>(npts) * D * 8;
         const size_t ob = static_cast<size_t>(npts) * K * osz;

@@ -89,14 +89,6 @@ cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_
 cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
                                  const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
                                  int band, bool periodic, const float2* val, cudaStream_t s);
-// All residual passes of a 3D table in one launch (residual3d.cu):
-// r = rhs - (A_0 x A_1 x A_2) (c_hi + c_lo), bit-identical to the three
-// launch_residual_pass calls (axis 2, 1, then 0). n, band, periodic, val per
-// axis; c_lo may be null; `channels` blocks of prod(n) values.
-bool residual3d_supported(const int* n, const int* band, int channels);
-cudaError_t launch_residual3d(const float* c_hi, const float* c_lo, const float* rhs_hi, const float* rhs_lo, float* r,
-                              const int* n, const int* band, const int* periodic, const float2* const* val,
-                              int channels, cudaStream_t s);
 // (c, lo) += corr in double-float (lo read as 0 unless has_lo).
 cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait

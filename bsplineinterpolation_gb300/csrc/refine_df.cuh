@@ -127,6 +127,40 @@ __device__ __forceinline__ void dot2_band_row_t(Dot2& acc, const float* __restri
     }
 }
 
+// ---- two independent accumulations per instruction ----
+// Blackwell's packed FP32x2 add / multiply / FMA carry out the same IEEE
+// single-precision operation, rounded to nearest, on each half of a register
+// pair, so the x2 forms below give, lane by lane, exactly the results of the
+// scalar forms above (a - b is fma(b, -1, a), one rounding of the exact
+// difference, as __fsub_rn). Two elements of a residual pass then cost the
+// instructions of one.
+struct Dot2x2 {
+    float2 s, c;
+};
+
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+
+// s + e = a + b exactly, per lane (df_two_sum).
+__device__ __forceinline__ void df_two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = __fadd2_rn(a, b);
+    const float2 bb = sub2_rn(s, a);
+    e = __fadd2_rn(sub2_rn(a, sub2_rn(s, bb)), sub2_rn(b, bb));
+}
+
+// dot2_add per lane: acc += (ahi + alo) * (xh + xl).
+template <bool HAS_LO>
+__device__ __forceinline__ void dot2_add2(Dot2x2& acc, float2 ahi, float2 alo, float2 xh, float2 xl) {
+    const float2 p = __fmul2_rn(ahi, xh);
+    float2 q = __ffma2_rn(ahi, xh, make_float2(-p.x, -p.y));
+    q = __ffma2_rn(alo, xh, q);
+    if (HAS_LO) q = __ffma2_rn(ahi, xl, q);
+    float2 t;
+    df_two_sum2(acc.s, p, acc.s, t);
+    acc.c = __fadd2_rn(acc.c, __fadd2_rn(t, q));
+}
+
 // Normalised double-float value of an accumulator.
 __device__ __forceinline__ DF dot2_value(const Dot2& acc) { return df_two_sum(acc.s, acc.c); }
 

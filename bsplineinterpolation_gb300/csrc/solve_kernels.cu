@@ -226,6 +226,74 @@ struct AxisPos {
 // the warp's coefficient loads are broadcasts.
 constexpr int kResidualIlp = 4;
 
+// One element pair of a residual pass: elements e0, e1 (e1 >= N: a dummy
+// lane with zero coefficients and operands, never stored) as the two lanes
+// of the packed accumulator. Each lane applies dot2_band_row_t's taps in its
+// order; a tap that is zero in one lane only adds an exact zero there (the
+// running sum and error term keep their values), so each lane's result is
+// that of the scalar pass.
+template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
+__device__ __forceinline__ void residual_pair(const float* __restrict__ in_hi, const float* __restrict__ in_lo,
+                                              float* __restrict__ out_hi, float* __restrict__ out_lo,
+                                              const float* __restrict__ rhs_hi, const float* __restrict__ rhs_lo,
+                                              float* __restrict__ r, const AxisPos& pos, I S, I N, int n,
+                                              const float2* __restrict__ val, I e0, I e1) {
+    constexpr int W = 2 * BAND + 1;
+    const bool v1 = e1 < N;
+    const I i0 = pos(e0), i1 = v1 ? pos(e1) : I(0);
+    const I b0 = e0 - i0 * S, b1 = v1 ? e1 - i1 * S : I(0);
+    Dot2x2 acc{make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+    if (FINAL) {
+        acc.s = make_float2(rhs_hi[e0], v1 ? rhs_hi[e1] : 0.0f);
+        acc.c = make_float2(rhs_lo[e0], v1 ? rhs_lo[e1] : 0.0f);
+    }
+    const float2* __restrict__ row0 = val + static_cast<int64_t>(i0) * W;
+    const float2* __restrict__ row1 = val + static_cast<int64_t>(i1) * W;
+#pragma unroll
+    for (int d = 0; d < W; ++d) {
+        float2 a0 = __ldg(row0 + d);
+        float2 a1 = v1 ? __ldg(row1 + d) : make_float2(0.0f, 0.0f);
+        const bool z0 = a0.x == 0.0f, z1 = a1.x == 0.0f;
+        if (z0 && z1) continue;
+        if (FINAL) {
+            a0.x = -a0.x;
+            a0.y = -a0.y;
+            a1.x = -a1.x;
+            a1.y = -a1.y;
+        }
+        float2 xh = make_float2(0.0f, 0.0f), xl = make_float2(0.0f, 0.0f);
+        if (!z0) {
+            int c = static_cast<int>(i0) - BAND + d;
+            if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
+            const I j = b0 + static_cast<I>(c) * S;
+            xh.x = __ldg(in_hi + j);
+            if (HAS_LO) xl.x = __ldg(in_lo + j);
+        }
+        if (!z1) {
+            int c = static_cast<int>(i1) - BAND + d;
+            if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
+            const I j = b1 + static_cast<I>(c) * S;
+            xh.y = __ldg(in_hi + j);
+            if (HAS_LO) xl.y = __ldg(in_lo + j);
+        }
+        dot2_add2<HAS_LO>(acc, make_float2(a0.x, a1.x), make_float2(a0.y, a1.y), xh, xl);
+    }
+    if (FINAL) {
+        const float2 v = __fadd2_rn(acc.s, acc.c);
+        r[e0] = v.x;
+        if (v1) r[e1] = v.y;
+    } else {
+        float2 h, l;
+        df_two_sum2(acc.s, acc.c, h, l);
+        out_hi[e0] = h.x;
+        out_lo[e0] = l.x;
+        if (v1) {
+            out_hi[e1] = h.y;
+            out_lo[e1] = l.y;
+        }
+    }
+}
+
 template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
 __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restrict__ in_hi,
                                                             const float* __restrict__ in_lo, float* __restrict__ out_hi,
@@ -237,22 +305,11 @@ __global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restr
     const I stride = static_cast<I>(gridDim.x) * blockDim.x;
     for (I e0 = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e0 < N; e0 += kResidualIlp * stride) {
 #pragma unroll
-        for (int u = 0; u < kResidualIlp; ++u) {
+        for (int u = 0; u < kResidualIlp; u += 2) {
             const I e = e0 + u * stride;
-            if (e < N) {
-                const I i = pos(e);
-                Dot2 acc{0.0f, 0.0f};
-                if (FINAL) acc = Dot2{rhs_hi[e], rhs_lo[e]};
-                dot2_band_row_t<BAND, PERIODIC, HAS_LO, FINAL, I>(acc, in_hi, in_lo, e - i * S, static_cast<int>(i), n,
-                                                                   S, val);
-                if (FINAL) {
-                    r[e] = __fadd_rn(acc.s, acc.c);
-                } else {
-                    const DF v = dot2_value(acc);
-                    out_hi[e] = v.hi;
-                    out_lo[e] = v.lo;
-                }
-            }
+            if (e < N)
+                residual_pair<I, BAND, PERIODIC, HAS_LO, FINAL>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, S,
+                                                                N, n, val, e, e + stride);
         }
     }
 }
