@@ -96,6 +96,8 @@ SIGNATURES = {
     "intp_locate": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P]),
     "intp_locate_binned": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_stream_synchronize": (C.c_int, [_P]),
+    "intp_debug_set_wait_limit": (C.c_int, [C.c_uint32]),
+    "intp_debug_fail_allocations": (C.c_int, [C.c_int32]),
     "intp_last_error": (C.c_char_p, []),
     "intp_launch_count": (C.c_uint64, []),
     "intp_bandlu_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P,

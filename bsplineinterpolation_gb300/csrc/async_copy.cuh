@@ -13,6 +13,11 @@ namespace intp_gb300 {
 static __device__ int g_device_error;
 constexpr int kErrWaitTimeout = 1;
 
+// Diagnostics (intp_debug_set_wait_limit): when nonzero, the binned
+// evaluation's wait for each staged tile gives up after this many
+// non-blocking probes of its barrier instead of its normal bounded wait.
+static __device__ uint32_t g_tile_wait_probes;
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -36,6 +41,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
             "{\n"
             ".reg .pred p;\n"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n"
+            "}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    atomicExch(&g_device_error, kErrWaitTimeout);
+    return false;
+}
+
+// At most `probes` non-blocking tests of phase `parity` (mbarrier.test_wait);
+// on giving up sets the device error flag like mbar_wait.
+__device__ __forceinline__ bool mbar_probe(uint64_t* bar, uint32_t parity, uint32_t probes) {
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t i = 0; i < probes; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n"
+            ".reg .pred p;\n"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
             "selp.u32 %0, 1, 0, p;\n"
             "}\n"
             : "=r"(done)
@@ -118,6 +144,14 @@ __device__ __forceinline__ void cp_async_wait_all() {
         cudaMemcpyToSymbolAsync(g_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);            \
         cudaStreamSynchronize(s);                                                                             \
         return v;                                                                                             \
+    }
+
+// Defines `cudaError_t NAME(uint32_t)`: sets this translation unit's copy of
+// g_tile_wait_probes (0 = the normal wait).
+#define INTP_DEFINE_WAIT_PROBE_SETTER(NAME)                                                    \
+    cudaError_t NAME(uint32_t probes) {                                                        \
+        return cudaMemcpyToSymbol(g_tile_wait_probes, &probes, sizeof(uint32_t), 0,            \
+                                  cudaMemcpyHostToDevice);                                     \
     }
 
 }  // namespace intp_gb300

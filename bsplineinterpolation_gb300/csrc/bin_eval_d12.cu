@@ -65,5 +65,6 @@ cudaError_t launch_bin_eval_d12(const TableDev& t, const BinGeom& g, const CUten
 }
 
 INTP_DEFINE_DEVICE_ERROR_READER(take_device_error_bin_d12)
+INTP_DEFINE_WAIT_PROBE_SETTER(set_wait_probes_bin_d12)
 
 }  // namespace intp_gb300

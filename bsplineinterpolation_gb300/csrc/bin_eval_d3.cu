@@ -64,5 +64,6 @@ cudaError_t launch_bin_eval_d3(const TableDev& t, const BinGeom& g, const CUtens
 }
 
 INTP_DEFINE_DEVICE_ERROR_READER(take_device_error_bin_d3)
+INTP_DEFINE_WAIT_PROBE_SETTER(set_wait_probes_bin_d3)
 
 }  // namespace intp_gb300

@@ -42,9 +42,9 @@ namespace intp_gb300 {
 namespace bin_detail {
 
 constexpr int kBinThreads = 256;   // evaluation CTA
-constexpr int kLocateThreads = 1024;  // count CTA (one per SM: one slice of the chunk each)
-constexpr int kSortThreads = 512;     // scatter CTA (two per SM; four records per thread in flight)
-constexpr int kPermuteParts = 2;      // scatter CTAs per count CTA's slice
+constexpr int kLocateThreads = 768;  // count CTA (two per SM at up to 42 registers)
+constexpr int kSortThreads = 768;    // scatter CTA (two per SM at up to 42 registers)
+constexpr int kPermuteParts = 1;     // scatter CTAs per count CTA's slice
 
 // Exact span and FP32 local offset of one coordinate on axis a (mixed form),
 // with 32-bit span indices (binned tables have fewer than 2^31 knots per
@@ -134,7 +134,7 @@ __device__ __forceinline__ void rec_load(const uint32_t* rec, int64_t slot, uint
 // Shared-memory atomics are aggregated per warp (__match_any_sync), and every
 // thread runs the same number of loop trips so the match sees all lanes.
 template <int D>
-__global__ void __launch_bounds__(kLocateThreads, 1) locate_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
+__global__ void __launch_bounds__(kLocateThreads, 2) locate_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
                                                              int64_t n, int64_t slice, uint32_t* __restrict__ in_rec,
                                                              uint32_t* __restrict__ rank,
                                                              uint32_t* __restrict__ blkcount) {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kLocateThreads, 1) locate_kernel(TableDev t, B
 
 // Every record of the slice to slot = (first slot of its (bucket, CTA) pair)
 // + (its rank there, from the locate kernel): independent streaming copies,
-// four records per thread and trip with all loads in flight. CTA j takes
+// three records per thread and trip with all loads in flight. CTA j takes
 // part j % kPermuteParts of count CTA j / kPermuteParts's slice.
 template <int D>
 __global__ void __launch_bounds__(kSortThreads, 2) permute_kernel(BinGeom g, int64_t n, int64_t slice,
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) permute_kernel(BinGeom g, int
                                                               uint32_t* __restrict__ rec) {
     extern __shared__ uint32_t sh_first[];
     constexpr int RW = rec_words<D>();
-    constexpr int U = 4;
+    constexpr int U = 3;
     const int nblk = gridDim.x / kPermuteParts, blk = blockIdx.x / kPermuteParts;
     const int part = blockIdx.x - blk * kPermuteParts;
     for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_first[b] = __ldg(blkoffset + b * nblk + blk);
@@ -265,40 +265,8 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
 #pragma unroll
     for (int d = 1; d < D; ++d) axis_weights32<O>(t.ax[d], c[d], u[d], 0, w[d]);
     float Pz[W];
-    // axis-0 positions two at a time: each FP32x2 instruction (Blackwell's
-    // packed add / FMA) carries the same operation for positions i0 and
-    // i0 + 1, in the order of the scalar recurrence
-    // Pz[i0] = sum_rows wr * sum_i w_{D-1}[i] (tile - cref)
-    constexpr int kPairs = D >= 2 ? W / 2 : 0;
-    const float2 nref = make_float2(-cref, -cref);
 #pragma unroll
-    for (int pr = 0; pr < kPairs; ++pr) {
-        float2 acc = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int rw = 0; rw < ROWS1; ++rw) {
-            int off = 2 * pr * TS::S(0);
-            float wr = 1.0f;
-            int rem = rw;
-#pragma unroll
-            for (int d = D - 2; d >= 1; --d) {
-                const int i = rem % W;
-                rem /= W;
-                wr *= w[d][i];
-                off += i * TS::S(d);
-            }
-            float2 s2 = make_float2(0.0f, 0.0f);
-#pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const float2 op = __fadd2_rn(make_float2(tl[off + i], tl[off + TS::S(0) + i]), nref);
-                s2 = __ffma2_rn(make_float2(w[D - 1][i], w[D - 1][i]), op, s2);
-            }
-            acc = __ffma2_rn(make_float2(wr, wr), s2, acc);
-        }
-        Pz[2 * pr] = acc.x;
-        Pz[2 * pr + 1] = acc.y;
-    }
-#pragma unroll
-    for (int i0 = 2 * kPairs; i0 < W; ++i0) {
+    for (int i0 = 0; i0 < W; ++i0) {
         float acc = 0.0f;
 #pragma unroll
         for (int rw = 0; rw < ROWS1; ++rw) {
@@ -317,8 +285,8 @@ __device__ __forceinline__ void lean_point(const TableDev& t, const int (&c)[D],
             } else {
                 float s = 0.0f;
 #pragma unroll
-                for (int i = 0; i < W; ++i) s = fmaf(w[D - 1][i], tl[off + i] - cref, s);
-                acc = fmaf(wr, s, acc);
+                for (int i = 0; i < W; ++i) s += w[D - 1][i] * (tl[off + i] - cref);
+                acc += wr * s;
             }
         }
         Pz[i0] = acc;
@@ -611,7 +579,8 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
                     if constexpr (D == 2) tma_load_2d(tile_lo, &tmap_lo, org[1], org[0], &sh_bar);
                 }
             }
-            const bool ok = mbar_wait(&sh_bar, bar_phase);
+            const uint32_t probes = g_tile_wait_probes;  // diagnostics: a forced short wait
+            const bool ok = probes ? mbar_probe(&sh_bar, bar_phase, probes) : mbar_wait(&sh_bar, bar_phase);
             if (!__syncthreads_and(ok)) {
                 if (!ok) mbar_wait(&sh_bar, bar_phase);  // bounded: let the copy in flight land
                 return;

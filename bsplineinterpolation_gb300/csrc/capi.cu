@@ -24,6 +24,16 @@ using namespace intp_gb300;
 namespace {
 
 std::atomic<unsigned long long> g_launches{0};
+// Diagnostics (intp_debug_fail_allocations): device allocations of tables
+// still to be failed as out of memory, without calling the allocator.
+std::atomic<int> g_fail_allocs{0};
+
+bool take_injected_alloc_failure() {
+    int v = g_fail_allocs.load();
+    while (v > 0)
+        if (g_fail_allocs.compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
 
 // binned evaluation: queries per chunk (one sort of up to 2^28 queries: each
 // bucket's tile is staged once per evaluation CTA that meets the bucket, and
@@ -122,6 +132,7 @@ struct intp_table {
     cudaStream_t alloc_stream = nullptr;
 
     cudaError_t dmalloc(void** p, size_t bytes) {
+        if (take_injected_alloc_failure()) return cudaErrorMemoryAllocation;
         return stream_ordered ? cudaMallocAsync(p, bytes, alloc_stream) : cudaMalloc(p, bytes);
     }
     void dfree(void* p) {
@@ -936,6 +947,18 @@ intp_status intp_locate_binned(const intp_table* t, const double* coords, int64_
         return fail(INTP_ERR_UNSUPPORTED, "the table does not take the binned evaluation path");
     INTP_CUDA(binned_span_readout(t->dev, t->bins, coords, npts, cells, static_cast<cudaStream_t>(stream)),
               "binned span read-out");
+    return INTP_OK;
+}
+
+intp_status intp_debug_set_wait_limit(uint32_t probes) {
+    INTP_CUDA(set_wait_probes_bin_d3(probes), "cudaMemcpyToSymbol(wait probes)");
+    INTP_CUDA(set_wait_probes_bin_d12(probes), "cudaMemcpyToSymbol(wait probes)");
+    return INTP_OK;
+}
+
+intp_status intp_debug_fail_allocations(int32_t count) {
+    if (count < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "count must be >= 0");
+    g_fail_allocs.store(count);
     return INTP_OK;
 }
 

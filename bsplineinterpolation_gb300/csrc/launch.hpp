@@ -57,6 +57,9 @@ cudaError_t launch_bin_eval_d3(const TableDev&, const BinGeom&, const CUtensorMa
 // Read and clear the device error flag of the binned evaluation units.
 int take_device_error_bin_d12(cudaStream_t s);
 int take_device_error_bin_d3(cudaStream_t s);
+// Diagnostics: probes of the binned evaluation's tile wait (0 = normal wait).
+cudaError_t set_wait_probes_bin_d12(uint32_t probes);
+cudaError_t set_wait_probes_bin_d3(uint32_t probes);
 // Bucket geometry of the binned evaluation for a table: compile-time bucket
 // sizes per dimension (bucket_log2); smem_buckets = 0 when the table has too
 // many buckets or too many knots for the binned path.

@@ -14,6 +14,8 @@
 
 #include <cstdint>
 
+#include "async_copy.cuh"
+
 namespace intp_gb300 {
 
 template <class R>
@@ -202,6 +204,100 @@ struct WarpContigChunksV4 {
                 }
             }
         }
+    }
+};
+
+// StridedChunks with the chunk loads streamed ahead through shared memory:
+// each thread keeps a ring of NB chunk buffers (cp.async element copies, one
+// commit group per chunk) and, when the substitution asks for chunk c, the
+// copies of chunks c+1 .. c+NB-1 are already in flight. The loaded values
+// and the arithmetic are those of StridedChunks; only the waiting changes
+// (the serial chain of a line no longer waits a memory latency per chunk)
+// and no registers hold data in flight.
+//
+// The substitution's request order is fixed: (cyclic only) the last Q
+// elements, the forward chunks i0 = 0, K, 2K, ..., then the back chunks
+// ending at n-1, n-1-K, .... The ring follows that order; the back chunks
+// are fetched only after the forward sweep has written the whole line (a
+// block fence orders those writes before the copies that read them back).
+// ring[slot][k][tid]: thread-fastest, so a warp's accesses to one buffer
+// element are conflict-free.
+template <class R, int K, int NB>
+struct PrefetchStridedChunks {
+    R* base;
+    int64_t S;
+    int64_t n;
+    R* ring;       // NB * K * nthreads elements
+    int nthreads;
+    int tid;
+    bool cyc_head;  // the cyclic substitution's first request (last Q elements) comes first
+    int Q;
+    // request sequence state
+    mutable int next_req;    // index of the next request in the forward+back order
+    mutable int next_issue;  // index of the next chunk to issue
+    int nf;                  // forward chunks
+    __device__ __forceinline__ int total() const { return 2 * nf; }
+    // chunk j of the sequence: [lo, lo + cnt)
+    __device__ __forceinline__ void chunk(int j, int64_t& lo, int& cnt) const {
+        if (j < nf) {
+            lo = static_cast<int64_t>(j) * K;
+            cnt = static_cast<int>(n - lo < K ? n - lo : K);
+        } else {
+            const int64_t i1 = n - 1 - static_cast<int64_t>(j - nf) * K;
+            cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
+            lo = i1 - cnt + 1;
+        }
+    }
+    __device__ __forceinline__ R* slot(int j, int k) const { return ring + ((j % NB) * K + k) * nthreads + tid; }
+    __device__ __forceinline__ void issue(int j) const {
+        int64_t lo;
+        int cnt;
+        chunk(j, lo, cnt);
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) cp_async<sizeof(R)>(slot(j, k), base + (lo + k) * S);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    // issue chunks up to `upto` (exclusive), forward chunks any time, back
+    // chunks once the forward sweep is done (next_req >= nf)
+    __device__ __forceinline__ void fill(int upto) const {
+        while (next_issue < upto && next_issue < total()) {
+            if (next_issue >= nf && next_req < nf) break;
+            issue(next_issue++);
+        }
+    }
+    template <int KK>
+    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[KK]) const {
+        static_assert(KK == K, "chunk size of the ring");
+        if (cyc_head && next_req < 0) {
+            // the cyclic head: a direct load of the last Q elements
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (k < cnt) buf[k] = base[(i0 + k) * S];
+            next_req = 0;
+            return;
+        }
+        if (next_req == nf) __threadfence_block();  // the forward writes before the back copies
+        fill(next_req + NB);
+        // wait for chunk next_req: groups complete in order, and at most
+        // next_issue - next_req - 1 later ones may stay pending
+        const int pending = next_issue - next_req - 1;
+        if (pending >= 2)
+            asm volatile("cp.async.wait_group 2;" ::: "memory");
+        else if (pending == 1)
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = *slot(next_req, k);
+        ++next_req;
+    }
+    template <int KK>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[KK]) const {
+#pragma unroll
+        for (int k = 0; k < KK; ++k)
+            if (k < cnt) base[(i0 + k) * S] = buf[k];
     }
 };
 

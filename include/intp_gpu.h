@@ -187,6 +187,23 @@ intp_status intp_locate(const intp_table* table, const double* coords, int64_t n
 intp_status intp_locate_binned(const intp_table* table, const double* coords, int64_t npts,
                                int64_t* cells, void* stream);
 
+/* ---- diagnostics (failure paths) ----
+ * No counterpart in the reference. They let a test drive the library's
+ * failure paths without faulting or hanging the device. */
+
+/* The binned evaluation waits for each staged tile on a barrier with a
+ * bounded wait, and when the wait runs out it records INTP_ERR_TIMEOUT (read
+ * by intp_stream_synchronize) and stops its work, after letting the copy in
+ * flight land. probes > 0 replaces that wait by `probes` non-blocking tests
+ * of the barrier, so that it runs out at once; 0 restores the normal wait.
+ * Device-wide; for tests only. */
+intp_status intp_debug_set_wait_limit(uint32_t probes);
+/* Fails the next `count` device allocations of table storage (creation,
+ * including tables built by the serving loop) as out of memory
+ * (INTP_ERR_OUT_OF_MEMORY, the reference's std::bad_alloc) without calling
+ * the allocator; 0 clears it. Process-wide; for tests only. */
+intp_status intp_debug_fail_allocations(int32_t count);
+
 /* Waits for `stream`. */
 intp_status intp_stream_synchronize(void* stream);
 

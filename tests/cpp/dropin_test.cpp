@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <array>
 #include <vector>
@@ -210,6 +211,23 @@ static int extras() {
         }
         const auto cp = circle.spline().control_points();
         if (cp.size() != pn) ++bad;
+    }
+    // an allocation failure surfaces as the reference's std::bad_alloc
+    // (aligned-allocator.hpp); intp_debug_fail_allocations injects one
+    {
+        intp_debug_fail_allocations(1);
+        bool thrown = false;
+        try {
+            intp::InterpolationFunction1D<3> g(std::make_pair(v.begin(), v.end()));
+            (void)g;
+        } catch (const std::bad_alloc&) {
+            thrown = true;
+        }
+        intp_debug_fail_allocations(0);
+        if (!thrown) {
+            std::printf("no bad_alloc on an allocation failure\n");
+            ++bad;
+        }
     }
     std::printf("extras %d\n", bad);
     return bad;
