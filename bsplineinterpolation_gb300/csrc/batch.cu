@@ -113,36 +113,36 @@ __device__ __forceinline__ FactorView<R> factor_view(const AxisFactorDev& f, int
 
 template <>
 __device__ __forceinline__ FactorView<float> factor_view<float>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf};
+    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf, f.clo, f.chi};
 }
 
 template <>
 __device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right};
+    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right, f.clo, f.chi};
 }
 
 // Lines are walked in chunks of this many elements (registers per lane).
 constexpr int kBatchChunk = 16;
 
-template <class R, class Line>
+template <class R, class Line, bool CONST_ROWS = false>
 __device__ __forceinline__ void solve_dispatch(int p, bool cyc, const FactorView<R>& fv, const Line& line) {
     if (cyc) {
         switch (p) {
-            case 0: solve_line_chunked<R, 0, 0, true, kBatchChunk>(fv, line); return;
-            case 1: solve_line_chunked<R, 1, 1, true, kBatchChunk>(fv, line); return;
-            case 2: solve_line_chunked<R, 2, 2, true, kBatchChunk>(fv, line); return;
-            case 3: solve_line_chunked<R, 3, 3, true, kBatchChunk>(fv, line); return;
+            case 0: solve_line_chunked<R, 0, 0, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+            case 1: solve_line_chunked<R, 1, 1, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+            case 2: solve_line_chunked<R, 2, 2, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+            case 3: solve_line_chunked<R, 3, 3, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
         }
         return;
     }
     switch (p) {
-        case 0: solve_line_chunked<R, 0, 0, false, kBatchChunk>(fv, line); return;
-        case 1: solve_line_chunked<R, 1, 1, false, kBatchChunk>(fv, line); return;
-        case 2: solve_line_chunked<R, 2, 2, false, kBatchChunk>(fv, line); return;
-        case 3: solve_line_chunked<R, 3, 3, false, kBatchChunk>(fv, line); return;
-        case 4: solve_line_chunked<R, 4, 4, false, kBatchChunk>(fv, line); return;
-        case 5: solve_line_chunked<R, 5, 5, false, kBatchChunk>(fv, line); return;
-        case 6: solve_line_chunked<R, 6, 6, false, kBatchChunk>(fv, line); return;
+        case 0: solve_line_chunked<R, 0, 0, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 1: solve_line_chunked<R, 1, 1, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 2: solve_line_chunked<R, 2, 2, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 3: solve_line_chunked<R, 3, 3, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 4: solve_line_chunked<R, 4, 4, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 5: solve_line_chunked<R, 5, 5, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 6: solve_line_chunked<R, 6, 6, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
     }
 }
 
@@ -174,7 +174,14 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) tile[r * pitch + k] = src[static_cast<int64_t>(r) * ni + k];
         __syncwarp();
-        if (lane < it.rows) solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
+        // a staged line walked by one lane (1D tables): the factor's constant
+        // rows come from registers
+        if (lane < it.rows) {
+            if (it.rows == 1)
+                solve_dispatch<R, SmemChunks<R>, true>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
+            else
+                solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
+        }
         __syncwarp();
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) src[static_cast<int64_t>(r) * ni + k] = tile[r * pitch + k];
@@ -187,60 +194,125 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
     }
 }
 
-// Residual pass of the refinement with Dot2 accumulation: mid = A_axis in
-// as a double-float, or corr = F - A_axis in (FP32) on the table's last pass
-// (axis 0), for every line of the item. Each output element is an
-// independent band-row product (dot2_band_row, the operations of the
-// single-table residual), so the lanes spread over the elements of each line
-// of the contiguous axis (coalesced) and over adjacent lines of a strided
-// axis. HAS_LO: the input is double-float (else plain FP32).
+// Residual pass j of the refinement over the value chunks (element-parallel,
+// 256 threads per chunk of at most kChunkElems values of one table): axis
+// D - 1 - j of the chunk's table, the operations of batch_stencil_kernel on
+// every element (dot2_band_row: mid = A_axis in as a double-float, or
+// corr = F - A_axis in on the table's last pass), with two elements per
+// thread in the packed form (dot2_add2) and the band known at compile time.
+template <int BAND, bool PERIODIC, bool HAS_LO, bool LAST>
+__device__ __forceinline__ void stencil_chunk(const float* __restrict__ ih, const float* __restrict__ il,
+                                              float* __restrict__ mid_hi, float* __restrict__ mid_lo,
+                                              float* __restrict__ corr, const float* __restrict__ fhi,
+                                              const float* __restrict__ flo, int start, int len, int n, int S,
+                                              const float2* __restrict__ val) {
+    constexpr int W = 2 * BAND + 1;
+    for (int e = threadIdx.x; e < len; e += 2 * blockDim.x) {
+        const int ea = start + e, eb = ea + static_cast<int>(blockDim.x);
+        const bool vb = e + static_cast<int>(blockDim.x) < len;
+        const int ia = (ea / S) % n, ib = vb ? (eb / S) % n : 0;
+        const int ba = ea - ia * S, bb = vb ? eb - ib * S : 0;
+        Dot2x2 acc{make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+        if (LAST) {
+            acc.s = make_float2(fhi[ea], vb ? fhi[eb] : 0.0f);
+            acc.c = make_float2(flo[ea], vb ? flo[eb] : 0.0f);
+        }
+#pragma unroll
+        for (int d = 0; d < W; ++d) {
+            float2 a0 = __ldg(val + ia * W + d);
+            float2 a1 = vb ? __ldg(val + ib * W + d) : make_float2(0.0f, 0.0f);
+            const bool z0 = a0.x == 0.0f, z1 = a1.x == 0.0f;
+            if (z0 && z1) continue;
+            if (LAST) {
+                a0 = make_float2(-a0.x, -a0.y);
+                a1 = make_float2(-a1.x, -a1.y);
+            }
+            float2 xh = make_float2(0.0f, 0.0f), xl = make_float2(0.0f, 0.0f);
+            if (!z0) {
+                int c = ia - BAND + d;
+                if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
+                const int j = ba + c * S;
+                xh.x = __ldg(ih + j);
+                if (HAS_LO) xl.x = __ldg(il + j);
+            }
+            if (!z1) {
+                int c = ib - BAND + d;
+                if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
+                const int j = bb + c * S;
+                xh.y = __ldg(ih + j);
+                if (HAS_LO) xl.y = __ldg(il + j);
+            }
+            dot2_add2<HAS_LO>(acc, make_float2(a0.x, a1.x), make_float2(a0.y, a1.y), xh, xl);
+        }
+        if (LAST) {
+            const float2 v = __fadd2_rn(acc.s, acc.c);
+            corr[ea] = v.x;
+            if (vb) corr[eb] = v.y;
+        } else {
+            float2 h, l;
+            df_two_sum2(acc.s, acc.c, h, l);
+            mid_hi[ea] = h.x;
+            mid_lo[ea] = l.x;
+            if (vb) {
+                mid_hi[eb] = h.y;
+                mid_lo[eb] = l.y;
+            }
+        }
+    }
+}
+
 template <bool HAS_LO>
-__global__ void __launch_bounds__(32) batch_stencil_kernel(const float* __restrict__ in_hi,
-                                                           const float* __restrict__ in_lo, float* __restrict__ mid_hi,
-                                                           float* __restrict__ mid_lo, float* __restrict__ corr,
-                                                           const float* __restrict__ fhi, const float* __restrict__ flo,
-                                                           const SolveItem* __restrict__ items,
-                                                           const TableDev* __restrict__ tables,
-                                                           const AxisFactorDev* __restrict__ fac,
-                                                           const int64_t* __restrict__ off,
-                                                           const int32_t* __restrict__ refine, int step) {
-    const SolveItem it = items[blockIdx.x];
-    if (refine[it.table] <= step) return;
-    const int lane = threadIdx.x;
-    const TableDev& t = tables[it.table];
-    const AxisDev& ax = t.ax[it.axis];
-    const AxisFactorDev& f = fac[it.table * kBatchMaxDim + it.axis];
+__global__ void __launch_bounds__(256) batch_stencil_chunk_kernel(const float* __restrict__ in_hi,
+                                                                  const float* __restrict__ in_lo,
+                                                                  float* __restrict__ mid_hi, float* __restrict__ mid_lo,
+                                                                  float* __restrict__ corr,
+                                                                  const float* __restrict__ fhi,
+                                                                  const float* __restrict__ flo,
+                                                                  const ChunkItem* __restrict__ chunks,
+                                                                  const TableDev* __restrict__ tables,
+                                                                  const AxisFactorDev* __restrict__ fac,
+                                                                  const int64_t* __restrict__ off,
+                                                                  const int32_t* __restrict__ refine, int step,
+                                                                  int pass) {
+    const ChunkItem ck = chunks[blockIdx.x];
+    if (refine[ck.table] <= step) return;
+    const TableDev& t = tables[ck.table];
+    const int axis = t.dim - 1 - pass;
+    if (axis < 0) return;
+    const AxisDev& ax = t.ax[axis];
+    const AxisFactorDev& f = fac[ck.table * kBatchMaxDim + axis];
+    const int64_t o0 = off[ck.table];
+    const bool last = axis == 0;
     // batched tables hold fewer than 2^31 values each: 32-bit index math
-    const int n = static_cast<int>(ax.n), S = static_cast<int>(ax.stride);
-    const int64_t o0 = off[it.table];
+    const int n = static_cast<int>(ax.n), S = static_cast<int>(ax.stride), start = static_cast<int>(ck.start);
     const float* ih = in_hi + o0;
     const float* il = HAS_LO ? in_lo + o0 : nullptr;
-    auto row = [&](int base, int i) {
-        const int e = base + i * S;
-        Dot2 acc{0.0f, 0.0f};
-        if (it.last) acc = Dot2{fhi[o0 + e], flo[o0 + e]};
-        dot2_band_row<HAS_LO, int>(acc, it.last ? -1.0f : 1.0f, ih, il, base, i, n, S, f.band, ax.periodic != 0,
-                                   f.sval);
-        if (it.last) {
-            corr[o0 + e] = __fadd_rn(acc.s, acc.c);
-        } else {
-            const DF v = dot2_value(acc);
-            mid_hi[o0 + e] = v.hi;
-            mid_lo[o0 + e] = v.lo;
-        }
-    };
-    if (S == 1) {
-        for (int r = 0; r < it.rows; ++r) {
-            const int base = static_cast<int>(it.line0 + r) * n;
-            for (int i = lane; i < n; i += 32) row(base, i);
-        }
+    float *mh = mid_hi + o0, *ml = mid_lo + o0, *cr = corr + o0;
+    const float *fh = fhi + o0, *fl = flo + o0;
+#define INTP_BATCH_STENCIL(B)                                                                                      \
+    case B:                                                                                                        \
+        if (ax.periodic) {                                                                                         \
+            if (last)                                                                                              \
+                stencil_chunk<B, true, HAS_LO, true>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);      \
+            else                                                                                                   \
+                stencil_chunk<B, true, HAS_LO, false>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);     \
+        } else {                                                                                                   \
+            if (last)                                                                                              \
+                stencil_chunk<B, false, HAS_LO, true>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);     \
+            else                                                                                                   \
+                stencil_chunk<B, false, HAS_LO, false>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);    \
+        }                                                                                                          \
         return;
+    switch (f.band) {
+        INTP_BATCH_STENCIL(0)
+        INTP_BATCH_STENCIL(1)
+        INTP_BATCH_STENCIL(2)
+        INTP_BATCH_STENCIL(3)
+        INTP_BATCH_STENCIL(4)
+        INTP_BATCH_STENCIL(5)
+        INTP_BATCH_STENCIL(6)
     }
-    if (lane >= it.rows) return;
-    const int l = static_cast<int>(it.line0) + lane;
-    const int o = l / S, tt = l - o * S;
-    const int base = o * n * S + tt;
-    for (int i = 0; i < n; ++i) row(base, i);
+#undef INTP_BATCH_STENCIL
 }
 
 // Element-wise passes over chunk items:
@@ -442,9 +514,9 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
             const intp_batch::Pass& p = b->pass[j];
             if (p.nitems == 0) continue;
             float** out = ping[j & 1];
-            auto k = il ? batch_stencil_kernel<true> : batch_stencil_kernel<false>;
-            k<<<static_cast<unsigned>(p.nitems), 32, 0, s>>>(ih, il, out[0], out[1], corr, fhi, flo, p.items,
-                                                             b->d_tables, b->d_fac, b->d_off, b->d_refine, step);
+            auto k = il ? batch_stencil_chunk_kernel<true> : batch_stencil_chunk_kernel<false>;
+            k<<<nch, 256, 0, s>>>(ih, il, out[0], out[1], corr, fhi, flo, b->d_chunks, b->d_tables, b->d_fac, b->d_off,
+                                  b->d_refine, step, j);
             note_launch();
             BATCH_CUDA(cudaGetLastError(), "batch residual");
             ih = out[0];

@@ -290,7 +290,7 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
         cudaError_t e = launch_line_solve_f32(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
-                                              f.dinvf, f.bottomf, f.rightf, s);
+                                              f.dinvf, f.bottomf, f.rightf, s, f.clo, f.chi);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -302,7 +302,7 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
         cudaError_t e = launch_line_solve_f64(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lower, f.upper,
-                                              f.dinv, f.bottom, f.right, s);
+                                              f.dinv, f.bottom, f.right, s, f.clo, f.chi);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -661,6 +661,8 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
         fd.sval = reinterpret_cast<const float2*>(base + o.sval);
         fd.band = (ax.stencil.width - 1) / 2;
+        fd.clo = f.const_lo;
+        fd.chi = f.const_hi;
     }
 }
 

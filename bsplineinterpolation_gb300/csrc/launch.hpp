@@ -73,12 +73,14 @@ cudaError_t launch_range_check(const TableDev& t, const double* coords, int64_t 
 // solve (solve_kernels.cu)
 // Band / cyclic-band solves of every line along one axis with the factor's
 // lower / upper bands, inverse diagonal and cyclic corner blocks.
+// Rows clo .. chi-1 of the factor are identical to row clo (taken from
+// registers in those rows; clo = chi: none).
 cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const double* lower, const double* upper, const double* dinv, const double* bottom,
-                                  const double* right, cudaStream_t s);
+                                  const double* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0);
 cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const float* lower, const float* upper, const float* dinv, const float* bottom,
-                                  const float* right, cudaStream_t s);
+                                  const float* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
 // FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),

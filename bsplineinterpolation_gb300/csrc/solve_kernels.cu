@@ -49,29 +49,15 @@ constexpr int kSolveWarps = 4;  // warps per block
 
 // Strided axis (S > 1): one thread per line; adjacent threads own adjacent
 // lines (adjacent t), so every chunk load and store of a warp is a run of
-// contiguous elements. The chunk loads stream kPrefetch chunks ahead through
-// a per-thread shared-memory ring (PrefetchStridedChunks).
-constexpr int kPrefetch = 3;
-
-template <class R>
-constexpr size_t strided_ring_bytes() {
-    return static_cast<size_t>(kPrefetch) * line_chunk<R>() * kSolveWarps * 32 * sizeof(R);
-}
-
+// contiguous elements. No shared memory: occupancy is set by registers only.
 template <class R, int P, int Q, bool CYC>
 __global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R* __restrict__ x, int64_t n,
                                                                               int64_t S, int64_t nlines,
                                                                               FactorView<R> f) {
-    extern __shared__ __align__(16) unsigned char ring_raw[];
-    constexpr int K = line_chunk<R>();
-    R* ring = reinterpret_cast<R*>(ring_raw);
-    const int nf = static_cast<int>((n + K - 1) / K);
     for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
          l += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t o = l / S, t = l - o * S;
-        PrefetchStridedChunks<R, K, kPrefetch> io{x + o * n * S + t, S, n, ring, static_cast<int>(blockDim.x),
-                                                  static_cast<int>(threadIdx.x), CYC, Q, CYC ? -1 : 0, 0, nf};
-        solve_line_chunked<R, P, Q, CYC, K>(f, io);
+        solve_line_chunked<R, P, Q, CYC, line_chunk<R>()>(f, StridedChunks<R>{x + o * n * S + t, S});
     }
 }
 
@@ -124,7 +110,7 @@ cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const Fa
         if (!vec) solve_warp_contig_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, nlines, f);
     } else {
         const int grid = grid_for(nlines, kThreads, 152 * 64);
-        solve_warp_strided_kernel<R, P, Q, CYC><<<grid, kThreads, strided_ring_bytes<R>(), s>>>(x, n, S, nlines, f);
+        solve_warp_strided_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, S, nlines, f);
     }
     note_launch();
     return cudaGetLastError();
@@ -402,15 +388,15 @@ int take_device_error(cudaStream_t s) {
 
 cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const double* lower, const double* upper, const double* dinv, const double* bottom,
-                                  const double* right, cudaStream_t s) {
-    FactorView<double> f{n, lower, upper, dinv, bottom, right};
+                                  const double* right, cudaStream_t s, int64_t clo, int64_t chi) {
+    FactorView<double> f{n, lower, upper, dinv, bottom, right, clo, chi};
     return launch_solve_r<double>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 
 cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const float* lower, const float* upper, const float* dinv, const float* bottom,
-                                  const float* right, cudaStream_t s) {
-    FactorView<float> f{n, lower, upper, dinv, bottom, right};
+                                  const float* right, cudaStream_t s, int64_t clo, int64_t chi) {
+    FactorView<float> f{n, lower, upper, dinv, bottom, right, clo, chi};
     return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 

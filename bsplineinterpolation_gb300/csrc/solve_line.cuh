@@ -13,8 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-
-#include "async_copy.cuh"
+#include <type_traits>
 
 namespace intp_gb300 {
 
@@ -26,6 +25,9 @@ struct FactorView {
     const R* dinv;    // [n]
     const R* bottom;  // [Q*n]
     const R* right;   // [P*n]
+    // rows clo .. chi-1 are identical to row clo: the substitution takes them
+    // from registers (same values, no loads); clo = chi: none
+    int64_t clo = 0, chi = 0;
 };
 
 // a * b + c with one rounding (FP32 or FP64).
@@ -207,109 +209,30 @@ struct WarpContigChunksV4 {
     }
 };
 
-// StridedChunks with the chunk loads streamed ahead through shared memory:
-// each thread keeps a ring of NB chunk buffers (cp.async element copies, one
-// commit group per chunk) and, when the substitution asks for chunk c, the
-// copies of chunks c+1 .. c+NB-1 are already in flight. The loaded values
-// and the arithmetic are those of StridedChunks; only the waiting changes
-// (the serial chain of a line no longer waits a memory latency per chunk)
-// and no registers hold data in flight.
-//
-// The substitution's request order is fixed: (cyclic only) the last Q
-// elements, the forward chunks i0 = 0, K, 2K, ..., then the back chunks
-// ending at n-1, n-1-K, .... The ring follows that order; the back chunks
-// are fetched only after the forward sweep has written the whole line (a
-// block fence orders those writes before the copies that read them back).
-// ring[slot][k][tid]: thread-fastest, so a warp's accesses to one buffer
-// element are conflict-free.
-template <class R, int K, int NB>
-struct PrefetchStridedChunks {
-    R* base;
-    int64_t S;
-    int64_t n;
-    R* ring;       // NB * K * nthreads elements
-    int nthreads;
-    int tid;
-    bool cyc_head;  // the cyclic substitution's first request (last Q elements) comes first
-    int Q;
-    // request sequence state
-    mutable int next_req;    // index of the next request in the forward+back order
-    mutable int next_issue;  // index of the next chunk to issue
-    int nf;                  // forward chunks
-    __device__ __forceinline__ int total() const { return 2 * nf; }
-    // chunk j of the sequence: [lo, lo + cnt)
-    __device__ __forceinline__ void chunk(int j, int64_t& lo, int& cnt) const {
-        if (j < nf) {
-            lo = static_cast<int64_t>(j) * K;
-            cnt = static_cast<int>(n - lo < K ? n - lo : K);
-        } else {
-            const int64_t i1 = n - 1 - static_cast<int64_t>(j - nf) * K;
-            cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
-            lo = i1 - cnt + 1;
-        }
-    }
-    __device__ __forceinline__ R* slot(int j, int k) const { return ring + ((j % NB) * K + k) * nthreads + tid; }
-    __device__ __forceinline__ void issue(int j) const {
-        int64_t lo;
-        int cnt;
-        chunk(j, lo, cnt);
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) cp_async<sizeof(R)>(slot(j, k), base + (lo + k) * S);
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-    // issue chunks up to `upto` (exclusive), forward chunks any time, back
-    // chunks once the forward sweep is done (next_req >= nf)
-    __device__ __forceinline__ void fill(int upto) const {
-        while (next_issue < upto && next_issue < total()) {
-            if (next_issue >= nf && next_req < nf) break;
-            issue(next_issue++);
-        }
-    }
-    template <int KK>
-    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[KK]) const {
-        static_assert(KK == K, "chunk size of the ring");
-        if (cyc_head && next_req < 0) {
-            // the cyclic head: a direct load of the last Q elements
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                if (k < cnt) buf[k] = base[(i0 + k) * S];
-            next_req = 0;
-            return;
-        }
-        if (next_req == nf) __threadfence_block();  // the forward writes before the back copies
-        fill(next_req + NB);
-        // wait for chunk next_req: groups complete in order, and at most
-        // next_issue - next_req - 1 later ones may stay pending
-        const int pending = next_issue - next_req - 1;
-        if (pending >= 2)
-            asm volatile("cp.async.wait_group 2;" ::: "memory");
-        else if (pending == 1)
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        else
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) buf[k] = *slot(next_req, k);
-        ++next_req;
-    }
-    template <int KK>
-    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[KK]) const {
-#pragma unroll
-        for (int k = 0; k < KK; ++k)
-            if (k < cnt) base[(i0 + k) * S] = buf[k];
-    }
-};
-
 // Substitution of one line with the band / cyclic-band factor, walking the
 // line in chunks of K elements (K loads in flight per lane, the values of a
 // chunk held in registers). Every step is the same sequence of roundings as
 // the textbook recurrences written out with explicit FMAs, so all callers
 // (strided lines, transposed contiguous lines, batched items) agree bit for
 // bit.
-template <class R, int P, int Q, bool CYC, int K, class Io>
+// CONST_ROWS: take the factor's constant interior rows (FactorView::clo ..
+// chi) from registers. It pays where one lane walks a long line alone (the
+// factor loads of each chunk would wait on L2); where a warp's lanes share
+// the factor row, the loads are broadcasts and the registers cost occupancy.
+template <class R, int P, int Q, bool CYC, int K, class Io, bool CONST_ROWS = false>
 __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const Io& io) {
     const int64_t n = f.n;
+    // the factor's constant interior row, in registers (non-cyclic factors);
+    // a chunk that lies inside [clo, chi) reads its rows from here
+    const bool has_const = CONST_ROWS && !CYC && f.chi > f.clo;
+    R cl[CONST_ROWS && P > 0 ? P : 1], cu[CONST_ROWS && Q > 0 ? Q : 1], cd = 0;
+    if (has_const) {
+#pragma unroll
+        for (int kk = 0; kk < P; ++kk) cl[kk] = __ldg(f.lower + f.clo * P + kk);
+#pragma unroll
+        for (int kk = 0; kk < Q; ++kk) cu[kk] = __ldg(f.upper + f.clo * Q + kk);
+        cd = __ldg(f.dinv + f.clo);
+    }
     // ---- forward: y = L^{-1} x ----
     R win[P > 0 ? P : 1];  // y_{i-P} .. y_{i-1}
 #pragma unroll
@@ -321,10 +244,9 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
 #pragma unroll
         for (int r = 0; r < Q; ++r) acc[r] = tmp[r];
     }
-    for (int64_t i0 = 0; i0 < n; i0 += K) {
-        const int cnt = static_cast<int>(n - i0 < K ? n - i0 : K);
-        R buf[K];
-        io.load(i0, cnt, buf);
+    // one chunk's forward rows; CST: every row of the chunk is the constant row
+    auto forward = [&](auto cst, int64_t i0, int cnt, R (&buf)[K]) {
+        constexpr bool CST = decltype(cst)::value;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if (k < cnt) {
@@ -337,7 +259,8 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
                         if (i == n - Q + r) v = acc[r];
                 }
 #pragma unroll
-                for (int kk = 0; kk < P; ++kk) v = fma_r(-__ldg(f.lower + i * P + kk), win[kk], v);
+                for (int kk = 0; kk < P; ++kk)
+                    v = fma_r(-(CST ? cl[kk] : __ldg(f.lower + i * P + kk)), win[kk], v);
                 if (CYC && i < n - P - 1) {
 #pragma unroll
                     for (int r = 0; r < Q; ++r) acc[r] = fma_r(-__ldg(f.bottom + r * n + i), v, acc[r]);
@@ -348,6 +271,19 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
                 if (P > 0) win[P - 1] = v;
             }
         }
+    };
+    for (int64_t i0 = 0; i0 < n; i0 += K) {
+        const int cnt = static_cast<int>(n - i0 < K ? n - i0 : K);
+        R buf[K];
+        io.load(i0, cnt, buf);
+        if constexpr (CONST_ROWS) {
+            if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
+                forward(std::true_type{}, i0, cnt, buf);
+                io.store(i0, cnt, buf);
+                continue;
+            }
+        }
+        forward(std::false_type{}, i0, cnt, buf);
         io.store(i0, cnt, buf);
     }
     // ---- back: x = U^{-1} y ----
@@ -357,11 +293,8 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
     R tail[P > 0 ? P : 1];  // cyclic: z_{n-P} .. z_{n-1}
 #pragma unroll
     for (int k = 0; k < P; ++k) tail[k] = 0;
-    for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
-        const int cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
-        const int64_t i0 = i1 - cnt + 1;
-        R buf[K];
-        io.load(i0, cnt, buf);
+    auto back = [&](auto cst, int64_t i0, int cnt, R (&buf)[K]) {
+        constexpr bool CST = decltype(cst)::value;
 #pragma unroll
         for (int k = K - 1; k >= 0; --k) {
             if (k < cnt) {
@@ -373,8 +306,9 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
                         if (n - P + r > i + Q) v = fma_r(-__ldg(f.right + r * n + i), tail[r], v);
                 }
 #pragma unroll
-                for (int kk = Q - 1; kk >= 0; --kk) v = fma_r(-__ldg(f.upper + i * Q + kk), zw[kk], v);
-                v *= __ldg(f.dinv + i);
+                for (int kk = Q - 1; kk >= 0; --kk)
+                    v = fma_r(-(CST ? cu[kk] : __ldg(f.upper + i * Q + kk)), zw[kk], v);
+                v *= CST ? cd : __ldg(f.dinv + i);
                 buf[k] = v;
                 if (CYC) {
 #pragma unroll
@@ -386,6 +320,20 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
                 if (Q > 0) zw[0] = v;
             }
         }
+    };
+    for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
+        const int cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
+        const int64_t i0 = i1 - cnt + 1;
+        R buf[K];
+        io.load(i0, cnt, buf);
+        if constexpr (CONST_ROWS) {
+            if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
+                back(std::true_type{}, i0, cnt, buf);
+                io.store(i0, cnt, buf);
+                continue;
+            }
+        }
+        back(std::false_type{}, i0, cnt, buf);
         io.store(i0, cnt, buf);
     }
 }

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 namespace intp_gb300 {
 
@@ -123,6 +124,29 @@ LineFactor line_factor_from(const BandStore& lu) {
         for (int64_t r = 0; r < p; ++r) {
             const int64_t j = n - p + r;
             for (int64_t i = 0; i < j - q; ++i) f.right[r * n + i] = lu.at_side(i, j);
+        }
+    }
+    // the longest run of rows identical to its first row (bitwise)
+    if (!lu.cyclic && n > 0) {
+        auto same = [&](int64_t a, int64_t b) {
+            if (std::memcmp(&f.dinv[a], &f.dinv[b], sizeof(double)) != 0) return false;
+            if (p > 0 && std::memcmp(&f.lower[a * p], &f.lower[b * p], sizeof(double) * p) != 0) return false;
+            if (q > 0 && std::memcmp(&f.upper[a * q], &f.upper[b * q], sizeof(double) * q) != 0) return false;
+            return true;
+        };
+        int64_t best_lo = 0, best_hi = 0, lo = 0;
+        for (int64_t i = 1; i <= n; ++i) {
+            if (i == n || !same(lo, i)) {
+                if (i - lo > best_hi - best_lo) {
+                    best_lo = lo;
+                    best_hi = i;
+                }
+                lo = i;
+            }
+        }
+        if (best_hi - best_lo >= 2) {
+            f.const_lo = best_lo;
+            f.const_hi = best_hi;
         }
     }
     return f;

@@ -65,6 +65,10 @@ struct LineFactor {
     int p = 0, q = 0;
     bool cyclic = false;
     std::vector<double> lower, upper, dinv, bottom, right;
+    // rows const_lo .. const_hi-1 are bit-identical to row const_lo (the LU
+    // rows of a uniform axis converge to one row away from its ends);
+    // non-cyclic factors only, an empty range otherwise
+    int64_t const_lo = 0, const_hi = 0;
 };
 
 // Row layout of a factored band matrix (above) for the GPU line solves.

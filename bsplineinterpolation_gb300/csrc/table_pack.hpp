@@ -42,6 +42,7 @@ struct AxisFactorDev {
     const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
     const float2* sval;
     int band;
+    int64_t clo, chi;  // rows identical to row clo (LineFactor::const_lo/const_hi)
 };
 
 // Arena offsets of one table's per-axis arrays.
