@@ -661,8 +661,8 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
         fd.sval = reinterpret_cast<const float2*>(base + o.sval);
         fd.band = (ax.stencil.width - 1) / 2;
-        fd.clo = f.const_lo;
-        fd.chi = f.const_hi;
+        fd.clo = ax.factor.const_lo;
+        fd.chi = ax.factor.const_hi;
     }
 }
 
