@@ -98,6 +98,7 @@ SIGNATURES = {
     "intp_stream_synchronize": (C.c_int, [_P]),
     "intp_debug_set_wait_limit": (C.c_int, [C.c_uint32]),
     "intp_debug_fail_allocations": (C.c_int, [C.c_int32]),
+    "intp_debug_set_segment_warmup": (C.c_int, [C.c_int32]),
     "intp_last_error": (C.c_char_p, []),
     "intp_launch_count": (C.c_uint64, []),
     "intp_bandlu_create": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P,

@@ -113,36 +113,80 @@ __device__ __forceinline__ FactorView<R> factor_view(const AxisFactorDev& f, int
 
 template <>
 __device__ __forceinline__ FactorView<float> factor_view<float>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf, f.clo, f.chi};
+    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf, f.clo32, f.chi32, f.zside32};
 }
 
 template <>
 __device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right, f.clo, f.chi};
+    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right, f.clo, f.chi, f.zside};
 }
 
 // Lines are walked in chunks of this many elements (registers per lane).
 constexpr int kBatchChunk = 16;
 
-template <class R, class Line, bool CONST_ROWS = false>
+template <class R, class Line>
 __device__ __forceinline__ void solve_dispatch(int p, bool cyc, const FactorView<R>& fv, const Line& line) {
+    constexpr int K = kBatchChunk;
     if (cyc) {
         switch (p) {
-            case 0: solve_line_chunked<R, 0, 0, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-            case 1: solve_line_chunked<R, 1, 1, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-            case 2: solve_line_chunked<R, 2, 2, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-            case 3: solve_line_chunked<R, 3, 3, true, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+            case 0: solve_line_chunked<R, 0, 0, true, K, Line>(fv, line); return;
+            case 1: solve_line_chunked<R, 1, 1, true, K, Line>(fv, line); return;
+            case 2: solve_line_chunked<R, 2, 2, true, K, Line>(fv, line); return;
+            case 3: solve_line_chunked<R, 3, 3, true, K, Line>(fv, line); return;
         }
         return;
     }
     switch (p) {
-        case 0: solve_line_chunked<R, 0, 0, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 1: solve_line_chunked<R, 1, 1, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 2: solve_line_chunked<R, 2, 2, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 3: solve_line_chunked<R, 3, 3, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 4: solve_line_chunked<R, 4, 4, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 5: solve_line_chunked<R, 5, 5, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
-        case 6: solve_line_chunked<R, 6, 6, false, kBatchChunk, Line, CONST_ROWS>(fv, line); return;
+        case 0: solve_line_chunked<R, 0, 0, false, K, Line>(fv, line); return;
+        case 1: solve_line_chunked<R, 1, 1, false, K, Line>(fv, line); return;
+        case 2: solve_line_chunked<R, 2, 2, false, K, Line>(fv, line); return;
+        case 3: solve_line_chunked<R, 3, 3, false, K, Line>(fv, line); return;
+        case 4: solve_line_chunked<R, 4, 4, false, K, Line>(fv, line); return;
+        case 5: solve_line_chunked<R, 5, 5, false, K, Line>(fv, line); return;
+        case 6: solve_line_chunked<R, 6, 6, false, K, Line>(fv, line); return;
+    }
+}
+
+// A line of at least this many elements that is a warp's only line is solved
+// by the whole warp (solve_line_warp).
+constexpr int64_t kWarpLineMin = 128;
+
+// Warm-up rows of the warp-segmented substitution: enough for the zero
+// state's error to fall below the last bit in FP32 / FP64.
+template <class R>
+constexpr int warm_rows() {
+    return sizeof(R) == 4 ? 64 : 128;
+}
+
+}  // namespace
+
+namespace intp_gb300 {
+INTP_DEFINE_WARM_CAP_SETTER(set_warm_cap_batch)
+}  // namespace intp_gb300
+
+namespace {
+
+template <class R>
+__device__ __forceinline__ void solve_dispatch_warp(int p, bool cyc, const FactorView<R>& fv, const LineRef<R>& line,
+                                                    int lane) {
+    constexpr int W = warm_rows<R>();
+    if (cyc) {
+        switch (p) {
+            case 0: solve_line_warp<R, 0, 0, true, W, true>(fv, line, lane); return;
+            case 1: solve_line_warp<R, 1, 1, true, W, true>(fv, line, lane); return;
+            case 2: solve_line_warp<R, 2, 2, true, W, true>(fv, line, lane); return;
+            case 3: solve_line_warp<R, 3, 3, true, W, true>(fv, line, lane); return;
+        }
+        return;
+    }
+    switch (p) {
+        case 0: solve_line_warp<R, 0, 0, false, W, true>(fv, line, lane); return;
+        case 1: solve_line_warp<R, 1, 1, false, W, true>(fv, line, lane); return;
+        case 2: solve_line_warp<R, 2, 2, false, W, true>(fv, line, lane); return;
+        case 3: solve_line_warp<R, 3, 3, false, W, true>(fv, line, lane); return;
+        case 4: solve_line_warp<R, 4, 4, false, W, true>(fv, line, lane); return;
+        case 5: solve_line_warp<R, 5, 5, false, W, true>(fv, line, lane); return;
+        case 6: solve_line_warp<R, 6, 6, false, W, true>(fv, line, lane); return;
     }
 }
 
@@ -174,14 +218,10 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) tile[r * pitch + k] = src[static_cast<int64_t>(r) * ni + k];
         __syncwarp();
-        // a staged line walked by one lane (1D tables): the factor's constant
-        // rows come from registers
-        if (lane < it.rows) {
-            if (it.rows == 1)
-                solve_dispatch<R, SmemChunks<R>, true>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
-            else
-                solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
-        }
+        if (it.rows == 1 && n >= kWarpLineMin)
+            solve_dispatch_warp<R>(band.x, band.y != 0, fv, LineRef<R>{tile, 1}, lane);
+        else if (lane < it.rows)
+            solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
         __syncwarp();
         for (int r = 0; r < it.rows; ++r)
             for (int k = lane; k < ni; k += 32) src[static_cast<int64_t>(r) * ni + k] = tile[r * pitch + k];

@@ -96,7 +96,7 @@ intp_status cuda_fail(cudaError_t e, const char* what) {
 
 std::vector<float> to_f32(const std::vector<double>& v) {
     std::vector<float> r(v.size());
-    for (size_t i = 0; i < v.size(); ++i) r[i] = static_cast<float>(v[i]);
+    for (size_t i = 0; i < v.size(); ++i) r[i] = factor_f32(v[i]);
     return r;
 }
 
@@ -290,7 +290,7 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
         cudaError_t e = launch_line_solve_f32(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerf, f.upperf,
-                                              f.dinvf, f.bottomf, f.rightf, s, f.clo, f.chi);
+                                              f.dinvf, f.bottomf, f.rightf, s, f.clo32, f.chi32, f.zside32);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -302,7 +302,7 @@ cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
         const AxisFactorDev& f = t->fac[a];
         const LineFactor& lf = t->model.axis[a].factor;
         cudaError_t e = launch_line_solve_f64(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lower, f.upper,
-                                              f.dinv, f.bottom, f.right, s, f.clo, f.chi);
+                                              f.dinv, f.bottom, f.right, s, f.clo, f.chi, f.zside);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -663,6 +663,10 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.band = (ax.stencil.width - 1) / 2;
         fd.clo = ax.factor.const_lo;
         fd.chi = ax.factor.const_hi;
+        fd.clo32 = ax.factor.const_lo32;
+        fd.chi32 = ax.factor.const_hi32;
+        fd.zside = ax.factor.zside;
+        fd.zside32 = ax.factor.zside32;
     }
 }
 
@@ -955,6 +959,13 @@ intp_status intp_locate_binned(const intp_table* t, const double* coords, int64_
 intp_status intp_debug_set_wait_limit(uint32_t probes) {
     INTP_CUDA(set_wait_probes_bin_d3(probes), "cudaMemcpyToSymbol(wait probes)");
     INTP_CUDA(set_wait_probes_bin_d12(probes), "cudaMemcpyToSymbol(wait probes)");
+    return INTP_OK;
+}
+
+intp_status intp_debug_set_segment_warmup(int32_t rows) {
+    if (rows < -1) return fail(INTP_ERR_INVALID_ARGUMENT, "rows must be >= -1");
+    INTP_CUDA(set_warm_cap_solve(rows), "cudaMemcpyToSymbol(warm-up cap)");
+    INTP_CUDA(set_warm_cap_batch(rows), "cudaMemcpyToSymbol(warm-up cap)");
     return INTP_OK;
 }
 

@@ -60,6 +60,9 @@ int take_device_error_bin_d3(cudaStream_t s);
 // Diagnostics: probes of the binned evaluation's tile wait (0 = normal wait).
 cudaError_t set_wait_probes_bin_d12(uint32_t probes);
 cudaError_t set_wait_probes_bin_d3(uint32_t probes);
+// Caps the warm-up of the warp-segmented line solves (test hook; -1: none).
+cudaError_t set_warm_cap_solve(int rows);
+cudaError_t set_warm_cap_batch(int rows);
 // Bucket geometry of the binned evaluation for a table: compile-time bucket
 // sizes per dimension (bucket_log2); smem_buckets = 0 when the table has too
 // many buckets or too many knots for the binned path.
@@ -77,10 +80,12 @@ cudaError_t launch_range_check(const TableDev& t, const double* coords, int64_t 
 // registers in those rows; clo = chi: none).
 cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const double* lower, const double* upper, const double* dinv, const double* bottom,
-                                  const double* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0);
+                                  const double* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0,
+                                  int64_t zside = INT64_MAX);
 cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const float* lower, const float* upper, const float* dinv, const float* bottom,
-                                  const float* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0);
+                                  const float* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0,
+                                  int64_t zside = INT64_MAX);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
 // FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),

@@ -47,6 +47,18 @@ constexpr int line_chunk() {
 }
 constexpr int kSolveWarps = 4;  // warps per block
 
+// Lines of at least kWarpLineMin elements, fewer than kWarpLineMaxLines of
+// them (under one line per lane on every SM), are solved a warp per line.
+constexpr int64_t kWarpLineMin = 128;
+constexpr int64_t kWarpLineMaxLines = 152 * 32;
+
+// Warm-up rows of the warp-segmented substitution: enough for the zero
+// state's error to fall below the last bit in FP32 / FP64.
+template <class R>
+constexpr int warm_rows() {
+    return sizeof(R) == 4 ? 64 : 128;
+}
+
 // Strided axis (S > 1): one thread per line; adjacent threads own adjacent
 // lines (adjacent t), so every chunk load and store of a warp is a run of
 // contiguous elements. No shared memory: occupancy is set by registers only.
@@ -95,11 +107,27 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_v4_kern
     }
 }
 
+// Few long lines: one warp per line, the line cut into 32 segments
+// (solve_line_warp; the same values as one lane walking it).
+template <class R, int P, int Q, bool CYC>
+__global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_line_kernel(R* __restrict__ x, int64_t n, int64_t S,
+                                                                           int64_t nlines, FactorView<R> f) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t l = blockIdx.x * static_cast<int64_t>(kSolveWarps) + warp; l < nlines;
+         l += static_cast<int64_t>(gridDim.x) * kSolveWarps) {
+        const int64_t o = l / S, t = l - o * S;
+        solve_line_warp<R, P, Q, CYC, warm_rows<R>(), true>(f, LineRef<R>{x + o * n * S + t, S}, lane);
+    }
+}
+
 template <class R, int P, int Q, bool CYC>
 cudaError_t launch_solve_pq(R* x, int64_t n, int64_t S, int64_t nlines, const FactorView<R>& f,
                             cudaStream_t s) {
     constexpr int kThreads = kSolveWarps * 32;
-    if (S == 1) {
+    if (n >= kWarpLineMin && nlines < kWarpLineMaxLines) {
+        const int grid = grid_for(nlines, kSolveWarps, 152 * 64);
+        solve_warp_line_kernel<R, P, Q, CYC><<<grid, kThreads, 0, s>>>(x, n, S, nlines, f);
+    } else if (S == 1) {
         const int64_t groups = (nlines + 31) / 32;
         const int grid = grid_for(groups, kSolveWarps, 152 * 64);
         bool vec = false;
@@ -377,6 +405,8 @@ __global__ void __launch_bounds__(256) correct_kernel(float* __restrict__ c, flo
 
 }  // namespace
 
+INTP_DEFINE_WARM_CAP_SETTER(set_warm_cap_solve)
+
 int take_device_error(cudaStream_t s) {
     int v = 0, zero = 0;
     if (cudaMemcpyFromSymbolAsync(&v, g_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -388,15 +418,17 @@ int take_device_error(cudaStream_t s) {
 
 cudaError_t launch_line_solve_f64(double* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const double* lower, const double* upper, const double* dinv, const double* bottom,
-                                  const double* right, cudaStream_t s, int64_t clo, int64_t chi) {
-    FactorView<double> f{n, lower, upper, dinv, bottom, right, clo, chi};
+                                  const double* right, cudaStream_t s, int64_t clo, int64_t chi,
+                                  int64_t zside) {
+    FactorView<double> f{n, lower, upper, dinv, bottom, right, clo, chi, zside};
     return launch_solve_r<double>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 
 cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
                                   const float* lower, const float* upper, const float* dinv, const float* bottom,
-                                  const float* right, cudaStream_t s, int64_t clo, int64_t chi) {
-    FactorView<float> f{n, lower, upper, dinv, bottom, right, clo, chi};
+                                  const float* right, cudaStream_t s, int64_t clo, int64_t chi,
+                                  int64_t zside) {
+    FactorView<float> f{n, lower, upper, dinv, bottom, right, clo, chi, zside};
     return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 

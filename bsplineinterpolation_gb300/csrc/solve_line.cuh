@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <climits>
 #include <type_traits>
 
 namespace intp_gb300 {
@@ -28,6 +29,9 @@ struct FactorView {
     // rows clo .. chi-1 are identical to row clo: the substitution takes them
     // from registers (same values, no loads); clo = chi: none
     int64_t clo = 0, chi = 0;
+    // cyclic: the bottom side-band entries of rows zside .. n-P-2 are all
+    // zero (INT64_MAX: not known)
+    int64_t zside = INT64_MAX;
 };
 
 // a * b + c with one rounding (FP32 or FP64).
@@ -335,6 +339,334 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
         }
         back(std::false_type{}, i0, cnt, buf);
         io.store(i0, cnt, buf);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-segmented substitution of one line (all 32 lanes of a warp call).
+//
+// Each sweep's rows are cut into 32 segments, one per lane. A lane runs the
+// recurrence over the W rows before its segment from a zero state, then over
+// its segment, writing it. The zero state's error decays geometrically (the
+// factor's recurrences are contractions for B-spline collocation: about
+// 0.27 per row at order 3, 0.6 at order 7), and once P consecutive values
+// equal the serial sweep's bit for bit, every later value does too (the
+// same operations on the same operands). A lane then checks exactly that:
+// its warm-up values at the P rows before its segment against the values
+// its neighbour wrote there. A lane whose check fails is recomputed from
+// its neighbour's (exact) values, lowest lane first, and the next lane is
+// checked again. The result therefore equals the serial sweep's
+// (solve_line_chunked) bit for bit, whatever W is; W only sets how rarely a
+// segment is recomputed (64 rows in FP32 and 128 in FP64 lock every order;
+// a host simulation of orders 1..7 locked within 47 rows in FP32).
+//
+// Cyclic factors: the forward segments cover rows 0 .. n-Q-1; the bottom
+// rows' side-band sums are then formed by one lane in row order over the
+// rows with nonzero side-band entries (FactorView::zside onwards they are
+// +0, whose products leave a finite nonzero sum unchanged; where that does
+// not hold, the whole row range is walked), and the last Q rows follow
+// serially. The back sweep first computes the last P rows serially (their
+// values are the side-band operands of every other row), then the
+// segments cover rows 0 .. n-P-1.
+// ---------------------------------------------------------------------------
+
+// Test hook (one copy per translation unit): when >= 0, solve_line_warp
+// warms up over at most this many rows, so that its recompute path runs.
+static __device__ int g_warm_rows_cap = -1;
+
+#define INTP_DEFINE_WARM_CAP_SETTER(NAME)                                                     \
+    cudaError_t NAME(int rows) {                                                               \
+        return cudaMemcpyToSymbol(g_warm_rows_cap, &rows, sizeof(int), 0, cudaMemcpyHostToDevice); \
+    }
+
+template <class R>
+__device__ __forceinline__ bool bits_equal(R a, R b) {
+    if constexpr (sizeof(R) == 4)
+        return __float_as_uint(a) == __float_as_uint(b);
+    else
+        return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// Element i of a line at base[i * S].
+template <class R>
+struct LineRef {
+    R* base;
+    int64_t S;
+    __device__ __forceinline__ R ld(int64_t i) const { return base[i * S]; }
+    __device__ __forceinline__ void st(int64_t i, R v) const { base[i * S] = v; }
+};
+
+// Factor rows of one line, from memory or (rows clo .. chi-1 with
+// CONST_ROWS) from registers.
+template <class R, int P, int Q, bool CYC, bool CONST_ROWS>
+struct FactorRows {
+    static constexpr int P1 = P > 0 ? P : 1, Q1 = Q > 0 ? Q : 1;
+    const FactorView<R>& f;
+    bool has_const;
+    R cl[P1], cu[Q1], cd, cb[Q1], cr[P1];
+    __device__ __forceinline__ explicit FactorRows(const FactorView<R>& fv) : f(fv), cd(0) {
+        has_const = CONST_ROWS && f.chi > f.clo;
+        if (has_const) {
+#pragma unroll
+            for (int kk = 0; kk < P; ++kk) cl[kk] = __ldg(f.lower + f.clo * P + kk);
+#pragma unroll
+            for (int kk = 0; kk < Q; ++kk) cu[kk] = __ldg(f.upper + f.clo * Q + kk);
+            cd = __ldg(f.dinv + f.clo);
+            if (CYC) {
+#pragma unroll
+                for (int r = 0; r < Q; ++r) cb[r] = __ldg(f.bottom + r * f.n + f.clo);
+#pragma unroll
+                for (int r = 0; r < P; ++r) cr[r] = __ldg(f.right + r * f.n + f.clo);
+            }
+        }
+    }
+    __device__ __forceinline__ bool in_const(int64_t i) const { return has_const && i >= f.clo && i < f.chi; }
+    __device__ __forceinline__ void lower(int64_t i, R (&l)[P1]) const {
+        const bool c = in_const(i);
+#pragma unroll
+        for (int kk = 0; kk < P; ++kk) l[kk] = c ? cl[kk] : __ldg(f.lower + i * P + kk);
+    }
+    __device__ __forceinline__ void upper(int64_t i, R (&u)[Q1], R& d, R (&rr)[P1]) const {
+        const bool c = in_const(i);
+#pragma unroll
+        for (int kk = 0; kk < Q; ++kk) u[kk] = c ? cu[kk] : __ldg(f.upper + i * Q + kk);
+        d = c ? cd : __ldg(f.dinv + i);
+        if (CYC) {
+#pragma unroll
+            for (int r = 0; r < P; ++r) rr[r] = c ? cr[r] : __ldg(f.right + r * f.n + i);
+        }
+    }
+};
+
+// One forward row (without the cyclic side-band sums): v = x_i - L(i, i-P ..
+// i-1) . win, in solve_line_chunked's order; win shifts in v.
+template <class R, int P, int Q, bool CYC, bool CONST_ROWS>
+__device__ __forceinline__ R forward_row(const FactorRows<R, P, Q, CYC, CONST_ROWS>& fr, int64_t i, R v,
+                                         R (&win)[P > 0 ? P : 1]) {
+    R l[P > 0 ? P : 1];
+    fr.lower(i, l);
+#pragma unroll
+    for (int kk = 0; kk < P; ++kk) v = fma_r(-l[kk], win[kk], v);
+#pragma unroll
+    for (int kk = 0; kk + 1 < P; ++kk) win[kk] = win[kk + 1];
+    if (P > 0) win[P - 1] = v;
+    return v;
+}
+
+// One back row: the right side band against tail (cyclic), the band against
+// zw, times dinv; zw shifts in the result.
+template <class R, int P, int Q, bool CYC, bool CONST_ROWS>
+__device__ __forceinline__ R back_row(const FactorRows<R, P, Q, CYC, CONST_ROWS>& fr, int64_t i, R v,
+                                      R (&zw)[Q > 0 ? Q : 1], const R (&tail)[P > 0 ? P : 1]) {
+    constexpr int P1 = P > 0 ? P : 1, Q1 = Q > 0 ? Q : 1;
+    R u[Q1], d, rr[P1];
+    fr.upper(i, u, d, rr);
+    const int64_t n = fr.f.n;
+    if (CYC) {
+#pragma unroll
+        for (int r = P - 1; r >= 0; --r)
+            if (n - P + r > i + Q) v = fma_r(-rr[r], tail[r], v);
+    }
+#pragma unroll
+    for (int kk = Q - 1; kk >= 0; --kk) v = fma_r(-u[kk], zw[kk], v);
+    v *= d;
+#pragma unroll
+    for (int kk = Q - 1; kk > 0; --kk) zw[kk] = zw[kk - 1];
+    if (Q > 0) zw[0] = v;
+    return v;
+}
+
+template <class R, int N>
+__device__ __forceinline__ bool states_equal(const R (&a)[N], const R (&b)[N], int count) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < N; ++k) ok = ok && (k >= count || bits_equal(a[k], b[k]));
+    return ok;
+}
+
+template <class R, int P, int Q, bool CYC, int W, bool CONST_ROWS = false, class Line = LineRef<R>>
+__device__ __forceinline__ void solve_line_warp(const FactorView<R>& f, const Line& x, int lane) {
+    constexpr int P1 = P > 0 ? P : 1, Q1 = Q > 0 ? Q : 1;
+    constexpr unsigned kAll = 0xffffffffu;
+    const int64_t n = f.n;
+    if (n <= 0) return;
+    const FactorRows<R, P, Q, CYC, CONST_ROWS> fr(f);
+    int64_t Wr = W;
+    {
+        const int cap = g_warm_rows_cap;
+        if (cap >= 0 && cap < W) Wr = cap;
+    }
+    // segment length: odd, so the 32 lanes' rows of one step fall in
+    // distinct shared-memory banks
+    auto seg_len = [](int64_t m) {
+        const int64_t L = (m + 31) / 32;
+        return L | 1;
+    };
+
+    // ---- forward: rows 0 .. nf-1 in segments ----
+    // Phase A: warm-up and segment without stores, giving the state entering
+    // the segment (start) and the state leaving it (end). Lane order fixes
+    // the starts: lane 0 and any lane whose warm-up began at row 0 start
+    // exactly; a later lane's start is exact when it equals, bit for bit,
+    // its (exact) predecessor's end, and is replaced by that end otherwise.
+    // Phase B: every lane runs its segment from its start, storing it.
+    const int64_t nf = CYC ? n - Q : n;
+    {
+        const int64_t L = seg_len(nf);
+        const int64_t a = lane * L < nf ? lane * L : nf, b = a + L < nf ? a + L : nf;
+        const int64_t s0 = a - Wr > 0 ? a - Wr : 0;
+        R start[P1], end[P1];
+#pragma unroll
+        for (int k = 0; k < P1; ++k) start[k] = 0;
+#pragma unroll 4
+        for (int64_t i = s0; i < a; ++i) forward_row(fr, i, x.ld(i), start);
+        auto run = [&]() {
+#pragma unroll
+            for (int k = 0; k < P1; ++k) end[k] = start[k];
+#pragma unroll 4
+            for (int64_t i = a; i < b; ++i) forward_row(fr, i, x.ld(i), end);
+        };
+        run();
+        auto mismatch = [&]() {
+            R prev[P1];
+#pragma unroll
+            for (int k = 0; k < P1; ++k) prev[k] = __shfl_up_sync(kAll, end[k], 1);
+            return s0 > 0 && a < b && !states_equal(start, prev, P);
+        };
+        unsigned bad = __ballot_sync(kAll, mismatch());
+        while (bad) {
+            const int fl = __ffs(bad) - 1;
+            R prev[P1];
+#pragma unroll
+            for (int k = 0; k < P1; ++k) prev[k] = __shfl_sync(kAll, end[k], fl > 0 ? fl - 1 : 0);
+            if (lane == fl) {
+#pragma unroll
+                for (int k = 0; k < P1; ++k) start[k] = prev[k];
+                run();
+            }
+            bad &= ~(1u << fl);
+            const bool m = mismatch();
+            const unsigned again = __ballot_sync(kAll, lane == fl + 1 && m);
+            bad = (bad & ~(2u << fl)) | again;
+        }
+        {
+            R win[P1];
+#pragma unroll
+            for (int k = 0; k < P1; ++k) win[k] = start[k];
+#pragma unroll 4
+            for (int64_t i = a; i < b; ++i) x.st(i, forward_row(fr, i, x.ld(i), win));
+        }
+        __syncwarp();
+    }
+    if (CYC) {
+        // the bottom rows' side-band sums in row order, then rows n-Q .. n-1
+        const int64_t nb = n - P - 1;  // rows feeding the sums: 0 .. nb-1
+        const int64_t z = f.zside < nb ? f.zside : nb;
+        // the +0 entries of rows z .. nb-1 leave a sum unchanged unless the
+        // sum is 0 or not finite, or a row value is not finite
+        bool odd = false;
+        for (int64_t i = z + lane; i < nb; i += 32) {
+            const R v = x.ld(i);
+            odd = odd || !(v - v == R(0));
+        }
+        odd = __any_sync(kAll, odd);
+        if (lane == 0) {
+            R acc[Q1];
+#pragma unroll
+            for (int r = 0; r < Q; ++r) acc[r] = x.ld(n - Q + r);
+            for (int64_t i = 0; i < z; ++i) {
+                const R v = x.ld(i);
+#pragma unroll
+                for (int r = 0; r < Q; ++r) acc[r] = fma_r(-__ldg(f.bottom + r * n + i), v, acc[r]);
+            }
+#pragma unroll
+            for (int r = 0; r < Q; ++r) odd = odd || !(acc[r] != R(0) && acc[r] - acc[r] == R(0));
+            if (odd) {
+                for (int64_t i = z; i < nb; ++i) {
+                    const R v = x.ld(i);
+#pragma unroll
+                    for (int r = 0; r < Q; ++r) acc[r] = fma_r(-__ldg(f.bottom + r * n + i), v, acc[r]);
+                }
+            }
+            R win[P1];
+#pragma unroll
+            for (int k = 0; k < P1; ++k) win[k] = 0;
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+                if (nf - P + k >= 0) win[k] = x.ld(nf - P + k);
+#pragma unroll
+            for (int r = 0; r < Q; ++r) x.st(nf + r, forward_row(fr, nf + r, acc[r], win));
+        }
+        __syncwarp();
+    }
+
+    // ---- back: rows nk-1 .. 0 in segments, the same two phases from the
+    // top lane down ----
+    R tail[P1];  // cyclic: x_{n-P} .. x_{n-1}
+#pragma unroll
+    for (int k = 0; k < P1; ++k) tail[k] = 0;
+    R top[Q1];  // the state entering row nk-1 from above
+#pragma unroll
+    for (int k = 0; k < Q1; ++k) top[k] = 0;
+    const int64_t nk = CYC ? n - P : n;
+    if (CYC) {
+        if (lane == 0) {
+            R zw[Q1];
+#pragma unroll
+            for (int k = 0; k < Q1; ++k) zw[k] = 0;
+            for (int64_t i = n - 1; i >= nk; --i) x.st(i, back_row(fr, i, x.ld(i), zw, tail));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < P; ++r) tail[r] = x.ld(n - P + r);
+#pragma unroll
+        for (int kk = 0; kk < Q; ++kk) top[kk] = x.ld(nk + kk);
+    }
+    {
+        const int64_t L = seg_len(nk);
+        const int64_t a = lane * L < nk ? lane * L : nk, b = a + L < nk ? a + L : nk;
+        const int64_t t0 = b + Wr < nk ? b + Wr : nk;  // warm-up rows b .. t0-1
+        R start[Q1], end[Q1];
+#pragma unroll
+        for (int k = 0; k < Q1; ++k) start[k] = t0 == nk ? top[k] : R(0);
+#pragma unroll 4
+        for (int64_t i = t0 - 1; i >= b; --i) back_row(fr, i, x.ld(i), start, tail);
+        auto run = [&]() {
+#pragma unroll
+            for (int k = 0; k < Q1; ++k) end[k] = start[k];
+#pragma unroll 4
+            for (int64_t i = b - 1; i >= a; --i) back_row(fr, i, x.ld(i), end, tail);
+        };
+        run();
+        auto mismatch = [&]() {
+            R next[Q1];
+#pragma unroll
+            for (int k = 0; k < Q1; ++k) next[k] = __shfl_down_sync(kAll, end[k], 1);
+            return t0 < nk && a < b && !states_equal(start, next, Q);
+        };
+        unsigned bad = __ballot_sync(kAll, mismatch());
+        while (bad) {
+            const int fl = 31 - __clz(bad);
+            R next[Q1];
+#pragma unroll
+            for (int k = 0; k < Q1; ++k) next[k] = __shfl_sync(kAll, end[k], fl < 31 ? fl + 1 : 31);
+            if (lane == fl) {
+#pragma unroll
+                for (int k = 0; k < Q1; ++k) start[k] = next[k];
+                run();
+            }
+            bad &= ~(1u << fl);
+            const bool m = mismatch();
+            const unsigned again = __ballot_sync(kAll, lane == fl - 1 && m);
+            bad = (bad & ~(fl > 0 ? 1u << (fl - 1) : 0u)) | again;
+        }
+        {
+            R zw[Q1];
+#pragma unroll
+            for (int k = 0; k < Q1; ++k) zw[k] = start[k];
+#pragma unroll 4
+            for (int64_t i = b - 1; i >= a; --i) x.st(i, back_row(fr, i, x.ld(i), zw, tail));
+        }
     }
 }
 

@@ -126,12 +126,35 @@ LineFactor line_factor_from(const BandStore& lu) {
             for (int64_t i = 0; i < j - q; ++i) f.right[r * n + i] = lu.at_side(i, j);
         }
     }
-    // the longest run of rows identical to its first row (bitwise)
-    if (!lu.cyclic && n > 0) {
+    // the longest run of rows identical to its first row (bitwise): band,
+    // dinv and, on a cyclic factor, the side-band entries of the row (these
+    // decay away from the corners and reach exactly 0); once for the FP64
+    // values and once for their FP32 roundings
+    auto longest_run = [&](auto tag, int64_t& out_lo, int64_t& out_hi) {
+        using T = decltype(tag);
+        auto eq = [](double a, double b) {
+            T x, y;
+            if constexpr (sizeof(T) == 4) {
+                x = factor_f32(a);
+                y = factor_f32(b);
+            } else {
+                x = a;
+                y = b;
+            }
+            return std::memcmp(&x, &y, sizeof(T)) == 0;
+        };
         auto same = [&](int64_t a, int64_t b) {
-            if (std::memcmp(&f.dinv[a], &f.dinv[b], sizeof(double)) != 0) return false;
-            if (p > 0 && std::memcmp(&f.lower[a * p], &f.lower[b * p], sizeof(double) * p) != 0) return false;
-            if (q > 0 && std::memcmp(&f.upper[a * q], &f.upper[b * q], sizeof(double) * q) != 0) return false;
+            if (!eq(f.dinv[a], f.dinv[b])) return false;
+            for (int64_t k = 0; k < p; ++k)
+                if (!eq(f.lower[a * p + k], f.lower[b * p + k])) return false;
+            for (int64_t k = 0; k < q; ++k)
+                if (!eq(f.upper[a * q + k], f.upper[b * q + k])) return false;
+            if (f.cyclic) {
+                for (int64_t r = 0; r < q; ++r)
+                    if (!eq(f.bottom[r * n + a], f.bottom[r * n + b])) return false;
+                for (int64_t r = 0; r < p; ++r)
+                    if (!eq(f.right[r * n + a], f.right[r * n + b])) return false;
+            }
             return true;
         };
         int64_t best_lo = 0, best_hi = 0, lo = 0;
@@ -144,10 +167,35 @@ LineFactor line_factor_from(const BandStore& lu) {
                 lo = i;
             }
         }
+        out_lo = out_hi = 0;
         if (best_hi - best_lo >= 2) {
-            f.const_lo = best_lo;
-            f.const_hi = best_hi;
+            out_lo = best_lo;
+            out_hi = best_hi;
         }
+    };
+    if (n > 0) {
+        longest_run(double{}, f.const_lo, f.const_hi);
+        longest_run(float{}, f.const_lo32, f.const_hi32);
+    }
+    if (f.cyclic) {
+        // the first row from which every later side-band sum entry is zero
+        const int64_t nb = n - p - 1;
+        f.zside = f.zside32 = nb > 0 ? nb : 0;
+        bool nz64 = false, nz32 = false;
+        for (int64_t i = nb - 1; i >= 0 && !(nz64 && nz32); --i)
+            for (int64_t r = 0; r < q; ++r) {
+                const double v = f.bottom[r * n + i];
+                if (!nz64 && v != 0.0) {
+                    nz64 = true;
+                    f.zside = i + 1;
+                }
+                if (!nz32 && factor_f32(v) != 0.0f) {
+                    nz32 = true;
+                    f.zside32 = i + 1;
+                }
+            }
+        if (!nz64) f.zside = 0;
+        if (!nz32) f.zside32 = 0;
     }
     return f;
 }

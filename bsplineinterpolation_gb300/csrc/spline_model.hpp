@@ -66,10 +66,25 @@ struct LineFactor {
     bool cyclic = false;
     std::vector<double> lower, upper, dinv, bottom, right;
     // rows const_lo .. const_hi-1 are bit-identical to row const_lo (the LU
-    // rows of a uniform axis converge to one row away from its ends);
-    // non-cyclic factors only, an empty range otherwise
+    // rows of a uniform axis converge to one row away from its ends, and a
+    // cyclic factor's side-band entries decay to 0 there); const_lo32 ..
+    // const_hi32 the same for the FP32 roundings of the rows; empty ranges
+    // where no two consecutive rows agree
     int64_t const_lo = 0, const_hi = 0;
+    int64_t const_lo32 = 0, const_hi32 = 0;
+    // cyclic: bottom[r*n + i] is 0 for every r and every i in zside ..
+    // n-p-2 (zside32: the same for the FP32 roundings)
+    int64_t zside = 0, zside32 = 0;
 };
+
+// FP32 copy of a factor entry: the rounding to nearest, with a zero result
+// always +0 (the cyclic side-band entries alternate in sign as they decay,
+// so their FP32 underflows would otherwise alternate between -0 and +0 and
+// no two rows would agree bitwise).
+inline float factor_f32(double v) {
+    const float x = static_cast<float>(v);
+    return x == 0.0f ? 0.0f : x;
+}
 
 // Row layout of a factored band matrix (above) for the GPU line solves.
 LineFactor line_factor_from(const BandStore& lu);

@@ -42,7 +42,9 @@ struct AxisFactorDev {
     const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
     const float2* sval;
     int band;
-    int64_t clo, chi;  // rows identical to row clo (LineFactor::const_lo/const_hi)
+    int64_t clo, chi;      // FP64 rows identical to row clo (LineFactor::const_lo/const_hi)
+    int64_t clo32, chi32;  // the same for the FP32 rows (LineFactor::const_lo32/const_hi32)
+    int64_t zside, zside32;  // cyclic side-band sums: zero entries from here (LineFactor::zside/zside32)
 };
 
 // Arena offsets of one table's per-axis arrays.

@@ -198,6 +198,15 @@ intp_status intp_locate_binned(const intp_table* table, const double* coords, in
  * of the barrier, so that it runs out at once; 0 restores the normal wait.
  * Device-wide; for tests only. */
 intp_status intp_debug_set_wait_limit(uint32_t probes);
+/* Long mesh lines (single tables with few lines, and batched 1D tables)
+ * are solved by a warp each: every lane takes a segment, starts a warm-up
+ * of up to 64 (FP32) or 128 (FP64) rows before it from a zero state,
+ * checks bit for bit that the warm-up reached its neighbour's values, and
+ * is recomputed from them where it did not, so the control points equal a
+ * serial sweep's. rows >= 0 caps the warm-up at `rows` (0: every segment
+ * but the first is recomputed); -1 restores it. Device-wide; for tests
+ * only. */
+intp_status intp_debug_set_segment_warmup(int32_t rows);
 /* Fails the next `count` device allocations of table storage (creation,
  * including tables built by the serving loop) as out of memory
  * (INTP_ERR_OUT_OF_MEMORY, the reference's std::bad_alloc) without calling
