@@ -672,6 +672,9 @@ def run_batched(args, torch, steps=5, warmup=3):
     del parts
     npts = int(offsets[-1])
     out = torch.empty((npts, 1), device="cuda", dtype=torch.float32)
+    # the line solves' schedule for this batch (work queue, staging budget,
+    # lines per item), chosen by timing each candidate build once
+    schedule = b.autotune(vals)
     for _ in range(warmup):
         b.build(vals)
         b.evaluate(coords, offsets, out=out)
@@ -697,7 +700,7 @@ def run_batched(args, torch, steps=5, warmup=3):
                         " %d queries" % (len(specs), npts),
             "points_per_s": npts / (total_ms / 1e3), "build_ms": build_ms, "eval_ms": eval_ms,
             "eval_points_per_s": npts / (eval_ms / 1e3), "mesh_values": int(values.size),
-            "max_rel_err_vs_fp64": err, "steps": steps, "warmup": warmup}
+            "max_rel_err_vs_fp64": err, "steps": steps, "warmup": warmup, "schedule": schedule}
 
 
 # ---------------------------------------------------------------------------

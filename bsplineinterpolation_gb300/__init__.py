@@ -506,6 +506,32 @@ class TableBatch:
             _lib.check(lib.intp_batch_build(self._h, v.ctypes.data, 0, _stream_ptr(stream)))
             _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
 
+    def set_schedule(self, persistent=False, stage_kb=16, strided_rows=32):
+        """Schedule of the line solves (intp_batch_set_schedule); results do
+        not depend on it."""
+        sc = _lib.BatchSchedule(int(bool(persistent)), int(stage_kb), int(strided_rows), 0, 0.0)
+        _lib.check(_lib.load().intp_batch_set_schedule(self._h, C.byref(sc)))
+
+    def schedule(self):
+        sc = _lib.BatchSchedule()
+        _lib.check(_lib.load().intp_batch_get_schedule(self._h, C.byref(sc)))
+        return sc.as_dict()
+
+    def autotune(self, values, stream=None):
+        """Times a build under each candidate schedule (intp_batch_autotune),
+        keeps the fastest and leaves the batch built; returns the choice."""
+        lib = _lib.load()
+        sc = _lib.BatchSchedule()
+        if _is_cuda_tensor(values):
+            torch = _torch()
+            v = values.to(torch.float64).contiguous().reshape(-1)
+            _lib.check(lib.intp_batch_autotune(self._h, C.c_void_p(v.data_ptr()), 1, _stream_ptr(stream),
+                                               C.byref(sc)))
+        else:
+            v = np.ascontiguousarray(np.asarray(values, np.float64).ravel())
+            _lib.check(lib.intp_batch_autotune(self._h, v.ctypes.data, 0, _stream_ptr(stream), C.byref(sc)))
+        return sc.as_dict()
+
     def control_points(self, i):
         out = np.zeros(self.sizes[i])
         _lib.check(_lib.load().intp_batch_get_control_points(self._h, i, out.ctypes.data))

@@ -66,6 +66,16 @@ class ServerStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BatchSchedule(C.Structure):
+    """intp_batch_schedule."""
+    _fields_ = [("persistent", C.c_int32), ("stage_kb", C.c_int32), ("strided_rows", C.c_int32),
+                ("pad_", C.c_int32), ("build_ms", C.c_double)]
+
+    def as_dict(self):
+        return {"persistent": self.persistent, "stage_kb": self.stage_kb, "strided_rows": self.strided_rows,
+                "build_ms": self.build_ms}
+
+
 class IntpError(RuntimeError):
     """Failure reported by the CUDA library (status code and message)."""
 
@@ -110,6 +120,9 @@ SIGNATURES = {
     "intp_batch_info": (C.c_int, [_P, _P, _P]),
     "intp_batch_build": (C.c_int, [_P, _P, C.c_int32, _P]),
     "intp_batch_get_control_points": (C.c_int, [_P, C.c_int64, _P]),
+    "intp_batch_set_schedule": (C.c_int, [_P, C.POINTER(BatchSchedule)]),
+    "intp_batch_get_schedule": (C.c_int, [_P, C.POINTER(BatchSchedule)]),
+    "intp_batch_autotune": (C.c_int, [_P, _P, C.c_int32, _P, C.POINTER(BatchSchedule)]),
     "intp_batch_eval": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P, C.c_int32, _P]),
     "intp_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "intp_server_destroy": (C.c_int, [_P]),

@@ -40,8 +40,8 @@ namespace {
 constexpr int kBatchMaxDim = 3;
 constexpr int32_t kChunkElems = 8192;
 constexpr int64_t kEvalRun = 2048;           // query points per evaluation CTA
-constexpr size_t kStageBytes = 16 * 1024;     // shared memory per warp for contiguous lines
 constexpr size_t kStageMaxBytes = 200 * 1024;  // longest contiguous line staged
+constexpr int kMaxLaunches = 64;               // work counters of one build (persistent passes)
 
 intp_status bfail(intp_status s, const std::string& msg);
 
@@ -68,15 +68,26 @@ struct intp_batch {
     const int2* d_bands = nullptr;  // (band width, cyclic) per (table, axis)
     const ChunkItem* d_chunks = nullptr;
     int64_t nchunks = 0;
+    // One axis pass: its work items in two launches, those whose staged
+    // lines fit the schedule's per-warp budget, then the rest (longer staged
+    // lines, launched with their own shared-memory size).
     struct Pass {
         const SolveItem* items = nullptr;
         int64_t nitems = 0;
-        size_t smem_elems = 0;     // staging elements per warp (contiguous pass)
+        size_t smem_elems = 0;     // staging elements per warp
+        const SolveItem* long_items = nullptr;
+        int64_t nlong = 0;
+        size_t smem_long = 0;
     } pass[kBatchMaxDim];
     int npasses = 0;
     bool has_ctrl = false;
+    intp_batch_schedule sched{0, 16, 32, 0, 0.0};
+    void* work = nullptr;                // the schedule's work lists (device)
+    unsigned int* counters = nullptr;    // work counters of the persistent passes (device)
 
     ~intp_batch() {
+        if (work) cudaFree(work);
+        if (counters) cudaFree(counters);
         if (arena) cudaFree(arena);
         if (ctrl) cudaFree(ctrl);
         if (ctrl_lo) cudaFree(ctrl_lo);
@@ -190,19 +201,17 @@ __device__ __forceinline__ void solve_dispatch_warp(int p, bool cyc, const Facto
     }
 }
 
-// One warp per item (one CTA = one warp). `bands` holds the band width and
-// cyclic flag of every (table, axis). Items of tables whose refinement count
-// is not above `step` are skipped (step < 0: none skipped).
+// The work of one item (up to 32 lines of one table and axis) for one warp.
+// `bands` holds the band width and cyclic flag of every (table, axis).
+// Items of tables whose refinement count is not above `step` are skipped
+// (step < 0: none skipped).
 template <class R>
-__global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
-                                                         const TableDev* __restrict__ tables,
-                                                         const AxisFactorDev* __restrict__ fac,
-                                                         const int64_t* __restrict__ off,
-                                                         const int32_t* __restrict__ refine, int step,
-                                                         const int2* __restrict__ bands) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* tile = reinterpret_cast<R*>(smem_raw);
-    const SolveItem it = items[blockIdx.x];
+__device__ __forceinline__ void batch_solve_item(R* __restrict__ data, const SolveItem& it, R* tile,
+                                                 const TableDev* __restrict__ tables,
+                                                 const AxisFactorDev* __restrict__ fac,
+                                                 const int64_t* __restrict__ off,
+                                                 const int32_t* __restrict__ refine, int step,
+                                                 const int2* __restrict__ bands) {
     if (step >= 0 && refine[it.table] <= step) return;
     const int lane = threadIdx.x;
     const TableDev& t = tables[it.table];
@@ -231,6 +240,32 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
         const int64_t l = it.line0 + lane;
         const int64_t o = l / S, tt = l - o * S;
         solve_dispatch<R>(band.x, band.y != 0, fv, StridedChunks<R>{base + o * n * S + tt, S});
+    }
+}
+
+// One warp per CTA. PERSIST: a grid of a few warps per SM drains the list
+// through an atomic counter (longest lines first), else one CTA per item.
+template <class R, bool PERSIST>
+__global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
+                                                         int64_t nitems, unsigned int* __restrict__ counter,
+                                                         const TableDev* __restrict__ tables,
+                                                         const AxisFactorDev* __restrict__ fac,
+                                                         const int64_t* __restrict__ off,
+                                                         const int32_t* __restrict__ refine, int step,
+                                                         const int2* __restrict__ bands) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* tile = reinterpret_cast<R*>(smem_raw);
+    if constexpr (!PERSIST) {
+        batch_solve_item<R>(data, items[blockIdx.x], tile, tables, fac, off, refine, step, bands);
+    } else {
+        for (;;) {
+            unsigned int idx = 0;
+            if (threadIdx.x == 0) idx = atomicAdd(counter, 1u);
+            idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+            if (static_cast<int64_t>(idx) >= nitems) return;
+            batch_solve_item<R>(data, items[idx], tile, tables, fac, off, refine, step, bands);
+            __syncwarp();
+        }
     }
 }
 
@@ -436,12 +471,21 @@ int sm_count_batch() {
     return n;
 }
 
-// Work lists of the axis passes and of the element-wise kernels.
-void build_work(const intp_batch& b, std::vector<std::vector<SolveItem>>& passes, std::vector<size_t>& smem_elems,
+// Work lists of the axis passes under a schedule (lines per strided item,
+// shared memory per warp for staged contiguous lines) and the value chunks
+// of the element-wise kernels. Per pass: the items that fit the staging
+// budget, then (in their own list) the staged lines longer than it.
+struct PassLists {
+    std::vector<SolveItem> items, long_items;
+    size_t smem = 0, smem_long = 0;
+};
+
+void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<PassLists>& passes,
                 std::vector<ChunkItem>& chunks) {
     const size_t esz = b.elem();
+    const size_t stage = static_cast<size_t>(sc.stage_kb) * 1024;
     passes.assign(kBatchMaxDim, {});
-    smem_elems.assign(kBatchMaxDim, 0);
+    chunks.clear();
     for (int64_t i = 0; i < b.ntables; ++i) {
         const TableModel& m = b.models[i];
         for (int j = 0; j < m.dim; ++j) {
@@ -449,15 +493,19 @@ void build_work(const intp_batch& b, std::vector<std::vector<SolveItem>>& passes
             const int64_t n = m.axis[a].n;
             const int64_t nlines = m.total / n;
             const bool contig = (a == m.dim - 1);
-            int64_t rows_max = 32;
+            int64_t rows_max = sc.strided_rows;
             bool staged = false;
+            size_t line_bytes = 0;
             if (contig) {
-                const size_t line_bytes = static_cast<size_t>(n + 1) * esz;
+                rows_max = 32;
+                line_bytes = static_cast<size_t>(n + 1) * esz;
                 if (line_bytes <= kStageMaxBytes) {
                     staged = true;
-                    rows_max = std::max<int64_t>(1, std::min<int64_t>(32, static_cast<int64_t>(kStageBytes / line_bytes)));
+                    rows_max = std::max<int64_t>(1, std::min<int64_t>(32, static_cast<int64_t>(stage / line_bytes)));
                 }
             }
+            const bool is_long = staged && line_bytes > stage;
+            PassLists& pl = passes[j];
             for (int64_t l0 = 0; l0 < nlines; l0 += rows_max) {
                 SolveItem it{};
                 it.table = static_cast<int32_t>(i);
@@ -466,9 +514,14 @@ void build_work(const intp_batch& b, std::vector<std::vector<SolveItem>>& passes
                 it.last = (a == 0) ? 1 : 0;
                 it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
                 it.line0 = l0;
-                passes[j].push_back(it);
-                if (staged)
-                    smem_elems[j] = std::max(smem_elems[j], static_cast<size_t>(it.rows) * static_cast<size_t>(n + 1));
+                const size_t need = staged ? static_cast<size_t>(it.rows) * static_cast<size_t>(n + 1) : 0;
+                if (is_long) {
+                    pl.long_items.push_back(it);
+                    pl.smem_long = std::max(pl.smem_long, need);
+                } else {
+                    pl.items.push_back(it);
+                    pl.smem = std::max(pl.smem, need);
+                }
             }
         }
         for (int64_t s = 0; s < m.total; s += kChunkElems) {
@@ -480,34 +533,110 @@ void build_work(const intp_batch& b, std::vector<std::vector<SolveItem>>& passes
         }
     }
     // longest lines first: the slowest warps start first
-    for (auto& p : passes)
-        std::stable_sort(p.begin(), p.end(), [&](const SolveItem& x, const SolveItem& y) {
-            return b.models[x.table].axis[x.axis].n > b.models[y.table].axis[y.axis].n;
-        });
+    auto longest_first = [&](const SolveItem& x, const SolveItem& y) {
+        return b.models[x.table].axis[x.axis].n > b.models[y.table].axis[y.axis].n;
+    };
+    for (auto& p : passes) {
+        std::stable_sort(p.items.begin(), p.items.end(), longest_first);
+        std::stable_sort(p.long_items.begin(), p.long_items.end(), longest_first);
+    }
 }
 
+// Builds and uploads the work lists of schedule sc (replacing the batch's).
+intp_status apply_schedule(intp_batch* b, const intp_batch_schedule& sc) {
+    if (sc.stage_kb < 1 || sc.stage_kb > 200 || sc.strided_rows < 1 || sc.strided_rows > 32)
+        return bfail(INTP_ERR_INVALID_ARGUMENT, "schedule: stage_kb in [1, 200], strided_rows in [1, 32]");
+    std::vector<PassLists> passes;
+    std::vector<ChunkItem> chunks;
+    build_work(*b, sc, passes, chunks);
+    Arena ar;
+    size_t o_items[kBatchMaxDim], o_long[kBatchMaxDim];
+    for (int j = 0; j < kBatchMaxDim; ++j) {
+        o_items[j] = ar.put(passes[j].items);
+        o_long[j] = ar.put(passes[j].long_items);
+    }
+    if (b->work) cudaFree(b->work);
+    b->work = nullptr;
+    BATCH_CUDA(cudaMalloc(&b->work, std::max<size_t>(ar.host.size(), 16)), "cudaMalloc(batch work lists)");
+    BATCH_CUDA(cudaMemcpy(b->work, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice), "cudaMemcpy(work lists)");
+    const unsigned char* base = static_cast<const unsigned char*>(b->work);
+    b->npasses = 0;
+    for (int j = 0; j < kBatchMaxDim; ++j) {
+        intp_batch::Pass& p = b->pass[j];
+        p.items = reinterpret_cast<const SolveItem*>(base + o_items[j]);
+        p.nitems = static_cast<int64_t>(passes[j].items.size());
+        p.smem_elems = passes[j].smem;
+        p.long_items = reinterpret_cast<const SolveItem*>(base + o_long[j]);
+        p.nlong = static_cast<int64_t>(passes[j].long_items.size());
+        p.smem_long = passes[j].smem_long;
+        if (p.nitems + p.nlong > 0) b->npasses = j + 1;
+    }
+    b->sched = sc;
+    b->sched.build_ms = 0.0;
+    return INTP_OK;
+}
+
+int batch_sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <class R, bool PERSIST>
+cudaError_t launch_items(intp_batch* b, R* data, const SolveItem* items, int64_t nitems, size_t smem_elems,
+                         unsigned int* counter, int step, const int2* bands, cudaStream_t s) {
+    if (nitems == 0) return cudaSuccess;
+    const size_t smem = smem_elems * sizeof(R);
+    auto k = batch_solve_kernel<R, PERSIST>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    int64_t grid = nitems;
+    if (PERSIST) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        grid = std::min<int64_t>(nitems, static_cast<int64_t>(per_sm) * batch_sm_count());
+    }
+    k<<<static_cast<unsigned>(grid), 32, smem, s>>>(data, items, nitems, counter, b->d_tables, b->d_fac, b->d_off,
+                                                    b->d_refine, step, bands);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// One solve of every table: the axis passes in order, each as its regular
+// and its long-line launch. `launch` numbers the persistent launches of the
+// build (their work counters were cleared when the build started).
 template <class R>
-cudaError_t run_passes(intp_batch* b, R* data, int step, const int2* bands, cudaStream_t s) {
+cudaError_t run_passes(intp_batch* b, R* data, int step, const int2* bands, int& launch, cudaStream_t s) {
     for (int j = 0; j < b->npasses; ++j) {
         const intp_batch::Pass& p = b->pass[j];
-        if (p.nitems == 0) continue;
-        const size_t smem = p.smem_elems * sizeof(R);
-        auto k = batch_solve_kernel<R>;
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        for (int part = 0; part < 2; ++part) {
+            const SolveItem* items = part == 0 ? p.items : p.long_items;
+            const int64_t nitems = part == 0 ? p.nitems : p.nlong;
+            const size_t smem = part == 0 ? p.smem_elems : p.smem_long;
+            if (nitems == 0) continue;
+            cudaError_t e;
+            if (b->sched.persistent && launch < kMaxLaunches)
+                e = launch_items<R, true>(b, data, items, nitems, smem, b->counters + launch++, step, bands, s);
+            else
+                e = launch_items<R, false>(b, data, items, nitems, smem, nullptr, step, bands, s);
             if (e != cudaSuccess) return e;
         }
-        k<<<static_cast<unsigned>(p.nitems), 32, smem, s>>>(data, p.items, b->d_tables, b->d_fac, b->d_off, b->d_refine,
-                                                             step, bands);
-        note_launch();
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t s) {
     const int64_t N = b->off[b->ntables];
+    int launch = 0;
+    if (b->sched.persistent)
+        BATCH_CUDA(cudaMemsetAsync(b->counters, 0, sizeof(unsigned int) * kMaxLaunches, s), "cudaMemsetAsync(counters)");
     const int2* bands = b->d_bands;
     const unsigned nch = static_cast<unsigned>(b->nchunks);
     if (!b->mixed()) {
@@ -516,7 +645,7 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
                                                              b->d_chunks, b->d_tables, b->d_off, b->d_refine, -1);
         note_launch();
         BATCH_CUDA(cudaGetLastError(), "batch shift copy");
-        BATCH_CUDA(run_passes<double>(b, c, -1, bands, s), "batch line solve (fp64)");
+        BATCH_CUDA(run_passes<double>(b, c, -1, bands, launch, s), "batch line solve (fp64)");
         b->has_ctrl = true;
         return INTP_OK;
     }
@@ -545,14 +674,12 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
                                                         b->d_tables, b->d_off, b->d_refine, -1);
     note_launch();
     BATCH_CUDA(cudaGetLastError(), "batch shift copy");
-    BATCH_CUDA(run_passes<float>(b, c, -1, bands, s), "batch line solve (fp32)");
+    BATCH_CUDA(run_passes<float>(b, c, -1, bands, launch, s), "batch line solve (fp32)");
     for (int step = 0; step < b->max_refine; ++step) {
         // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass, double-float:
         // c -> ping[0] -> ping[1] -> ..., each table's last pass writing corr
         const float *ih = c, *il = step > 0 ? b->ctrl_lo : nullptr;
         for (int j = 0; j < b->npasses; ++j) {
-            const intp_batch::Pass& p = b->pass[j];
-            if (p.nitems == 0) continue;
             float** out = ping[j & 1];
             auto k = il ? batch_stencil_chunk_kernel<true> : batch_stencil_chunk_kernel<false>;
             k<<<nch, 256, 0, s>>>(ih, il, out[0], out[1], corr, fhi, flo, b->d_chunks, b->d_tables, b->d_fac, b->d_off,
@@ -562,7 +689,7 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
             ih = out[0];
             il = out[1];
         }
-        BATCH_CUDA(run_passes<float>(b, corr, step, bands, s), "batch line solve (correction)");
+        BATCH_CUDA(run_passes<float>(b, corr, step, bands, launch, s), "batch line solve (correction)");
         batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, c, nullptr, nullptr, b->ctrl_lo, corr,
                                                             b->d_chunks, b->d_tables, b->d_off, b->d_refine, step);
         note_launch();
@@ -649,10 +776,9 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     Arena ar;
     std::vector<PackedTable> packed(static_cast<size_t>(ntables));
     for (int64_t i = 0; i < ntables; ++i) pack_table(b->models[i], ar, packed[i]);
-    std::vector<std::vector<SolveItem>> passes;
-    std::vector<size_t> smem_elems;
+    std::vector<PassLists> passes;
     std::vector<ChunkItem> chunks;
-    build_work(*b, passes, smem_elems, chunks);
+    build_work(*b, b->sched, passes, chunks);
     std::vector<int2> bands(static_cast<size_t>(ntables) * kBatchMaxDim, int2{0, 0});
     for (int64_t i = 0; i < ntables; ++i)
         for (int a = 0; a < b->models[i].dim; ++a) {
@@ -666,8 +792,6 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     const size_t o_ref = ar.put(refine32);
     const size_t o_bands = ar.put(bands);
     const size_t o_chunks = ar.put(chunks);
-    size_t o_pass[kBatchMaxDim];
-    for (int j = 0; j < kBatchMaxDim; ++j) o_pass[j] = ar.put(passes[j]);
     cudaError_t e = cudaMalloc(&b->arena, ar.host.size());
     if (e != cudaSuccess) {
         delete b;
@@ -707,12 +831,15 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     b->d_bands = reinterpret_cast<const int2*>(base + o_bands);
     b->d_chunks = reinterpret_cast<const ChunkItem*>(base + o_chunks);
     b->nchunks = static_cast<int64_t>(chunks.size());
-    b->npasses = 0;
-    for (int j = 0; j < kBatchMaxDim; ++j) {
-        b->pass[j].items = reinterpret_cast<const SolveItem*>(base + o_pass[j]);
-        b->pass[j].nitems = static_cast<int64_t>(passes[j].size());
-        b->pass[j].smem_elems = smem_elems[j];
-        if (!passes[j].empty()) b->npasses = j + 1;
+    e = cudaMalloc(reinterpret_cast<void**>(&b->counters), sizeof(unsigned int) * kMaxLaunches);
+    if (e != cudaSuccess) {
+        delete b;
+        return bcuda(e, "cudaMalloc(batch work counters)");
+    }
+    const intp_status st = apply_schedule(b, b->sched);
+    if (st != INTP_OK) {
+        delete b;
+        return st;
     }
     *out = b;
     return INTP_OK;
@@ -741,6 +868,77 @@ intp_status intp_batch_build(intp_batch* b, const double* values, int32_t values
     intp_status st = e == cudaSuccess ? batch_interpolate(b, static_cast<double*>(stage), s)
                                       : bcuda(e, "cudaMemcpyAsync(batch values)");
     cudaFreeAsync(stage, s);
+    return st;
+}
+
+intp_status intp_batch_set_schedule(intp_batch* b, const intp_batch_schedule* sc) {
+    if (!b || !sc) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    return apply_schedule(b, *sc);
+}
+
+intp_status intp_batch_get_schedule(const intp_batch* b, intp_batch_schedule* sc) {
+    if (!b || !sc) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *sc = b->sched;
+    return INTP_OK;
+}
+
+intp_status intp_batch_autotune(intp_batch* b, const double* values, int32_t values_on_device, void* stream,
+                                intp_batch_schedule* chosen) {
+    if (!b || !values) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the values on the device once, so the timings are of the builds alone
+    const double* v = values;
+    void* stage = nullptr;
+    if (!values_on_device) {
+        const size_t bytes = static_cast<size_t>(b->off[b->ntables]) * 8;
+        BATCH_CUDA(cudaMalloc(&stage, bytes), "cudaMalloc(autotune values)");
+        cudaError_t e = cudaMemcpy(stage, values, bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(stage);
+            return bcuda(e, "cudaMemcpy(autotune values)");
+        }
+        v = static_cast<const double*>(stage);
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    intp_status st = INTP_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        st = bfail(INTP_ERR_CUDA, "cudaEventCreate");
+    intp_batch_schedule best{};
+    double best_ms = 0.0;
+    const int32_t stage_kb[] = {8, 16, 32};
+    const int32_t rows[] = {16, 32};
+    for (int pers = 0; pers < 2 && st == INTP_OK; ++pers)
+        for (int32_t kb : stage_kb)
+            for (int32_t r : rows) {
+                if (st != INTP_OK) break;
+                intp_batch_schedule sc{pers, kb, r, 0, 0.0};
+                st = apply_schedule(b, sc);
+                if (st == INTP_OK) st = batch_interpolate(b, v, s);  // warm-up
+                if (st != INTP_OK) break;
+                cudaEventRecord(e0, s);
+                for (int rep = 0; rep < 2 && st == INTP_OK; ++rep) st = batch_interpolate(b, v, s);
+                cudaEventRecord(e1, s);
+                if (cudaEventSynchronize(e1) != cudaSuccess) st = bfail(INTP_ERR_CUDA, "autotune timing");
+                if (st != INTP_OK) break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                sc.build_ms = ms / 2.0;
+                if (best_ms == 0.0 || sc.build_ms < best_ms) {
+                    best = sc;
+                    best_ms = sc.build_ms;
+                }
+            }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st == INTP_OK) st = apply_schedule(b, best);
+    if (st == INTP_OK) {
+        b->sched.build_ms = best_ms;
+        // the batch holds the control points of the chosen schedule's build
+        st = batch_interpolate(b, v, s);
+        if (st == INTP_OK && cudaStreamSynchronize(s) != cudaSuccess) st = bfail(INTP_ERR_CUDA, "autotune build");
+    }
+    if (stage) cudaFree(stage);
+    if (st == INTP_OK && chosen) *chosen = b->sched;
     return st;
 }
 

@@ -249,6 +249,29 @@ intp_status intp_batch_info(const intp_batch* batch, int64_t* ntables, int64_t* 
  * (InterpolationTemplate.hpp:118-143) once per table. */
 intp_status intp_batch_build(intp_batch* batch, const double* values, int32_t values_on_device, void* stream);
 
+/* Schedule of a batch's line solves. No counterpart in the reference, whose
+ * tables build one by one on its thread pool (InterpolationTemplate.hpp:
+ * 547-569). None of the choices changes the arithmetic of any line: every
+ * schedule gives the same control points, bit for bit. */
+typedef struct intp_batch_schedule {
+    int32_t persistent;    /* 1: each axis pass is a grid of a few warps per SM draining an atomic work
+                              queue (longest lines first); 0: one CTA per work item */
+    int32_t stage_kb;      /* shared memory per warp for contiguous lines, KB (1..200); staged lines
+                              above it run in a launch of their own */
+    int32_t strided_rows;  /* lines per work item on strided axes (1..32) */
+    int32_t pad_;
+    double build_ms;       /* build time measured by intp_batch_autotune (0 when set by hand) */
+} intp_batch_schedule;
+
+/* Sets / reads the schedule (the default: one CTA per item, 16 KB, 32 lines). */
+intp_status intp_batch_set_schedule(intp_batch* batch, const intp_batch_schedule* schedule);
+intp_status intp_batch_get_schedule(const intp_batch* batch, intp_batch_schedule* schedule);
+/* Times a build of the batch from `values` (as intp_batch_build) under each
+ * candidate schedule, keeps the fastest, records its time in build_ms, and
+ * leaves the batch built under it (*chosen may be NULL). */
+intp_status intp_batch_autotune(intp_batch* batch, const double* values, int32_t values_on_device,
+                                void* stream, intp_batch_schedule* chosen);
+
 /* Control points of one table (prod(size) doubles, host memory).
  * Replaces BSpline::control_points (BSpline.hpp:575-577). */
 intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table, double* ctrl_host);
