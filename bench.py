@@ -579,12 +579,17 @@ def e2e(args, f, vals, pts, lib, torch):
     """Same metric through the C-ABI with host buffers: the step copies the
     values and coordinates from pinned host memory, solves, evaluates and
     copies the results back."""
+    import bsplineinterpolation_gb300 as bi
     npts = pts.shape[0]
     K = len(DERIVS)
-    hv = vals.cpu().pin_memory()
-    hp = pts.cpu().pin_memory()
+    # page-locked host buffers from the library's own host allocator
+    # (intp_host_alloc); the inputs are copied in before the timed region
+    hv = torch.from_numpy(bi.host_empty(tuple(vals.shape), np.float64))
+    hv.copy_(vals)
+    hp = torch.from_numpy(bi.host_empty(tuple(pts.shape), np.float64))
+    hp.copy_(pts)
     od = _out_dtype(args)
-    ho = torch.empty((npts, K), dtype=torch.float32 if od == 1 else torch.float64).pin_memory()
+    ho = torch.from_numpy(bi.host_empty((npts, K), np.float32 if od == 1 else np.float64))
     karr = np.ascontiguousarray(DERIVS, np.int32)
     h = f._h
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)

@@ -27,6 +27,7 @@ __all__ = [
     "BandLU",
     "TableBatch",
     "Server",
+    "host_empty",
     "IntpError",
     "IntpDomainError",
 ]
@@ -97,6 +98,33 @@ def _make_desc(order, periodicity, mesh_dims, x_ranges, precision, refine_steps,
             keep.append(c)
             desc.coords[d] = c.ctypes.data
     return desc, keep, dims, periodicity
+
+
+class _HostBlock:
+    """Owner of one intp_host_alloc block; freed when the last view goes."""
+
+    def __init__(self, nbytes):
+        self.ptr = C.c_void_p()
+        _lib.check(_lib.load().intp_host_alloc(nbytes, C.byref(self.ptr)))
+
+    def __del__(self):
+        if self.ptr:
+            _lib.load().intp_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def host_empty(shape, dtype=np.float64):
+    """An uninitialised numpy array in page-locked host memory from
+    intp_host_alloc: the host-buffer entry points (InterpolationFunction.
+    evaluate on numpy points, intp_eval_host) copy it to and from the device
+    at the full host link rate. The memory is released with the last view of
+    the array (torch.from_numpy views keep it too)."""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape))
+    block = _HostBlock(max(1, n) * dt.itemsize)
+    buf = (C.c_char * (max(1, n) * dt.itemsize)).from_address(block.ptr.value)
+    buf._intp_block = block  # the ctypes buffer owns the allocation
+    return np.frombuffer(buf, dtype=dt, count=n).reshape(shape)
 
 
 class InterpolationFunctionTemplate:

@@ -106,6 +106,8 @@ SIGNATURES = {
     "intp_locate": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P]),
     "intp_locate_binned": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_stream_synchronize": (C.c_int, [_P]),
+    "intp_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "intp_host_free": (C.c_int, [_P]),
     "intp_debug_set_wait_limit": (C.c_int, [C.c_uint32]),
     "intp_debug_fail_allocations": (C.c_int, [C.c_int32]),
     "intp_debug_set_segment_warmup": (C.c_int, [C.c_int32]),

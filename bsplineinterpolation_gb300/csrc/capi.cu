@@ -35,14 +35,22 @@ bool take_injected_alloc_failure() {
     return false;
 }
 
-// binned evaluation: queries per chunk (one sort of up to 2^28 queries: each
-// bucket's tile is staged once per evaluation CTA that meets the bucket, and
-// more queries per sort means more of them per staged tile), smallest batch
-// worth binning
-constexpr int64_t kDefaultChunk = int64_t{1} << 28;
-// host-buffer evaluation (intp_eval_host): points per copy-in / evaluate /
-// copy-out stage of its pipeline
-constexpr int64_t kHostPipelineChunk = int64_t{1} << 24;
+// binned evaluation: queries per chunk. Each bucket's tile is staged once per
+// evaluation CTA that meets the bucket, so more queries per sort share each
+// staged tile; but the scatter spreads its records over the whole chunk's
+// record array, and it slows down as that grows. 2^25 queries measured best
+// on the 3D cubic 256^3 workload (2^23: evaluation slower; 2^28: scatter
+// slower).
+constexpr int64_t kDefaultChunk = int64_t{1} << 25;
+// host-buffer evaluation (intp_eval_host): the largest chunk of its copy-in
+// / evaluate / copy-out pipeline, its first chunk (the copy-in that nothing
+// overlaps; chunks double from it), its last chunk (the copy-out that
+// nothing overlaps), and the device buffers of each kind in the ring
+constexpr int64_t kHostPipelineChunk = int64_t{1} << 25;
+constexpr int64_t kHostHeadChunk = int64_t{1} << 21;
+constexpr int64_t kHostTailChunk = int64_t{1} << 22;
+constexpr int kHostBuffers = 3;
+// the smallest batch worth binning
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
 
 // INTP_GB300_EVAL = direct | binned | auto (default); INTP_GB300_CHUNK = queries per chunk
@@ -814,9 +822,9 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     const int K = (derivs ? nderiv : 1) * t->channels;  // output values per point
     const size_t osz = out_dtype == INTP_F32 ? 4 : 8;
     // pipeline chunks: the copies of one chunk overlap the evaluation of the
-    // next, so they stay well below the sort's own chunk
+    // next; the largest stays within the sort's own chunk
     const int64_t chunk = std::min<int64_t>(eval_chunk(), kHostPipelineChunk);
-    if (npts <= chunk) {
+    if (npts <= std::min(chunk, kHostHeadChunk)) {
         const size_t cb = static_cast<size_t>(npts) * D * 8;
         const size_t ob = static_cast<size_t>(npts) * K * osz;
         void *dc = nullptr, *dout = nullptr;
@@ -840,40 +848,45 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
         if (st == INTP_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
         return st;
     }
-    // Several chunks: the copy of chunk i+1 in and of chunk i-1 out overlap
-    // the evaluation of chunk i (separate copy streams, two device buffers).
+    // Several chunks, kHostBuffers device buffers of each kind: the copy of
+    // chunk i+1 in and of chunk i-1 out overlap the evaluation of chunk i.
+    // The copy-in stream allocates its own buffers and does not wait for work
+    // queued earlier on the caller's stream, so the coordinates stream in
+    // while that work (typically the table's solve) runs; every evaluation
+    // still runs after it. Chunks grow from kHostHeadChunk (the first
+    // evaluation starts early) and the last one is at most kHostTailChunk
+    // (little copy-out remains after the last evaluation).
+    constexpr int NB = kHostBuffers;
     cudaStream_t h2d = nullptr, d2h = nullptr;
-    cudaEvent_t start = nullptr, in_ready[2] = {}, done[2] = {}, freed[2] = {};
-    void* din[2] = {};
-    void* dout[2] = {};
+    cudaEvent_t in_ready[NB] = {}, done[NB] = {}, freed[NB] = {};
+    void* din[NB] = {};
+    void* dout[NB] = {};
     const size_t cb = static_cast<size_t>(chunk) * D * 8, ob = static_cast<size_t>(chunk) * K * osz;
     cudaError_t e = cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
-    for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+    for (int j = 0; j < NB && e == cudaSuccess; ++j) {
         e = cudaEventCreateWithFlags(&in_ready[j], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[j], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&freed[j], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMallocAsync(&din[j], cb, s);
+        if (e == cudaSuccess) e = cudaMallocAsync(&din[j], cb, h2d);
         if (e == cudaSuccess) e = cudaMallocAsync(&dout[j], ob, s);
     }
     intp_status st = e == cudaSuccess ? INTP_OK : cuda_fail(e, "pipelined evaluation set-up");
-    if (st == INTP_OK) {
-        // the copy streams start after the caller's earlier work (and the buffers' allocation)
-        e = cudaEventRecord(start, s);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(h2d, start, 0);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(d2h, start, 0);
-        if (e != cudaSuccess) st = cuda_fail(e, "pipelined evaluation set-up");
-    }
     int64_t i = 0;
-    for (int64_t p0 = 0; p0 < npts && st == INTP_OK; p0 += chunk, ++i) {
-        const int j = static_cast<int>(i & 1);
-        const int64_t n = std::min(chunk, npts - p0);
-        if (i >= 2) e = cudaStreamWaitEvent(h2d, freed[j], 0);  // chunk i-2 copied out of buffer j
+    int64_t cur = std::min(chunk, kHostHeadChunk);
+    for (int64_t p0 = 0; p0 < npts && st == INTP_OK; ++i) {
+        const int j = static_cast<int>(i % NB);
+        const int64_t rem = npts - p0;
+        const int64_t tail = std::min(cur, kHostTailChunk);
+        const int64_t n = rem > cur + tail ? cur : (rem > tail ? rem - tail : rem);
+        cur = std::min(cur * 2, chunk);
+        // buffer j's previous chunk: evaluated (input free) and copied out (output free)
+        if (i >= NB) e = cudaStreamWaitEvent(h2d, done[j], 0);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(din[j], coords + p0 * D, static_cast<size_t>(n) * D * 8, cudaMemcpyHostToDevice, h2d);
         if (e == cudaSuccess) e = cudaEventRecord(in_ready[j], h2d);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, in_ready[j], 0);
+        if (e == cudaSuccess && i >= NB) e = cudaStreamWaitEvent(s, freed[j], 0);
         if (e != cudaSuccess) {
             st = cuda_fail(e, "pipelined evaluation (copy in)");
             break;
@@ -887,17 +900,18 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
                                 static_cast<size_t>(n) * K * osz, cudaMemcpyDeviceToHost, d2h);
         if (e == cudaSuccess) e = cudaEventRecord(freed[j], d2h);
         if (e != cudaSuccess) st = cuda_fail(e, "pipelined evaluation (copy out)");
+        p0 += n;
     }
-    // the caller's stream resumes after the last copy out; then release
-    if (d2h) {
+    // the caller's stream resumes after both copy streams; then release
+    for (cudaStream_t cs : {h2d, d2h}) {
         cudaEvent_t fin = nullptr;
-        if (cudaEventCreateWithFlags(&fin, cudaEventDisableTiming) == cudaSuccess) {
-            cudaEventRecord(fin, d2h);
+        if (cs && cudaEventCreateWithFlags(&fin, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(fin, cs);
             cudaStreamWaitEvent(s, fin, 0);
             cudaEventDestroy(fin);
         }
     }
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < NB; ++j) {
         if (din[j]) cudaFreeAsync(din[j], s);
         if (dout[j]) cudaFreeAsync(dout[j], s);
     }
@@ -905,12 +919,11 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     if (st == INTP_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
     if (h2d) cudaStreamSynchronize(h2d);
     if (d2h) cudaStreamSynchronize(d2h);
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < NB; ++j) {
         if (in_ready[j]) cudaEventDestroy(in_ready[j]);
         if (done[j]) cudaEventDestroy(done[j]);
         if (freed[j]) cudaEventDestroy(freed[j]);
     }
-    if (start) cudaEventDestroy(start);
     if (h2d) cudaStreamDestroy(h2d);
     if (d2h) cudaStreamDestroy(d2h);
     return st;
@@ -981,6 +994,19 @@ intp_status intp_stream_synchronize(void* stream) {
     const int err = take_device_error(s) | take_device_error_bin_d12(s) | take_device_error_bin_d3(s);
     if (err != 0)
         return fail(INTP_ERR_TIMEOUT, "a kernel's bounded wait for an asynchronous copy ran out");
+    return INTP_OK;
+}
+
+intp_status intp_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *ptr = nullptr;
+    if (bytes == 0) return INTP_OK;
+    INTP_CUDA(cudaHostAlloc(ptr, bytes, cudaHostAllocPortable), "cudaHostAlloc");
+    return INTP_OK;
+}
+
+intp_status intp_host_free(void* ptr) {
+    if (ptr) INTP_CUDA(cudaFreeHost(ptr), "cudaFreeHost");
     return INTP_OK;
 }
 

@@ -125,7 +125,13 @@ intp_status intp_eval(const intp_table* table, const double* coords, int64_t npt
                       void* stream);
 
 /* As intp_eval with host buffers: the coordinates are copied to the device,
- * evaluated, and the results copied back before the call returns. */
+ * evaluated, and the results copied back before the call returns. Large
+ * batches run as a pipeline of chunks (copy in, evaluate, copy out on three
+ * streams). The coordinates are read from coords_host as it is when the call
+ * is made: their copies do not wait for work queued earlier on `stream` (so
+ * they overlap, e.g., a solve of the table just queued there), while every
+ * evaluation does. Host memory from intp_host_alloc gives the full link
+ * rate. */
 intp_status intp_eval_host(const intp_table* table, const double* coords_host, int64_t npts,
                            const int32_t* derivs, int32_t nderiv, void* out_host,
                            int32_t out_dtype, void* stream);
@@ -215,6 +221,14 @@ intp_status intp_debug_fail_allocations(int32_t count);
 
 /* Waits for `stream`. */
 intp_status intp_stream_synchronize(void* stream);
+
+/* Page-locked host memory for the host-buffer entry points
+ * (intp_eval_host, intp_table_interpolate with host values): allocated by
+ * the CUDA runtime's own host allocator, so copies between it and the device
+ * run at the full host link rate. No counterpart in the reference, whose data
+ * never leaves host memory. intp_host_free releases it. */
+intp_status intp_host_alloc(size_t bytes, void** ptr);
+intp_status intp_host_free(void* ptr);
 
 /* Description of the last failure on the calling thread. */
 const char* intp_last_error(void);

@@ -140,3 +140,27 @@ def test_host_buffer_pipeline_equals_device_path(precision):
         host = f.evaluate(pts, derivs=derivs)
         dev = f.evaluate(torch.tensor(pts, device="cuda"), derivs=derivs).cpu().numpy()
     assert np.array_equal(host, dev)
+
+
+def test_host_alloc_pipeline_with_growing_chunks():
+    """intp_eval_host on page-locked buffers from intp_host_alloc, with a
+    batch large enough for the pipeline's growing chunks (2M, then 1M and a
+    4M tail for 7M points): every chunk takes the binned path and the results
+    equal one device-buffer evaluation bit for bit."""
+    import ctypes as C
+    from bsplineinterpolation_gb300 import _lib
+    lib = _lib.load()
+    n = 48
+    g = np.linspace(-1, 1, n)
+    v = np.exp(-g)[:, None, None] * np.cos(3 * g)[None, :, None] * np.sin(2 * g + 0.3)[None, None, :]
+    f = bi.InterpolationFunction(3, [False] * 3, torch.tensor(v, device="cuda"), (-1, 1), (-1, 1), (-1, 1),
+                                 precision="mixed")
+    npts = 7_000_000
+    hp = bi.host_empty((npts, 3))
+    hp[:] = np.random.default_rng(11).uniform(-1, 1, (npts, 3))
+    ho = bi.host_empty((npts, 2), np.float32)
+    karr = np.ascontiguousarray([[0, 0, 0], [1, 0, 0]], np.int32)
+    _lib.check(lib.intp_eval_host(f._h, C.c_void_p(hp.ctypes.data), npts, karr.ctypes.data, 2,
+                                  C.c_void_p(ho.ctypes.data), 1, None))
+    dev = f.evaluate(torch.tensor(hp, device="cuda"), derivs=[[0, 0, 0], [1, 0, 0]]).cpu().numpy()
+    assert np.array_equal(ho, dev)
