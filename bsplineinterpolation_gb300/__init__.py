@@ -27,6 +27,7 @@ __all__ = [
     "BandLU",
     "TableBatch",
     "Server",
+    "EvalProxy",
     "host_empty",
     "IntpError",
     "IntpDomainError",
@@ -178,6 +179,12 @@ class InterpolationFunctionTemplate:
             _lib.check(lib.intp_table_interpolate(self._h, m.ctypes.data, 0, _stream_ptr(stream)))
             _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
 
+    def eval_proxy(self, points, stream=None):
+        """Spans and basis weights of `points` (CUDA tensor, N x dim), reusable
+        for every function interpolated from this template
+        (InterpolationTemplate.hpp:145-176); see EvalProxy."""
+        return EvalProxy(self._h, self.dim, points, stream)
+
     def interpolate(self, mesh, stream=None):
         """Solve for control points of `mesh` (InterpolationTemplate.hpp:118-143);
         returns a new InterpolationFunction with its own device table."""
@@ -304,6 +311,11 @@ class InterpolationFunction:
                                       _stream_ptr(stream)))
         return res
 
+    def eval_proxy(self, points, stream=None):
+        """Spans and basis weights of `points` for this function's knots
+        (Interpolation.hpp:493-503); see EvalProxy."""
+        return EvalProxy(self._h, self.dim, points, stream)
+
     def locate(self, points, stream=None):
         """Knot-span indices (N x D int64) and wrapped coordinates, for CUDA
         tensors of points (BSpline.hpp:125-157)."""
@@ -405,6 +417,47 @@ class InterpolationFunctionTemplate1D(InterpolationFunctionTemplate):
         if x_range is None:
             x_range = (0.0, float(f_length - 1))
         super().__init__(order, [periodic], [f_length], x_range, **kw)
+
+
+class EvalProxy:
+    """Precomputed knot spans and value weights of N points (device memory),
+    reusable across every function that shares the knots -- the reference's
+    eval_proxy / pre_calc_coef (InterpolationTemplate.hpp:145-176,
+    BSpline.hpp:250-296) for a whole point set. proxy(f) gives f's values at
+    the points (N); proxy(f, g, ...) evaluates all of them in one launch and
+    gives an N x k tensor. Scalar tables of dimension 1..3."""
+
+    def __init__(self, table_handle, dim, points, stream=None):
+        torch = _torch()
+        lib = _lib.load()
+        pts = points.to(torch.float64).contiguous().reshape(-1, dim)
+        self.npts = pts.shape[0]
+        self.dim = dim
+        h = C.c_void_p()
+        _lib.check(lib.intp_proxy_create(table_handle, C.c_void_p(pts.data_ptr()), self.npts,
+                                         _stream_ptr(stream), C.byref(h)))
+        self._h = h
+        self._device = pts.device
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_proxy_destroy(h)
+            self._h = None
+
+    def __call__(self, *functions, out_dtype=None, stream=None):
+        torch = _torch()
+        lib = _lib.load()
+        if not functions:
+            raise ValueError("at least one function")
+        if out_dtype is None:
+            out_dtype = "f32" if functions[0].precision == "mixed" else "f64"
+        dt = torch.float32 if out_dtype == "f32" else torch.float64
+        out = torch.empty((self.npts, len(functions)), dtype=dt, device=self._device)
+        handles = (C.c_void_p * len(functions))(*[f._h.value for f in functions])
+        _lib.check(lib.intp_proxy_eval(self._h, handles, len(functions), C.c_void_p(out.data_ptr()),
+                                       _lib.F32 if out_dtype == "f32" else _lib.F64, _stream_ptr(stream)))
+        return out[:, 0] if len(functions) == 1 else out
 
 
 class BandLU:

@@ -107,6 +107,9 @@ SIGNATURES = {
     "intp_locate_binned": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "intp_stream_synchronize": (C.c_int, [_P]),
     "intp_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "intp_proxy_create": (C.c_int, [_P, _P, C.c_int64, _P, C.POINTER(C.c_void_p)]),
+    "intp_proxy_destroy": (C.c_int, [_P]),
+    "intp_proxy_eval": (C.c_int, [_P, _P, C.c_int32, _P, C.c_int32, _P]),
     "intp_host_free": (C.c_int, [_P]),
     "intp_debug_set_wait_limit": (C.c_int, [C.c_uint32]),
     "intp_debug_fail_allocations": (C.c_int, [C.c_int32]),

@@ -17,6 +17,7 @@
 #include "intp_gpu.h"
 #include "launch.hpp"
 #include "spline_model.hpp"
+#include "table_internal.hpp"
 #include "table_pack.hpp"
 
 using namespace intp_gb300;
@@ -70,9 +71,11 @@ int64_t eval_chunk() {
     return c >= 1024 ? std::min<long long>(c, int64_t{1} << 28) : kDefaultChunk;
 }
 
+}  // namespace
+
 // Keep memory freed by cudaFreeAsync in the device's default pool so
 // per-call scratch of the binned evaluation is reused, not re-mapped.
-void retain_pool_memory() {
+void intp_gb300::retain_pool_memory() {
     static std::atomic<bool> done{false};
     if (done.exchange(true)) return;
     int dev = 0;
@@ -82,6 +85,8 @@ void retain_pool_memory() {
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
 }
+
+namespace {
 
 thread_local std::string g_last_error;
 
@@ -161,6 +166,24 @@ struct intp_table {
     int steps() const { return !mixed() ? 0 : refine_steps < 0 ? auto_refine_steps(model) : refine_steps; }
     size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
     int64_t values() const { return model.total * channels; }  // control points over all channels
+};
+
+// An evaluation proxy: the geometry it was built with (to check the tables it
+// evaluates) and its per-point spans, offsets and weights in device memory.
+struct intp_proxy {
+    int device = 0;
+    int precision = INTP_PRECISION_FP64;
+    int dim = 0, order = 0;
+    bool periodic[kMaxDim]{};
+    std::vector<double> knots[kMaxDim];
+    int64_t npts = 0;
+    void* mem = nullptr;
+    int64_t* cells = nullptr;
+    void* xr = nullptr;
+    void* base = nullptr;
+    ~intp_proxy() {
+        if (mem) cudaFree(mem);
+    }
 };
 
 struct intp_bandlu {
@@ -955,6 +978,95 @@ intp_status intp_locate(const intp_table* t, const double* coords, int64_t npts,
     if (!t || (npts > 0 && (!coords || !cells))) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     INTP_CUDA(launch_locate(t->dev, coords, npts, cells, wrapped, static_cast<cudaStream_t>(stream)),
               "locate kernel");
+    return INTP_OK;
+}
+
+intp_status intp_proxy_create(const intp_table* t, const double* coords, int64_t npts, void* stream,
+                              intp_proxy** out) {
+    if (!t || !out || (npts > 0 && !coords)) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (npts < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "npts must be >= 0");
+    if (t->model.dim > 3 || t->channels != 1)
+        return fail(INTP_ERR_UNSUPPORTED, "evaluation proxies take scalar tables of dimension 1..3");
+    const int D = t->model.dim, W = t->model.order + 1;
+    const size_t rb = t->mixed() ? 4 : 8;
+    const size_t n = static_cast<size_t>(npts);
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t b_c = up(n * D * 8), b_x = up(n * D * rb), b_w = up(n * D * W * rb);
+    intp_proxy* p = new (std::nothrow) intp_proxy();
+    if (!p) return fail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    p->device = t->device;
+    p->precision = t->precision;
+    p->dim = D;
+    p->order = t->model.order;
+    for (int d = 0; d < D; ++d) {
+        p->periodic[d] = t->model.axis[d].periodic;
+        p->knots[d] = t->model.axis[d].knots;
+    }
+    p->npts = npts;
+    if (npts > 0) {
+        const cudaError_t e = cudaMalloc(&p->mem, b_c + b_x + b_w);
+        if (e != cudaSuccess) {
+            delete p;
+            return cuda_fail(e, "cudaMalloc(proxy)");
+        }
+        unsigned char* m = static_cast<unsigned char*>(p->mem);
+        p->cells = reinterpret_cast<int64_t*>(m);
+        p->xr = m + b_c;
+        p->base = m + b_c + b_x;
+        const cudaError_t e2 = launch_proxy_build(t->dev, t->mixed(), coords, npts, p->cells, p->xr, p->base,
+                                                  static_cast<cudaStream_t>(stream));
+        if (e2 != cudaSuccess) {
+            delete p;
+            return cuda_fail(e2, "proxy kernel");
+        }
+    }
+    *out = p;
+    return INTP_OK;
+}
+
+intp_status intp_proxy_destroy(intp_proxy* p) {
+    delete p;
+    return INTP_OK;
+}
+
+intp_status intp_proxy_eval(const intp_proxy* p, const intp_table* const* tables, int32_t ntables, void* out,
+                            int32_t out_dtype, void* stream) {
+    if (!p || (ntables > 0 && !tables) || (p->npts > 0 && ntables > 0 && !out))
+        return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    if (ntables < 0) return fail(INTP_ERR_INVALID_ARGUMENT, "ntables must be >= 0");
+    if (out_dtype != INTP_F32 && out_dtype != INTP_F64) return fail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    if (ntables == 0 || p->npts == 0) return INTP_OK;
+    std::vector<TableDev> devs(static_cast<size_t>(ntables));
+    for (int32_t j = 0; j < ntables; ++j) {
+        const intp_table* t = tables[j];
+        if (!t) return fail(INTP_ERR_INVALID_ARGUMENT, "null table");
+        if (!t->has_ctrl) return fail(INTP_ERR_STATE, "table has no control points yet");
+        bool same = t->model.dim == p->dim && t->model.order == p->order && t->precision == p->precision &&
+                    t->channels == 1 && t->device == p->device;
+        for (int d = 0; same && d < p->dim; ++d)
+            same = t->model.axis[d].periodic == p->periodic[d] && t->model.axis[d].knots == p->knots[d];
+        if (!same) return fail(INTP_ERR_INVALID_ARGUMENT, "table does not share the proxy's knots");
+        devs[static_cast<size_t>(j)] = t->dev;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DerivPlan plan{};
+    std::string err;
+    if (!make_plan(tables[0], nullptr, 0, plan, err)) return fail(INTP_ERR_INVALID_ARGUMENT, err);
+    TableDev* dd = nullptr;
+    const size_t bytes = devs.size() * sizeof(TableDev);
+    INTP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dd), bytes, s), "cudaMallocAsync(proxy tables)");
+    cudaError_t e = cudaMemcpyAsync(dd, devs.data(), bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_proxy_eval(dd, ntables, p->dim, p->order, p->precision == INTP_PRECISION_MIXED, p->npts,
+                              p->cells, p->xr, p->base, plan, out, out_dtype == INTP_F32 ? 1 : 0, s);
+    // the descriptors are read from pageable host memory by the copy: wait for
+    // it before `devs` goes out of scope
+    const cudaError_t e2 = cudaFreeAsync(dd, s);
+    const cudaError_t e3 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "proxy evaluation");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync(proxy tables)");
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaStreamSynchronize");
     return INTP_OK;
 }
 

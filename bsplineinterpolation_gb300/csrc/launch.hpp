@@ -86,6 +86,15 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
                                   const float* lower, const float* upper, const float* dinv, const float* bottom,
                                   const float* right, cudaStream_t s, int64_t clo = 0, int64_t chi = 0,
                                   int64_t zside = INT64_MAX);
+// Evaluation proxies (proxy.cu): per point and axis its span (cells), offset
+// (xr: FP64 coordinate, or FP32 local offset for mixed tables) and O+1
+// value weights (base), then the values of ntables tables (a device array of
+// descriptors) at every point, out[i * ntables + j].
+cudaError_t launch_proxy_build(const TableDev& t, bool mixed, const double* coords, int64_t npts, int64_t* cells,
+                               void* xr, void* base, cudaStream_t s);
+cudaError_t launch_proxy_eval(const TableDev* tables, int ntables, int dim, int order, bool mixed, int64_t npts,
+                              const int64_t* cells, const void* xr, const void* base, const DerivPlan& plan, void* out,
+                              int out_f32, cudaStream_t s);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
 // FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),

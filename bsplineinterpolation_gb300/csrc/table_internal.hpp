@@ -29,4 +29,8 @@ void table_release_scratch(intp_table* t);
 // Number of control points (product of the axis sizes).
 int64_t table_values(const intp_table* t);
 
+// Keeps memory freed to the current device's stream-ordered pool in the pool
+// (no release back to the driver at synchronisation points); once per process.
+void retain_pool_memory();
+
 }  // namespace intp_gb300

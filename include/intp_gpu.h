@@ -136,6 +136,29 @@ intp_status intp_eval_host(const intp_table* table, const double* coords_host, i
                            const int32_t* derivs, int32_t nderiv, void* out_host,
                            int32_t out_dtype, void* stream);
 
+/* ---- evaluation proxies ----
+ *
+ * Knot spans and basis weights of npts points (coords: npts x dim doubles,
+ * device memory), computed once with `table`'s knots and kept in device
+ * memory; intp_proxy_eval then evaluates any list of tables that share
+ * those knots (same dimension, order, precision, periodicity and knot
+ * vectors: tables built from one template) at all the points, value only.
+ * Each value equals what intp_eval's direct path returns for that table.
+ * Scalar tables of dimension 1..3.
+ * Replaces: InterpolationFunctionTemplate::eval_proxy
+ * (InterpolationTemplate.hpp:145-176), InterpolationFunction::eval_proxy
+ * (Interpolation.hpp:493-503) and BSpline::pre_calc_coef (BSpline.hpp:
+ * 250-296), which precompute one point's basis for reuse across functions. */
+typedef struct intp_proxy intp_proxy;
+intp_status intp_proxy_create(const intp_table* table, const double* coords, int64_t npts, void* stream,
+                              intp_proxy** out);
+intp_status intp_proxy_destroy(intp_proxy* proxy);
+/* out: npts x ntables values of out_dtype (device memory), point-major:
+ * out[i * ntables + j] = table j at point i. A table whose knots differ from
+ * the proxy's fails with INTP_ERR_INVALID_ARGUMENT. */
+intp_status intp_proxy_eval(const intp_proxy* proxy, const intp_table* const* tables, int32_t ntables, void* out,
+                            int32_t out_dtype, void* stream);
+
 /* Allocation-free form of intp_eval. No counterpart in the reference, whose
  * evaluation is per point on the host and needs no scratch.
  *
@@ -340,7 +363,11 @@ typedef struct intp_server_stats {
 #define INTP_SERVER_TABLE_GONE 2   /* evicted or released */
 #define INTP_SERVER_TABLE_FAILED 3
 
-/* Starts the worker on the current device (cfg may be NULL for defaults). */
+/* Starts the worker on the current device (cfg may be NULL for defaults).
+ * The server reserves min(memory_budget, 64 GiB) in the device's
+ * stream-ordered memory pool up front (the pool then keeps freed memory), so
+ * that admitting a request does not wait for new device memory to be
+ * mapped. */
 intp_status intp_server_create(const intp_server_config* cfg, intp_server** out);
 /* Finishes every submitted request, then frees the tables and the worker. */
 intp_status intp_server_destroy(intp_server* server);
