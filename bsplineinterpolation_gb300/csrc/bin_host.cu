@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "bin_impl.cuh"
 
@@ -137,21 +138,36 @@ int sm_count() {
     return n;
 }
 
+// INTP_GB300_SORT=permute: the three-pass sort (records written in input
+// order, then moved); default: count, then scatter from the coordinates.
+bool sort_two_pass() {
+    const char* v = std::getenv("INTP_GB300_SORT");
+    return !(v && std::strcmp(v, "permute") == 0);
+}
+
 template <int D>
 cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
                         uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec, uint32_t* rank,
                         uint32_t* rec, int64_t slice, cudaStream_t s) {
     using namespace bin_detail;
     const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
+    const bool two = sort_two_pass();
     auto kl = locate_kernel<D>;
     auto kp = permute_kernel<D>;
+    auto kc = count_kernel<D>;
+    auto ks = scatter_kernel<D>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t e = cudaSuccess;
+        for (const void* k : {reinterpret_cast<const void*>(kl), reinterpret_cast<const void*>(kp),
+                              reinterpret_cast<const void*>(kc), reinterpret_cast<const void*>(ks)})
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
+    if (two)
+        kc<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, blkcount);
+    else
+        kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
     note_launch();
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -161,7 +177,10 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    kp<<<nblk * kPermuteParts, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
+    if (two)
+        ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, rec);
+    else
+        kp<<<nblk * kPermuteParts, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }

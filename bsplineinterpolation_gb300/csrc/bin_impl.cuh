@@ -173,6 +173,84 @@ __global__ void __launch_bounds__(kLocateThreads, 2) locate_kernel(TableDev t, B
     for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) blkcount[b * nblk + blk] = sh_count[b];
 }
 
+// Counting pass of the two-pass sort (count_kernel, then scatter_kernel): the
+// per-(bucket, CTA) counts of the slice, from the same exact spans as
+// locate_kernel, writing no records.
+template <int D>
+__global__ void __launch_bounds__(kLocateThreads, 2) count_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
+                                                            int64_t n, int64_t slice,
+                                                            uint32_t* __restrict__ blkcount) {
+    extern __shared__ uint32_t sh_count[];
+    const int nblk = gridDim.x, blk = blockIdx.x;
+    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_count[b] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t p0 = blk * slice, p1 = (p0 + slice < n) ? p0 + slice : n;
+    for (int64_t base = p0; base < p1; base += blockDim.x) {
+        const int64_t p = base + threadIdx.x;
+        const bool valid = p < p1;
+        uint32_t b = 0xFFFFFFFFu;
+        if (valid) {
+            int cl[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                float u;
+                cl[d] = span_and_offset(t.ax[d], t.order, __ldg(coords + p * D + d), u) - t.order;
+            }
+            b = bucket_of<D>(g, cl);
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
+        const int leader = __ffs(peers) - 1;
+        if (valid && lane == leader) atomicAdd(&sh_count[b], static_cast<uint32_t>(__popc(peers)));
+    }
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) blkcount[b * nblk + blk] = sh_count[b];
+}
+
+// Scatter pass of the two-pass sort: CTA blk recomputes the record of every
+// query of its slice (the same spans and offsets as the counting pass) and
+// writes it to the next free slot of its (bucket, CTA) pair, taken from a
+// shared-memory cursor that starts at the pair's first slot (warp-aggregated
+// atomics). The order of records within a pair depends on timing; each
+// query's outputs do not. The tag holds the query's index within the slice,
+// as in permute_kernel's output.
+template <int D>
+__global__ void __launch_bounds__(kSortThreads, 2) scatter_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
+                                                              int64_t n, int64_t slice,
+                                                              const uint32_t* __restrict__ blkoffset,
+                                                              uint32_t* __restrict__ rec) {
+    extern __shared__ uint32_t sh_cursor[];
+    const int nblk = gridDim.x, blk = blockIdx.x;
+    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_cursor[b] = __ldg(blkoffset + b * nblk + blk);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t p0 = blk * slice, p1 = (p0 + slice < n) ? p0 + slice : n;
+    for (int64_t base = p0; base < p1; base += blockDim.x) {
+        const int64_t p = base + threadIdx.x;
+        const bool valid = p < p1;
+        uint32_t b = 0xFFFFFFFFu, cell = 0;
+        float u[D];
+        if (valid) {
+            int cl[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                cl[d] = span_and_offset(t.ax[d], t.order, __ldg(coords + p * D + d), u[d]) - t.order;
+                cell |= static_cast<uint32_t>(cl[d] & ((1 << g.lb[d]) - 1)) << g.shift[d];
+            }
+            b = bucket_of<D>(g, cl);
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
+        const int leader = __ffs(peers) - 1;
+        uint32_t first = 0;
+        if (valid && lane == leader) first = atomicAdd(&sh_cursor[b], static_cast<uint32_t>(__popc(peers)));
+        first = __shfl_sync(0xFFFFFFFFu, first, leader);
+        if (valid) {
+            const uint32_t slot = first + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
+            rec_store<D>(rec, slot, u, (static_cast<uint32_t>(p - p0) << kCellBits) | cell);
+        }
+    }
+}
+
 // Every record of the slice to slot = (first slot of its (bucket, CTA) pair)
 // + (its rank there, from the locate kernel): independent streaming copies,
 // three records per thread and trip with all loads in flight. CTA j takes
