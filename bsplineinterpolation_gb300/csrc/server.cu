@@ -9,13 +9,24 @@
 //   - evaluations queued against the same table (same derivative request and
 //     output type) are merged into one work unit: their coordinates are copied
 //     into one device buffer, evaluated by one intp_eval, and each request's
-//     results are copied back to its own host buffer.
+//     results are copied back to its own host buffer;
+//   - an evaluation larger than a work unit (kPiecePoints) is split into
+//     pieces, each its own unit; the request completes with its last piece.
 // Work units on different slots overlap on the device; requests that arrive
 // while others run are admitted as soon as a slot and memory free up, without
-// waiting for the running ones to drain.
+// waiting for the running ones to drain. A quarter of the slots (at least one
+// when there are two or more) take small requests only (evaluations of up to
+// kSmallPoints points, builds of up to kSmallValues values) and run on
+// high-priority streams, so that small requests neither queue behind large
+// ones for a slot nor wait for their kernels on the device; and at most
+// kMaxLargeInflight large units run at once, so that the host-to-device copy
+// queue, which serves every stream in order, stays short.
 //
 // Memory: resident tables plus the transient bytes of the work in flight stay
-// within the configured budget. A unit that does not fit evicts the least
+// within the configured budget. At creation the server reserves
+// min(budget, kPoolReserve) in the device's stream-ordered pool (freed
+// memory stays in the pool), so admissions carve from it instead of waiting
+// for new memory to be mapped while other requests queue. A unit that does not fit evicts the least
 // recently used resident tables that no queued or running request refers to;
 // when that is not enough it waits for running units to finish, and fails
 // with INTP_ERR_BUDGET when it could never fit.
@@ -25,10 +36,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <iterator>
 #include <list>
 #include <mutex>
 #include <new>
@@ -56,6 +70,20 @@ constexpr int64_t kDefaultMaxBatchPoints = int64_t{1} << 24;
 constexpr size_t kEvalScratchPerPoint = 36;
 constexpr size_t kEvalScratchFixed = size_t{16} << 20;
 constexpr int64_t kBinnedPoints = int64_t{1} << 18;
+// work-unit bounds: the largest evaluation unit (larger requests are split),
+// and what counts as small for the reserved slots
+constexpr int64_t kPiecePoints = int64_t{1} << 21;
+constexpr int64_t kSmallPoints = int64_t{1} << 16;
+constexpr int64_t kSmallValues = int64_t{1} << 18;
+// large units (evaluation pieces above kSmallPoints, builds above
+// kSmallValues) in flight at once: their host-to-device copies share the copy
+// engines first come first served, so more of them in flight only lengthens
+// the copy queue that a small request's copy waits behind
+constexpr int kMaxLargeInflight = 3;
+// device memory reserved in the stream-ordered pool at creation (at most the
+// budget): tables and work units are carved from it, so an admission does not
+// wait for the driver to map new memory while requests queue behind it
+constexpr uint64_t kPoolReserve = uint64_t{64} << 30;
 
 size_t eval_reserve(int64_t npts, size_t per_point) {
     return static_cast<size_t>(npts) * per_point + (npts >= kBinnedPoints ? kEvalScratchFixed : 0);
@@ -78,8 +106,12 @@ struct Request {
     int32_t nderiv = 0;
     void* out = nullptr;
     int32_t out_dtype = INTP_F32;
+    int64_t admitted = 0;  // points placed into work units so far
+    int parts_open = 0;    // work units in flight holding a piece of it
     // result
     Clock::time_point t_submit;
+    Clock::time_point t_admit;  // its first work unit was issued
+    bool admitted_once = false;
     intp_status status = INTP_OK;
     std::string error;
     bool done = false;
@@ -95,9 +127,16 @@ struct Table {
     uint64_t last_use = 0;  // LRU clock
 };
 
+// Points [off, off + n) of an evaluation request (a build: its whole request).
+struct Part {
+    Request* r = nullptr;
+    int64_t off = 0, n = 0;
+};
+
 struct Unit {
     bool build = false;
-    std::vector<Request*> reqs;
+    bool large = false;  // counted against kMaxLargeInflight
+    std::vector<Part> parts;
     int64_t table = 0;
     size_t reserve = 0;  // transient device bytes counted while in flight
     int64_t npts = 0;
@@ -107,8 +146,15 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
+    bool small_only = false;  // reserved for small requests (high-priority stream)
     Unit unit;
 };
+
+int64_t build_values(const intp_table_desc& d) {
+    int64_t n = 1;
+    for (int k = 0; k < d.dim; ++k) n *= d.size[k];
+    return n;
+}
 
 double ms_since(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
@@ -152,9 +198,14 @@ struct intp_server {
     uint64_t lru_clock = 0;
     uint64_t resident_bytes = 0;
     uint64_t inflight_bytes = 0;
+    int large_inflight = 0;
 
     // statistics since the last reset
     std::vector<double> lat_build, lat_eval;
+    // request trace (INTP_GB300_SERVER_TRACE=<file>): one line per completed
+    // request, written when the server is destroyed
+    std::string trace_path;
+    std::vector<std::string> trace;
     double points = 0;
     int64_t failed = 0, evictions = 0, merged_units = 0;
     Clock::time_point t_reset = Clock::now(), t_last = Clock::now();
@@ -178,6 +229,15 @@ bool same_request_shape(const Request* a, const Request* b) {
 }  // namespace
 
 void intp_server::complete(Request* r, intp_status st, const std::string& msg, Clock::time_point now) {
+    if (!trace_path.empty()) {
+        char line[256];
+        const Clock::time_point ta = r->admitted_once ? r->t_admit : now;
+        std::snprintf(line, sizeof line, "%lld,%d,%lld,%.3f,%.3f,%.3f,%d\n", static_cast<long long>(r->id),
+                      r->build ? 1 : 0, static_cast<long long>(r->build ? build_values(r->desc) : r->npts),
+                      ms_since(t_reset, r->t_submit), ms_since(r->t_submit, ta), ms_since(ta, now),
+                      static_cast<int>(st));
+        trace.emplace_back(line);
+    }
     r->status = st;
     r->error = msg;
     r->done = true;
@@ -237,8 +297,9 @@ void intp_server::finish_slot(Slot& s, cudaError_t e) {
     const Clock::time_point now = Clock::now();
     Unit& u = s.unit;
     inflight_bytes -= u.reserve;
+    if (u.large) --large_inflight;
     if (u.build) {
-        Request* r = u.reqs[0];
+        Request* r = u.parts[0].r;
         Table& tb = tables[u.table];
         if (e == cudaSuccess && tb.t) {
             table_release_scratch(tb.t);
@@ -255,10 +316,16 @@ void intp_server::finish_slot(Slot& s, cudaError_t e) {
             complete(r, INTP_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e), now);
         }
     } else {
-        for (Request* r : u.reqs)
-            complete(r, e == cudaSuccess ? INTP_OK : INTP_ERR_CUDA,
-                     e == cudaSuccess ? "" : std::string("evaluation: ") + cudaGetErrorString(e), now);
-        if (u.reqs.size() > 1) ++merged_units;
+        for (const Part& pt : u.parts) {
+            Request* r = pt.r;
+            if (e != cudaSuccess && r->status == INTP_OK) {
+                r->status = INTP_ERR_CUDA;
+                r->error = std::string("evaluation: ") + cudaGetErrorString(e);
+            }
+            r->parts_open--;
+            if (r->admitted == r->npts && r->parts_open == 0) complete(r, r->status, r->error, now);
+        }
+        if (u.parts.size() > 1) ++merged_units;
     }
     s.busy = false;
     s.unit = Unit{};
@@ -271,6 +338,11 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
     (void)lock;
     for (auto it = pending.begin(); it != pending.end(); ++it) {
         Request* r = *it;
+        // a reserved slot takes small requests only
+        if (s.small_only && (r->build ? build_values(r->desc) > kSmallValues : r->npts - r->admitted > kSmallPoints))
+            continue;
+        const bool large = r->build ? build_values(r->desc) > kSmallValues : r->npts - r->admitted > kSmallPoints;
+        if (large && large_inflight >= kMaxLargeInflight) continue;
         if (r->build) {
             const size_t need = table_build_scratch_bytes(&r->desc) +
                                 [&] {
@@ -288,7 +360,10 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
             pending.erase(it);
             Unit u;
             u.build = true;
-            u.reqs.push_back(r);
+            u.large = large;
+            u.parts.push_back(Part{r, 0, 0});
+            r->t_admit = Clock::now();
+            r->admitted_once = true;
             u.table = r->table;
             u.reserve = need;
             intp_table* t = nullptr;
@@ -306,6 +381,7 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
                 return true;
             }
             inflight_bytes += need;
+            if (u.large) ++large_inflight;
             cudaEventRecord(s.done, s.stream);
             s.unit = std::move(u);
             s.busy = true;
@@ -320,35 +396,54 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         }
         if (tt->second.state != kResident) continue;  // its build has not finished
         Table& tb = tt->second;
-        // merge the queued evaluations of the same shape, in submission order
+        // the next piece of this request, then (while the unit has room) the
+        // queued evaluations of the same shape that fit whole, in submission
+        // order
         Unit u;
         u.table = r->table;
         const int K = r->derivs.empty() ? 1 : r->nderiv;
         const size_t ob = r->out_dtype == INTP_F32 ? 4 : 8;
         const size_t per_pt = static_cast<size_t>(tb.dim) * 8 + static_cast<size_t>(K) * ob + kEvalScratchPerPoint;
-        for (auto jt = it; jt != pending.end(); ++jt) {
-            Request* q = *jt;
-            if (q->build || !same_request_shape(r, q)) continue;
-            if (!u.reqs.empty() && u.npts + q->npts > max_batch_points) break;
-            u.reqs.push_back(q);
-            u.npts += q->npts;
+        // a reserved slot, or the large-unit cap reached: the unit stays small
+        const bool small_unit = s.small_only || large_inflight >= kMaxLargeInflight;
+        const int64_t cap = std::min(max_batch_points, small_unit ? kSmallPoints : kPiecePoints);
+        u.parts.push_back(Part{r, r->admitted, std::min(r->npts - r->admitted, cap)});
+        u.npts = u.parts[0].n;
+        if (r->admitted + u.npts == r->npts) {
+            for (auto jt = std::next(it); jt != pending.end() && u.npts < cap; ++jt) {
+                Request* q = *jt;
+                if (q->build || !same_request_shape(r, q) || q->admitted != 0 || u.npts + q->npts > cap) continue;
+                u.parts.push_back(Part{q, 0, q->npts});
+                u.npts += q->npts;
+            }
         }
         u.reserve = eval_reserve(u.npts, per_pt);
         if (u.reserve > budget) {
-            // a single request too large for the budget on its own
+            // a single piece too large for the budget on its own
+            if (r->parts_open > 0) continue;  // wait for its other pieces, then fail
             pending.erase(it);
+            r->admitted = r->npts;
             fail_request(r, INTP_ERR_BUDGET, "evaluation exceeds the memory budget");
             return true;
         }
         if (!make_room(u.reserve)) {
-            // take the first request alone if the merged unit does not fit
-            if (u.reqs.size() == 1) continue;
-            u.reqs.resize(1);
-            u.npts = r->npts;
+            // take the first piece alone if the merged unit does not fit
+            if (u.parts.size() == 1) continue;
+            u.parts.resize(1);
+            u.npts = u.parts[0].n;
             u.reserve = eval_reserve(u.npts, per_pt);
             if (!make_room(u.reserve)) continue;
         }
-        for (Request* q : u.reqs) pending.remove(q);
+        const Clock::time_point t_now = Clock::now();
+        for (const Part& pt : u.parts) {
+            if (!pt.r->admitted_once) {
+                pt.r->t_admit = t_now;
+                pt.r->admitted_once = true;
+            }
+            pt.r->admitted += pt.n;
+            pt.r->parts_open++;
+            if (pt.r->admitted == pt.r->npts) pending.remove(pt.r);
+        }
         const int D = tb.dim;
         cudaStream_t st = s.stream;
         double* dc = nullptr;
@@ -356,12 +451,12 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dc), static_cast<size_t>(u.npts) * D * 8 + 16, st);
         if (e == cudaSuccess) e = cudaMallocAsync(&dout, static_cast<size_t>(u.npts) * K * ob + 16, st);
         int64_t off = 0;
-        for (Request* q : u.reqs) {
+        for (const Part& pt : u.parts) {
             if (e != cudaSuccess) break;
-            if (q->npts > 0)
-                e = cudaMemcpyAsync(dc + off * D, q->coords, static_cast<size_t>(q->npts) * D * 8, cudaMemcpyDefault,
-                                    st);
-            off += q->npts;
+            if (pt.n > 0)
+                e = cudaMemcpyAsync(dc + off * D, pt.r->coords + pt.off * D, static_cast<size_t>(pt.n) * D * 8,
+                                    cudaMemcpyDefault, st);
+            off += pt.n;
         }
         intp_status ist = INTP_OK;
         std::string msg;
@@ -371,12 +466,13 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
             if (ist != INTP_OK) msg = intp_last_error();
         }
         off = 0;
-        for (Request* q : u.reqs) {
+        for (const Part& pt : u.parts) {
             if (e != cudaSuccess || ist != INTP_OK) break;
-            if (q->npts > 0)
-                e = cudaMemcpyAsync(q->out, static_cast<unsigned char*>(dout) + static_cast<size_t>(off) * K * ob,
-                                    static_cast<size_t>(q->npts) * K * ob, cudaMemcpyDefault, st);
-            off += q->npts;
+            if (pt.n > 0)
+                e = cudaMemcpyAsync(static_cast<unsigned char*>(pt.r->out) + static_cast<size_t>(pt.off) * K * ob,
+                                    static_cast<unsigned char*>(dout) + static_cast<size_t>(off) * K * ob,
+                                    static_cast<size_t>(pt.n) * K * ob, cudaMemcpyDefault, st);
+            off += pt.n;
         }
         if (dc) cudaFreeAsync(dc, st);
         if (dout) cudaFreeAsync(dout, st);
@@ -387,13 +483,28 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
             }
             // copies already queued for earlier requests of the unit may still
             // be writing their outputs: the requests are reported done only
-            // once the slot's stream has drained
+            // once the slot's stream has drained (and, for a split request,
+            // once its other pieces have finished); their points not yet
+            // admitted are dropped
             cudaStreamSynchronize(st);
-            for (Request* q : u.reqs) fail_request(q, ist, msg);
+            for (const Part& pt : u.parts) {
+                Request* q = pt.r;
+                if (q->status == INTP_OK) {
+                    q->status = ist;
+                    q->error = msg;
+                }
+                if (q->admitted < q->npts) {
+                    q->admitted = q->npts;
+                    pending.remove(q);
+                }
+                if (--q->parts_open == 0) complete(q, q->status, q->error, Clock::now());
+            }
             return true;
         }
         tb.last_use = ++lru_clock;
         inflight_bytes += u.reserve;
+        u.large = u.npts > kSmallPoints;
+        if (u.large) ++large_inflight;
         cudaEventRecord(s.done, st);
         s.unit = std::move(u);
         s.busy = true;
@@ -427,7 +538,9 @@ void intp_server::run() {
                 Request* r = pending.front();
                 pending.pop_front();
                 if (r->build) tables[r->table].state = kFailed;
-                fail_request(r, INTP_ERR_STATE, "server shut down before the request could run");
+                r->admitted = r->npts;
+                if (r->parts_open == 0)  // always so: no unit is in flight
+                    fail_request(r, INTP_ERR_STATE, "server shut down before the request could run");
             }
             continue;
         }
@@ -459,6 +572,13 @@ intp_server::~intp_server() {
         if (s.stream) cudaStreamDestroy(s.stream);
     }
     for (auto& kv : requests) delete kv.second;  // includes any never waited on
+    if (!trace_path.empty()) {
+        if (FILE* f = std::fopen(trace_path.c_str(), "w")) {
+            std::fputs("id,build,size,submit_ms,queue_ms,service_ms,status\n", f);
+            for (const std::string& l : trace) std::fputs(l.c_str(), f);
+            std::fclose(f);
+        }
+    }
 }
 
 namespace {
@@ -483,14 +603,33 @@ intp_status intp_server_create(const intp_server_config* cfg, intp_server** out)
     if (!s) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
     if (c.memory_budget > 0) s->budget = c.memory_budget;
     if (c.max_batch_points > 0) s->max_batch_points = c.max_batch_points;
+    if (const char* tp = std::getenv("INTP_GB300_SERVER_TRACE")) s->trace_path = tp;
     cudaGetDevice(&s->device);
     s->slots.resize(static_cast<size_t>(nslots));
-    for (Slot& sl : s->slots) {
-        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    const int nsmall = nslots >= 2 ? std::max(1, nslots / 4) : 0;
+    for (int i = 0; i < nslots; ++i) {
+        Slot& sl = s->slots[static_cast<size_t>(i)];
+        sl.small_only = i < nsmall;
+        cudaError_t e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.small_only ? greatest : least);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             delete s;
             return sfail(INTP_ERR_CUDA, std::string("server streams: ") + cudaGetErrorString(e));
+        }
+    }
+    // keep freed pool memory in the pool, and reserve the working set up front
+    retain_pool_memory();
+    {
+        const size_t reserve = static_cast<size_t>(std::min<uint64_t>(s->budget, kPoolReserve));
+        cudaStream_t st = s->slots[0].stream;
+        void* p = nullptr;
+        if (cudaMallocAsync(&p, reserve, st) == cudaSuccess) {
+            cudaFreeAsync(p, st);
+            cudaStreamSynchronize(st);
+        } else {
+            cudaGetLastError();  // not fatal: the pool then grows on demand
         }
     }
     s->worker = std::thread([s] { s->run(); });
