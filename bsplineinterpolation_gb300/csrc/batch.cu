@@ -10,9 +10,9 @@
 // longest lines first. The arithmetic per line is solve_line_chunked, the same as the
 // single-table solves, so a batched table gets the control points that
 // intp_table_interpolate gives it, bit for bit. Mixed-precision batches
-// refine per table (double-float residual, FP32 correction, double-float
-// control points) with the same step count and the same arithmetic as a
-// single table.
+// solve each table in double-word arithmetic (R = DW, control points kept
+// as FP32 pairs), or in FP32 for tables built with refine_steps = 0, as a
+// single table is.
 //
 // Evaluation takes one list of query runs per (dimension, order) class and
 // evaluates each run with the per-point code of the direct kernel
@@ -28,7 +28,6 @@
 #include "batch.hpp"
 #include "intp_gpu.h"
 #include "launch.hpp"
-#include "refine_df.cuh"
 #include "solve_line.cuh"
 #include "spline_model.hpp"
 #include "table_pack.hpp"
@@ -53,8 +52,10 @@ struct intp_batch {
     int64_t ntables = 0;
     std::vector<TableModel> models;
     std::vector<int64_t> off;      // ntables + 1 element offsets
-    std::vector<int> refine;       // refinement steps per table (mixed)
-    int max_refine = 0;
+    // mixed: per table 0 (FP32 solve) or > 0 (double-word solve, control
+    // points kept as ctrl + ctrl_lo); the largest and the smallest value
+    std::vector<int> refine;
+    int max_refine = 0, min_refine = 1 << 30;
     std::vector<TableDev> h_tables;
     void* arena = nullptr;         // per-axis data, descriptors, work lists
     void* ctrl = nullptr;
@@ -132,6 +133,18 @@ __device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFact
     return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right, f.clo, f.chi, f.zside};
 }
 
+template <>
+__device__ __forceinline__ FactorView<DW> factor_view<DW>(const AxisFactorDev& f, int64_t n) {
+    return FactorView<DW>{n, f.lowerw, f.upperw, f.dinvw, f.bottomw, f.rightw, f.clo, f.chi, f.zside};
+}
+
+// Tables a pass works on (mixed batches): every table, the tables solved in
+// FP32 (refine = 0), or the ones solved in double-word arithmetic (refine > 0).
+constexpr int kSelAll = -1, kSelPlain = -2, kSelDW = -3;
+__device__ __forceinline__ bool selected(int sel, int refine) {
+    return sel == kSelAll || (sel == kSelPlain ? refine == 0 : refine > 0);
+}
+
 // Lines are walked in chunks of this many elements (registers per lane).
 constexpr int kBatchChunk = 16;
 
@@ -203,16 +216,17 @@ __device__ __forceinline__ void solve_dispatch_warp(int p, bool cyc, const Facto
 
 // The work of one item (up to 32 lines of one table and axis) for one warp.
 // `bands` holds the band width and cyclic flag of every (table, axis).
-// Items of tables whose refinement count is not above `step` are skipped
-// (step < 0: none skipped).
+// `sel` picks the tables of a mixed batch: -1 every table, kSelPlain the
+// tables solved in FP32 (refine = 0), kSelDW the ones solved in double-word
+// arithmetic (refine > 0).
 template <class R>
 __device__ __forceinline__ void batch_solve_item(R* __restrict__ data, const SolveItem& it, R* tile,
                                                  const TableDev* __restrict__ tables,
                                                  const AxisFactorDev* __restrict__ fac,
                                                  const int64_t* __restrict__ off,
-                                                 const int32_t* __restrict__ refine, int step,
+                                                 const int32_t* __restrict__ refine, int sel,
                                                  const int2* __restrict__ bands) {
-    if (step >= 0 && refine[it.table] <= step) return;
+    if (!selected(sel, refine[it.table])) return;
     const int lane = threadIdx.x;
     const TableDev& t = tables[it.table];
     const AxisDev& ax = t.ax[it.axis];
@@ -251,164 +265,42 @@ __global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, c
                                                          const TableDev* __restrict__ tables,
                                                          const AxisFactorDev* __restrict__ fac,
                                                          const int64_t* __restrict__ off,
-                                                         const int32_t* __restrict__ refine, int step,
+                                                         const int32_t* __restrict__ refine, int sel,
                                                          const int2* __restrict__ bands) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* tile = reinterpret_cast<R*>(smem_raw);
     if constexpr (!PERSIST) {
-        batch_solve_item<R>(data, items[blockIdx.x], tile, tables, fac, off, refine, step, bands);
+        batch_solve_item<R>(data, items[blockIdx.x], tile, tables, fac, off, refine, sel, bands);
     } else {
         for (;;) {
             unsigned int idx = 0;
             if (threadIdx.x == 0) idx = atomicAdd(counter, 1u);
             idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
             if (static_cast<int64_t>(idx) >= nitems) return;
-            batch_solve_item<R>(data, items[idx], tile, tables, fac, off, refine, step, bands);
+            batch_solve_item<R>(data, items[idx], tile, tables, fac, off, refine, sel, bands);
             __syncwarp();
         }
     }
 }
 
-// Residual pass j of the refinement over the value chunks (element-parallel,
-// 256 threads per chunk of at most kChunkElems values of one table): axis
-// D - 1 - j of the chunk's table, the operations of batch_stencil_kernel on
-// every element (dot2_band_row: mid = A_axis in as a double-float, or
-// corr = F - A_axis in on the table's last pass), with two elements per
-// thread in the packed form (dot2_add2) and the band known at compile time.
-template <int BAND, bool PERIODIC, bool HAS_LO, bool LAST>
-__device__ __forceinline__ void stencil_chunk(const float* __restrict__ ih, const float* __restrict__ il,
-                                              float* __restrict__ mid_hi, float* __restrict__ mid_lo,
-                                              float* __restrict__ corr, const float* __restrict__ fhi,
-                                              const float* __restrict__ flo, int start, int len, int n, int S,
-                                              const float2* __restrict__ val) {
-    constexpr int W = 2 * BAND + 1;
-    for (int e = threadIdx.x; e < len; e += 2 * blockDim.x) {
-        const int ea = start + e, eb = ea + static_cast<int>(blockDim.x);
-        const bool vb = e + static_cast<int>(blockDim.x) < len;
-        const int ia = (ea / S) % n, ib = vb ? (eb / S) % n : 0;
-        const int ba = ea - ia * S, bb = vb ? eb - ib * S : 0;
-        Dot2x2 acc{make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
-        if (LAST) {
-            acc.s = make_float2(fhi[ea], vb ? fhi[eb] : 0.0f);
-            acc.c = make_float2(flo[ea], vb ? flo[eb] : 0.0f);
-        }
-#pragma unroll
-        for (int d = 0; d < W; ++d) {
-            float2 a0 = __ldg(val + ia * W + d);
-            float2 a1 = vb ? __ldg(val + ib * W + d) : make_float2(0.0f, 0.0f);
-            const bool z0 = a0.x == 0.0f, z1 = a1.x == 0.0f;
-            if (z0 && z1) continue;
-            if (LAST) {
-                a0 = make_float2(-a0.x, -a0.y);
-                a1 = make_float2(-a1.x, -a1.y);
-            }
-            float2 xh = make_float2(0.0f, 0.0f), xl = make_float2(0.0f, 0.0f);
-            if (!z0) {
-                int c = ia - BAND + d;
-                if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
-                const int j = ba + c * S;
-                xh.x = __ldg(ih + j);
-                if (HAS_LO) xl.x = __ldg(il + j);
-            }
-            if (!z1) {
-                int c = ib - BAND + d;
-                if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
-                const int j = bb + c * S;
-                xh.y = __ldg(ih + j);
-                if (HAS_LO) xl.y = __ldg(il + j);
-            }
-            dot2_add2<HAS_LO>(acc, make_float2(a0.x, a1.x), make_float2(a0.y, a1.y), xh, xl);
-        }
-        if (LAST) {
-            const float2 v = __fadd2_rn(acc.s, acc.c);
-            corr[ea] = v.x;
-            if (vb) corr[eb] = v.y;
-        } else {
-            float2 h, l;
-            df_two_sum2(acc.s, acc.c, h, l);
-            mid_hi[ea] = h.x;
-            mid_lo[ea] = l.x;
-            if (vb) {
-                mid_hi[eb] = h.y;
-                mid_lo[eb] = l.y;
-            }
-        }
-    }
-}
-
-template <bool HAS_LO>
-__global__ void __launch_bounds__(256) batch_stencil_chunk_kernel(const float* __restrict__ in_hi,
-                                                                  const float* __restrict__ in_lo,
-                                                                  float* __restrict__ mid_hi, float* __restrict__ mid_lo,
-                                                                  float* __restrict__ corr,
-                                                                  const float* __restrict__ fhi,
-                                                                  const float* __restrict__ flo,
-                                                                  const ChunkItem* __restrict__ chunks,
-                                                                  const TableDev* __restrict__ tables,
-                                                                  const AxisFactorDev* __restrict__ fac,
-                                                                  const int64_t* __restrict__ off,
-                                                                  const int32_t* __restrict__ refine, int step,
-                                                                  int pass) {
-    const ChunkItem ck = chunks[blockIdx.x];
-    if (refine[ck.table] <= step) return;
-    const TableDev& t = tables[ck.table];
-    const int axis = t.dim - 1 - pass;
-    if (axis < 0) return;
-    const AxisDev& ax = t.ax[axis];
-    const AxisFactorDev& f = fac[ck.table * kBatchMaxDim + axis];
-    const int64_t o0 = off[ck.table];
-    const bool last = axis == 0;
-    // batched tables hold fewer than 2^31 values each: 32-bit index math
-    const int n = static_cast<int>(ax.n), S = static_cast<int>(ax.stride), start = static_cast<int>(ck.start);
-    const float* ih = in_hi + o0;
-    const float* il = HAS_LO ? in_lo + o0 : nullptr;
-    float *mh = mid_hi + o0, *ml = mid_lo + o0, *cr = corr + o0;
-    const float *fh = fhi + o0, *fl = flo + o0;
-#define INTP_BATCH_STENCIL(B)                                                                                      \
-    case B:                                                                                                        \
-        if (ax.periodic) {                                                                                         \
-            if (last)                                                                                              \
-                stencil_chunk<B, true, HAS_LO, true>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);      \
-            else                                                                                                   \
-                stencil_chunk<B, true, HAS_LO, false>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);     \
-        } else {                                                                                                   \
-            if (last)                                                                                              \
-                stencil_chunk<B, false, HAS_LO, true>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);     \
-            else                                                                                                   \
-                stencil_chunk<B, false, HAS_LO, false>(ih, il, mh, ml, cr, fh, fl, start, ck.len, n, S, f.sval);    \
-        }                                                                                                          \
-        return;
-    switch (f.band) {
-        INTP_BATCH_STENCIL(0)
-        INTP_BATCH_STENCIL(1)
-        INTP_BATCH_STENCIL(2)
-        INTP_BATCH_STENCIL(3)
-        INTP_BATCH_STENCIL(4)
-        INTP_BATCH_STENCIL(5)
-        INTP_BATCH_STENCIL(6)
-    }
-#undef INTP_BATCH_STENCIL
-}
-
 // Element-wise passes over chunk items:
-//  op 0: dst[shift(i)] = (R) src[i], or for refining tables with fhi (FP32
-//        destination) the double-float split of src[i] into fhi[shift(i)]
-//        (= dst) and flo[shift(i)]
-//  op 1: (ctrl, ctrl_lo)[i] += corr[i] in double-float  (refining tables only)
+//  op 0: dst[shift(i)] = (R) src[i]; in a mixed batch, for the tables solved
+//        in double-word arithmetic (refine > 0), the double-word split of
+//        src[i] into w[shift(i)] instead (the single-table shift copy's)
+//  op 1: (ctrl, ctrl_lo)[i] = (w[i].hi, w[i].lo)  (refine > 0 tables only)
 // The periodic shift moves index i to (i + O/2) mod n along every periodic
 // axis (InterpolationTemplate.hpp:451-462).
 template <class R>
 __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const double* __restrict__ src,
-                                                                R* __restrict__ dst, float* __restrict__ fhi,
-                                                                float* __restrict__ flo,
+                                                                R* __restrict__ dst, DW* __restrict__ w,
                                                                 float* __restrict__ ctrl_lo,
-                                                                const float* __restrict__ corr,
                                                                 const ChunkItem* __restrict__ chunks,
                                                                 const TableDev* __restrict__ tables,
                                                                 const int64_t* __restrict__ off,
-                                                                const int32_t* __restrict__ refine, int step) {
+                                                                const int32_t* __restrict__ refine) {
     const ChunkItem c = chunks[blockIdx.x];
-    if (op != 0 && refine[c.table] <= step) return;
+    const bool dw = w && refine[c.table] > 0;
+    if (op != 0 && !dw) return;
     const int64_t o0 = off[c.table];
     if (op == 0) {
         const TableDev& t = tables[c.table];
@@ -429,28 +321,21 @@ __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const do
                 o += idx * static_cast<int>(a.stride);
             }
             const double v = src[o0 + i];
-            if constexpr (sizeof(R) == 4) {
-                if (fhi && refine[c.table] > 0) {
-                    // integer split, as the single-table shift copy of a
-                    // refining table
-                    float h, l;
-                    split_double(v, h, l);
-                    dst[o0 + o] = h;
-                    fhi[o0 + o] = h;
-                    flo[o0 + o] = l;
-                    continue;
-                }
+            if (dw) {
+                float h, l;
+                split_double(v, h, l);
+                w[o0 + o] = DW(h, l);
+            } else {
+                dst[o0 + o] = static_cast<R>(v);
             }
-            dst[o0 + o] = static_cast<R>(v);
         }
     } else {
         float* x = reinterpret_cast<float*>(dst);
         for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
             const int64_t i = o0 + c.start + e;
-            float h = x[i], l = step > 0 ? ctrl_lo[i] : 0.0f;
-            df_correct(h, l, corr[i], step > 0);
-            x[i] = h;
-            ctrl_lo[i] = l;
+            const DW v = w[i];
+            x[i] = v.hi;
+            ctrl_lo[i] = v.lo;
         }
     }
 }
@@ -482,7 +367,9 @@ struct PassLists {
 
 void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<PassLists>& passes,
                 std::vector<ChunkItem>& chunks) {
-    const size_t esz = b.elem();
+    // staging bytes per element: 8 for FP64 and for the double-word solve of
+    // mixed batches (an FP32 pass then stages at most half its budget)
+    const size_t esz = b.mixed() ? sizeof(DW) : sizeof(double);
     const size_t stage = static_cast<size_t>(sc.stage_kb) * 1024;
     passes.assign(kBatchMaxDim, {});
     chunks.clear();
@@ -511,7 +398,6 @@ void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<
                 it.table = static_cast<int32_t>(i);
                 it.axis = static_cast<int16_t>(a);
                 it.staged = staged ? 1 : 0;
-                it.last = (a == 0) ? 1 : 0;
                 it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
                 it.line0 = l0;
                 const size_t need = staged ? static_cast<size_t>(it.rows) * static_cast<size_t>(n + 1) : 0;
@@ -588,7 +474,7 @@ int batch_sm_count() {
 
 template <class R, bool PERSIST>
 cudaError_t launch_items(intp_batch* b, R* data, const SolveItem* items, int64_t nitems, size_t smem_elems,
-                         unsigned int* counter, int step, const int2* bands, cudaStream_t s) {
+                         unsigned int* counter, int sel, const int2* bands, cudaStream_t s) {
     if (nitems == 0) return cudaSuccess;
     const size_t smem = smem_elems * sizeof(R);
     auto k = batch_solve_kernel<R, PERSIST>;
@@ -604,7 +490,7 @@ cudaError_t launch_items(intp_batch* b, R* data, const SolveItem* items, int64_t
         grid = std::min<int64_t>(nitems, static_cast<int64_t>(per_sm) * batch_sm_count());
     }
     k<<<static_cast<unsigned>(grid), 32, smem, s>>>(data, items, nitems, counter, b->d_tables, b->d_fac, b->d_off,
-                                                    b->d_refine, step, bands);
+                                                    b->d_refine, sel, bands);
     note_launch();
     return cudaGetLastError();
 }
@@ -613,7 +499,7 @@ cudaError_t launch_items(intp_batch* b, R* data, const SolveItem* items, int64_t
 // and its long-line launch. `launch` numbers the persistent launches of the
 // build (their work counters were cleared when the build started).
 template <class R>
-cudaError_t run_passes(intp_batch* b, R* data, int step, const int2* bands, int& launch, cudaStream_t s) {
+cudaError_t run_passes(intp_batch* b, R* data, int sel, const int2* bands, int& launch, cudaStream_t s) {
     for (int j = 0; j < b->npasses; ++j) {
         const intp_batch::Pass& p = b->pass[j];
         for (int part = 0; part < 2; ++part) {
@@ -623,9 +509,9 @@ cudaError_t run_passes(intp_batch* b, R* data, int step, const int2* bands, int&
             if (nitems == 0) continue;
             cudaError_t e;
             if (b->sched.persistent && launch < kMaxLaunches)
-                e = launch_items<R, true>(b, data, items, nitems, smem, b->counters + launch++, step, bands, s);
+                e = launch_items<R, true>(b, data, items, nitems, smem, b->counters + launch++, sel, bands, s);
             else
-                e = launch_items<R, false>(b, data, items, nitems, smem, nullptr, step, bands, s);
+                e = launch_items<R, false>(b, data, items, nitems, smem, nullptr, sel, bands, s);
             if (e != cudaSuccess) return e;
         }
     }
@@ -641,59 +527,42 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
     const unsigned nch = static_cast<unsigned>(b->nchunks);
     if (!b->mixed()) {
         double* c = static_cast<double*>(b->ctrl);
-        batch_elementwise_kernel<double><<<nch, 256, 0, s>>>(0, values, c, nullptr, nullptr, nullptr, nullptr,
-                                                             b->d_chunks, b->d_tables, b->d_off, b->d_refine, -1);
+        batch_elementwise_kernel<double><<<nch, 256, 0, s>>>(0, values, c, nullptr, nullptr, b->d_chunks, b->d_tables,
+                                                             b->d_off, b->d_refine);
         note_launch();
         BATCH_CUDA(cudaGetLastError(), "batch shift copy");
-        BATCH_CUDA(run_passes<double>(b, c, -1, bands, launch, s), "batch line solve (fp64)");
+        BATCH_CUDA(run_passes<double>(b, c, kSelAll, bands, launch, s), "batch line solve (fp64)");
         b->has_ctrl = true;
         return INTP_OK;
     }
+    // mixed: the tables with refine = 0 solve in FP32 in place; the others
+    // (all by default) in double-word arithmetic on a working array, split
+    // into (ctrl, ctrl_lo) at the end -- the single-table solve's operations
     float* c = static_cast<float*>(b->ctrl);
-    float *fhi = nullptr, *flo = nullptr, *corr = nullptr;
-    float* ping[2][2] = {};
+    DW* w = nullptr;
     if (b->max_refine > 0) {
-        const size_t need = static_cast<size_t>(N) * 28 + 1024;
+        const size_t need = static_cast<size_t>(N) * sizeof(DW) + 1024;
         if (b->scratch_bytes < need) {
             if (b->scratch) cudaFree(b->scratch);
             b->scratch = nullptr;
             b->scratch_bytes = 0;
-            BATCH_CUDA(cudaMalloc(&b->scratch, need), "cudaMalloc(batch refinement scratch)");
+            BATCH_CUDA(cudaMalloc(&b->scratch, need), "cudaMalloc(batch double-word scratch)");
             b->scratch_bytes = need;
         }
-        float* p = static_cast<float*>(b->scratch);
-        fhi = p;
-        flo = p + N;
-        ping[0][0] = p + 2 * N;
-        ping[0][1] = p + 3 * N;
-        ping[1][0] = p + 4 * N;
-        ping[1][1] = p + 5 * N;
-        corr = p + 6 * N;
+        w = static_cast<DW*>(b->scratch);
     }
-    batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(0, values, c, fhi, flo, nullptr, nullptr, b->d_chunks,
-                                                        b->d_tables, b->d_off, b->d_refine, -1);
+    batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(0, values, c, w, nullptr, b->d_chunks, b->d_tables, b->d_off,
+                                                        b->d_refine);
     note_launch();
     BATCH_CUDA(cudaGetLastError(), "batch shift copy");
-    BATCH_CUDA(run_passes<float>(b, c, -1, bands, launch, s), "batch line solve (fp32)");
-    for (int step = 0; step < b->max_refine; ++step) {
-        // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass, double-float:
-        // c -> ping[0] -> ping[1] -> ..., each table's last pass writing corr
-        const float *ih = c, *il = step > 0 ? b->ctrl_lo : nullptr;
-        for (int j = 0; j < b->npasses; ++j) {
-            float** out = ping[j & 1];
-            auto k = il ? batch_stencil_chunk_kernel<true> : batch_stencil_chunk_kernel<false>;
-            k<<<nch, 256, 0, s>>>(ih, il, out[0], out[1], corr, fhi, flo, b->d_chunks, b->d_tables, b->d_fac, b->d_off,
-                                  b->d_refine, step, j);
-            note_launch();
-            BATCH_CUDA(cudaGetLastError(), "batch residual");
-            ih = out[0];
-            il = out[1];
-        }
-        BATCH_CUDA(run_passes<float>(b, corr, step, bands, launch, s), "batch line solve (correction)");
-        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, c, nullptr, nullptr, b->ctrl_lo, corr,
-                                                            b->d_chunks, b->d_tables, b->d_off, b->d_refine, step);
+    if (b->min_refine == 0)
+        BATCH_CUDA(run_passes<float>(b, c, kSelPlain, bands, launch, s), "batch line solve (fp32)");
+    if (w) {
+        BATCH_CUDA(run_passes<DW>(b, w, kSelDW, bands, launch, s), "batch line solve (double-word)");
+        batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, c, w, b->ctrl_lo, b->d_chunks, b->d_tables,
+                                                            b->d_off, b->d_refine);
         note_launch();
-        BATCH_CUDA(cudaGetLastError(), "batch correction");
+        BATCH_CUDA(cudaGetLastError(), "batch double-word split");
     }
     b->has_ctrl = true;
     return INTP_OK;
@@ -762,8 +631,9 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
             }
             b->off[i + 1] = b->off[i] + b->models[i].total;
             if (b->mixed()) {
-                b->refine[i] = d.refine_steps < 0 ? auto_refine_steps(b->models[i]) : d.refine_steps;
+                b->refine[i] = d.refine_steps == 0 ? 0 : 1;
                 b->max_refine = std::max(b->max_refine, b->refine[i]);
+                b->min_refine = std::min(b->min_refine, b->refine[i]);
             }
         }
     } catch (const std::bad_alloc&) {

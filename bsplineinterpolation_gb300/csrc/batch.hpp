@@ -20,7 +20,7 @@ struct SolveItem {
     int32_t table;
     int16_t axis;
     int8_t staged;
-    int8_t last;    // the table's final residual pass (axis 0)
+    int8_t pad8;
     int32_t rows;
     int32_t pad;
     int64_t line0;

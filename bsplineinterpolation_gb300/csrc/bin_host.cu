@@ -5,7 +5,6 @@
 
 #include <algorithm>
 #include <cstdlib>
-#include <cstring>
 
 #include "bin_impl.cuh"
 
@@ -138,36 +137,21 @@ int sm_count() {
     return n;
 }
 
-// INTP_GB300_SORT=permute: the three-pass sort (records written in input
-// order, then moved); default: count, then scatter from the coordinates.
-bool sort_two_pass() {
-    const char* v = std::getenv("INTP_GB300_SORT");
-    return !(v && std::strcmp(v, "permute") == 0);
-}
-
 template <int D>
 cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec, uint32_t* rank,
-                        uint32_t* rec, int64_t slice, cudaStream_t s) {
+                        uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec, int64_t slice,
+                        cudaStream_t s) {
     using namespace bin_detail;
     const size_t smem = static_cast<size_t>(g.nbuckets) * 4;
-    const bool two = sort_two_pass();
-    auto kl = locate_kernel<D>;
-    auto kp = permute_kernel<D>;
     auto kc = count_kernel<D>;
     auto ks = scatter_kernel<D>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaSuccess;
-        for (const void* k : {reinterpret_cast<const void*>(kl), reinterpret_cast<const void*>(kp),
-                              reinterpret_cast<const void*>(kc), reinterpret_cast<const void*>(ks)})
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t e = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    if (two)
-        kc<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, blkcount);
-    else
-        kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, rank, blkcount);
+    kc<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, blkcount);
     note_launch();
     const int64_t m = g.nbuckets * nblk;
     const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -177,10 +161,7 @@ cudaError_t launch_sort(const TableDev& t, const BinGeom& g, const double* coord
     note_launch();
     scan_apply_kernel<<<static_cast<int>(ntiles), kScanThreads, 0, s>>>(blkcount, m, tile_sum, blkoffset);
     note_launch();
-    if (two)
-        ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, rec);
-    else
-        kp<<<nblk * kPermuteParts, kSortThreads, smem, s>>>(g, n, slice, in_rec, rank, blkoffset, rec);
+    ks<<<nblk, kSortThreads, smem, s>>>(t, g, coords, n, slice, blkoffset, rec);
     note_launch();
     return cudaGetLastError();
 }
@@ -199,7 +180,7 @@ cudaError_t launch_span_readout(const TableDev& t, const BinGeom& g, const doubl
         if (e != cudaSuccess) return e;
     }
     const int64_t slice = (n + nblk - 1) / nblk;
-    kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, nullptr, blkcount);
+    kl<<<nblk, kLocateThreads, smem, s>>>(t, g, coords, n, slice, in_rec, blkcount);
     note_launch();
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, int64_t{sm_count()} * 8);
     decode_spans_kernel<D><<<static_cast<int>(blocks), 256, 0, s>>>(g, t.order, in_rec, n, cells);
@@ -210,16 +191,16 @@ cudaError_t launch_span_readout(const TableDev& t, const BinGeom& g, const doubl
 int bin_record_words(int dim) { return dim == 1 ? bin_detail::rec_words<1>() : bin_detail::rec_words<2>(); }
 
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
-                           uint32_t* rank, uint32_t* rec, int64_t* slice, cudaStream_t s) {
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec, int64_t* slice,
+                           cudaStream_t s) {
     if (nblk < 1 || nblk > bin_detail::kMaxSortBlocks) return cudaErrorInvalidValue;
     const int64_t sl = (n + nblk - 1) / nblk;
     if (sl >= bin_detail::kMaxSlice) return cudaErrorInvalidValue;
     *slice = sl;
     switch (t.dim) {
-        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
-        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
-        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, sl, s);
+        case 1: return launch_sort<1>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, sl, s);
+        case 2: return launch_sort<2>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, sl, s);
+        case 3: return launch_sort<3>(t, g, coords, n, nblk, blkcount, blkoffset, tile_sum, rec, sl, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -305,8 +286,7 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t b_m = up(static_cast<size_t>(m) * 4), b_t = up(static_cast<size_t>(ntiles) * 4);
     const size_t b_r = up(static_cast<size_t>(cap) * 4 * bin_record_words(D));
-    const size_t b_k = up(static_cast<size_t>(cap) * 4);  // ranks
-    const size_t total = b_m * 2 + b_t + b_r * 2 + b_k;
+    const size_t total = b_m * 2 + b_t + b_r;
     void* mem = nullptr;
     cudaError_t e = cudaMallocAsync(&mem, total, s);
     if (e != cudaSuccess) return e;
@@ -317,11 +297,7 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     p += b_m;
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += b_t;
-    uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
-    p += b_r;
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
-    p += b_r;
-    uint32_t* rank = reinterpret_cast<uint32_t*>(p);
     const int K = plan.k;
     const size_t ob = out_f32 ? 4 : 8;
     const int grid_eval = sm_count();  // the launchers fill each SM
@@ -329,7 +305,7 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
         const int64_t n = std::min(cap, npts - p0);
         const double* c = coords + p0 * D;
         int64_t slice = 0;
-        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, in_rec, rank, rec, &slice, s);
+        e = bin_sort_chunk(t, g, c, n, nblk, blkcount, blkoffset, tile_sum, rec, &slice, s);
         if (e != cudaSuccess) break;
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * K * ob;
         e = D <= 2 ? launch_bin_eval_d12(t, g, tmap, blkoffset, nblk, slice, rec, n, plan, o, out_f32, grid_eval, s)

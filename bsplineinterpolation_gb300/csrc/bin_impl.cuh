@@ -7,20 +7,21 @@
 // every query of a bucket comes from one tile of prod(B_d + O) control points
 // staged once in shared memory.
 //
-//   locate:  exact span (integer keys) and FP32 local offsets of every query,
-//            one 8- or 16-byte record per query in input order, and
-//            per-(bucket, CTA) counts
+//   count:   exact spans of every query of a sort CTA's input slice, and the
+//            slice's per-bucket counts (per-(bucket, CTA) pairs)
 //   scan:    exclusive prefix sum over (bucket, CTA) -> first slot of each pair
-//   permute: every record moves to its pair's first slot plus its rank in the
-//            pair (counted by locate): one vector store, no atomics
+//   scatter: the same CTA recomputes each query's record (spans and FP32
+//            local offsets) and writes it to the next free slot of its pair
 //   eval:    CTA j takes the j-th equal slice of the sorted records, stages the
 //            tile of each bucket it meets with asynchronous copies, evaluates,
 //            writes out[index]
 //
-// Locate and permute aggregate their shared-memory atomics per warp
+// Count and scatter aggregate their shared-memory atomics per warp
 // (__match_any_sync): lanes of a warp that fall into one bucket take
 // consecutive slots with a single atomic, so clustered queries neither
-// serialise on a counter nor scatter their records.
+// serialise on a counter nor scatter their records. Recomputing the records
+// costs less than writing them in input order and moving them: a record is
+// written once (16 bytes per query) and read once.
 //
 // Queries are processed in chunks of the input, as large as a record's
 // 20-bit slice index allows (up to 2^28 queries): each bucket's tile is staged
@@ -44,7 +45,6 @@ namespace bin_detail {
 constexpr int kBinThreads = 256;   // evaluation CTA
 constexpr int kLocateThreads = 768;  // count CTA (two per SM at up to 42 registers)
 constexpr int kSortThreads = 768;    // scatter CTA (two per SM at up to 42 registers)
-constexpr int kPermuteParts = 1;     // scatter CTAs per count CTA's slice
 
 // Exact span and FP32 local offset of one coordinate on axis a (mixed form),
 // with 32-bit span indices (binned tables have fewer than 2^31 knots per
@@ -122,21 +122,13 @@ __device__ __forceinline__ void rec_load(const uint32_t* rec, int64_t slot, uint
     }
 }
 
-// Counting sort without global atomics. CTA `blk` owns the input slice
-// [blk*S, (blk+1)*S) (S < 2^20).
-//   locate:  exact spans and FP32 offsets of every query of the slice, one
-//            record per query written in input order, and the slice's
-//            per-bucket counts in blkcount[b * nblk + blk] (bucket-major);
-//   scan:    exclusive prefix sum over (bucket, CTA): the first slot of every
-//            pair (the first slot of bucket b is scan[b * nblk]);
-//   permute: moves every record of the slice to its pair's first slot plus
-//            the record's rank within the pair (written by locate).
-// Shared-memory atomics are aggregated per warp (__match_any_sync), and every
-// thread runs the same number of loop trips so the match sees all lanes.
+// Records of every query of the slice in input order, and the slice's
+// per-(bucket, CTA) counts: the read-out of the binned path's spans
+// (intp_locate_binned) decodes these records. Same spans and offsets as the
+// count and scatter kernels (span_and_offset).
 template <int D>
 __global__ void __launch_bounds__(kLocateThreads, 2) locate_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
                                                              int64_t n, int64_t slice, uint32_t* __restrict__ in_rec,
-                                                             uint32_t* __restrict__ rank,
                                                              uint32_t* __restrict__ blkcount) {
     extern __shared__ uint32_t sh_count[];
     const int nblk = gridDim.x, blk = blockIdx.x;
@@ -160,14 +152,10 @@ __global__ void __launch_bounds__(kLocateThreads, 2) locate_kernel(TableDev t, B
             b = bucket_of<D>(g, cl);
             rec_store<D>(in_rec, p, u, (b << kCellBits) | cell);
         }
-        // the query's rank among its CTA's queries of the bucket: one atomic
-        // per group of lanes with the same bucket
+        // one atomic per group of lanes with the same bucket
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
         const int leader = __ffs(peers) - 1;
-        uint32_t first = 0;
-        if (valid && lane == leader) first = atomicAdd(&sh_count[b], static_cast<uint32_t>(__popc(peers)));
-        first = __shfl_sync(0xFFFFFFFFu, first, leader);
-        if (valid && rank) rank[p] = first + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
+        if (valid && lane == leader) atomicAdd(&sh_count[b], static_cast<uint32_t>(__popc(peers)));
     }
     __syncthreads();
     for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) blkcount[b * nblk + blk] = sh_count[b];
@@ -212,8 +200,8 @@ __global__ void __launch_bounds__(kLocateThreads, 2) count_kernel(TableDev t, Bi
 // writes it to the next free slot of its (bucket, CTA) pair, taken from a
 // shared-memory cursor that starts at the pair's first slot (warp-aggregated
 // atomics). The order of records within a pair depends on timing; each
-// query's outputs do not. The tag holds the query's index within the slice,
-// as in permute_kernel's output.
+// query's outputs do not. The tag holds the query's index within the slice
+// (the evaluation finds the slice from the pair the slot lies in).
 template <int D>
 __global__ void __launch_bounds__(kSortThreads, 2) scatter_kernel(TableDev t, BinGeom g, const double* __restrict__ coords,
                                                               int64_t n, int64_t slice,
@@ -247,53 +235,6 @@ __global__ void __launch_bounds__(kSortThreads, 2) scatter_kernel(TableDev t, Bi
         if (valid) {
             const uint32_t slot = first + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
             rec_store<D>(rec, slot, u, (static_cast<uint32_t>(p - p0) << kCellBits) | cell);
-        }
-    }
-}
-
-// Every record of the slice to slot = (first slot of its (bucket, CTA) pair)
-// + (its rank there, from the locate kernel): independent streaming copies,
-// three records per thread and trip with all loads in flight. CTA j takes
-// part j % kPermuteParts of count CTA j / kPermuteParts's slice.
-template <int D>
-__global__ void __launch_bounds__(kSortThreads, 2) permute_kernel(BinGeom g, int64_t n, int64_t slice,
-                                                              const uint32_t* __restrict__ in_rec,
-                                                              const uint32_t* __restrict__ rank,
-                                                              const uint32_t* __restrict__ blkoffset,
-                                                              uint32_t* __restrict__ rec) {
-    extern __shared__ uint32_t sh_first[];
-    constexpr int RW = rec_words<D>();
-    constexpr int U = 3;
-    const int nblk = gridDim.x / kPermuteParts, blk = blockIdx.x / kPermuteParts;
-    const int part = blockIdx.x - blk * kPermuteParts;
-    for (int64_t b = threadIdx.x; b < g.nbuckets; b += blockDim.x) sh_first[b] = __ldg(blkoffset + b * nblk + blk);
-    __syncthreads();
-    const int64_t s0 = blk * slice, s1 = (s0 + slice < n) ? s0 + slice : n;
-    const int64_t p0 = s0 + (s1 - s0) * part / kPermuteParts, p1 = s0 + (s1 - s0) * (part + 1) / kPermuteParts;
-    constexpr uint32_t cell_mask = (1u << kCellBits) - 1u;
-    for (int64_t base = p0; base < p1; base += U * static_cast<int64_t>(blockDim.x)) {
-        uint32_t w[U][RW];
-        uint32_t rk[U];
-#pragma unroll
-        for (int j = 0; j < U; ++j) {
-            const int64_t p = base + j * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-            if (p < p1) {
-                rec_load<D>(in_rec, p, w[j]);
-                rk[j] = __ldg(rank + p);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < U; ++j) {
-            const int64_t p = base + j * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-            if (p < p1) {
-                const uint32_t tag = w[j][RW - 1];
-                const uint32_t slot = sh_first[tag >> kCellBits] + rk[j];
-                w[j][RW - 1] = (static_cast<uint32_t>(p - s0) << kCellBits) | (tag & cell_mask);
-                if constexpr (D == 1)
-                    reinterpret_cast<uint2*>(rec)[slot] = make_uint2(w[j][0], w[j][1]);
-                else
-                    reinterpret_cast<uint4*>(rec)[slot] = make_uint4(w[j][0], w[j][1], w[j][2], w[j][3]);
-            }
         }
     }
 }

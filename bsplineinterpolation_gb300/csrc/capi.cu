@@ -113,6 +113,12 @@ std::vector<float> to_f32(const std::vector<double>& v) {
     return r;
 }
 
+std::vector<DW> to_dw(const std::vector<double>& v) {
+    std::vector<DW> r(v.size());
+    for (size_t i = 0; i < v.size(); ++i) r[i] = dw_from_double(v[i]);
+    return r;
+}
+
 }  // namespace
 
 struct intp_table {
@@ -163,7 +169,9 @@ struct intp_table {
     }
     bool mixed() const { return precision == INTP_PRECISION_MIXED; }
     // refinement steps of the mixed solve (the automatic choice resolved)
-    int steps() const { return !mixed() ? 0 : refine_steps < 0 ? auto_refine_steps(model) : refine_steps; }
+    // mixed form: 1 = the double-word solve (control points as FP32 pairs),
+    // 0 = the plain FP32 solve (refine_steps = 0)
+    int steps() const { return !mixed() ? 0 : refine_steps == 0 ? 0 : 1; }
     size_t elem() const { return mixed() ? sizeof(float) : sizeof(double); }
     int64_t values() const { return model.total * channels; }  // control points over all channels
 };
@@ -327,6 +335,18 @@ cudaError_t solve_f32_all(intp_table* t, float* x, cudaStream_t s) {
     return cudaSuccess;
 }
 
+cudaError_t solve_dw_all(intp_table* t, DW* x, cudaStream_t s) {
+    for (int a = t->model.dim - 1; a >= 0; --a) {
+        const LineGeom g = line_geom(t, a);
+        const AxisFactorDev& f = t->fac[a];
+        const LineFactor& lf = t->model.axis[a].factor;
+        cudaError_t e = launch_line_solve_dw(x, g.n, g.S, g.nlines, lf.p, lf.q, lf.cyclic, f.lowerw, f.upperw, f.dinvw,
+                                             f.bottomw, f.rightw, s, f.clo, f.chi, f.zside);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t solve_f64_all(intp_table* t, double* x, cudaStream_t s) {
     for (int a = t->model.dim - 1; a >= 0; --a) {
         const LineGeom g = line_geom(t, a);
@@ -356,37 +376,16 @@ intp_status run_interpolate(intp_table* t, const double* values_dev, cudaStream_
         INTP_CUDA(launch_shift_copy_f64_f32(values_dev, c, nullptr, nullptr, sd, s), "shift copy");
         INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
     } else {
-        // Refinement in double-float: F split into (fhi, flo), residual
-        // passes ping-pong between two double-float buffers, the last one
-        // writing r = F - A c in FP32; the correction solve runs in place on
-        // r, and the control points accumulate it as (ctrl, ctrl_lo).
-        const size_t need = static_cast<size_t>(N) * 28 + 1024;
+        // Double-word solve: the shifted values split into double-words, one
+        // band substitution per axis in double-word arithmetic (R = DW), the
+        // solution split into the control points' two FP32 arrays.
+        const size_t need = static_cast<size_t>(N) * sizeof(DW) + 1024;
         intp_status st = ensure_scratch(t, need);
         if (st != INTP_OK) return st;
-        float* b = static_cast<float*>(t->scratch);
-        float *fhi = b, *flo = b + N, *corr = b + 6 * N;
-        float* ping[2][2] = {{b + 2 * N, b + 3 * N}, {b + 4 * N, b + 5 * N}};
-        INTP_CUDA(launch_shift_copy_f64_f32(values_dev, fhi, flo, c, sd, s), "shift copy");
-        INTP_CUDA(solve_f32_all(t, c, s), "line solve (fp32)");
-        for (int it = 0; it < steps; ++it) {
-            // r = F - (A_0 x ... x A_{D-1}) c, one axis per pass
-            const float *ih = c, *il = it > 0 ? t->ctrl_lo : nullptr;
-            int pp = 0;
-            for (int a = m.dim - 1; a >= 0; --a) {
-                const LineGeom g = line_geom(t, a);
-                const AxisFactorDev& f = t->fac[a];
-                const bool last = a == 0;
-                cudaError_t e = launch_residual_pass(ih, il, last ? nullptr : ping[pp][0], last ? nullptr : ping[pp][1],
-                                                     last ? fhi : nullptr, last ? flo : nullptr, last ? corr : nullptr,
-                                                     g.n, g.S, N, f.band, m.axis[a].periodic, f.sval, s);
-                if (e != cudaSuccess) return cuda_fail(e, "residual");
-                ih = ping[pp][0];
-                il = ping[pp][1];
-                pp ^= 1;
-            }
-            INTP_CUDA(solve_f32_all(t, corr, s), "line solve (correction)");
-            INTP_CUDA(launch_correct(c, t->ctrl_lo, corr, N, it > 0, s), "correction");
-        }
+        DW* w = static_cast<DW*>(t->scratch);
+        INTP_CUDA(launch_shift_copy_f64_dw(values_dev, w, sd, s), "shift copy");
+        INTP_CUDA(solve_dw_all(t, w, s), "line solve (double-word)");
+        INTP_CUDA(launch_dw_unpack(w, c, t->ctrl_lo, N, s), "double-word split");
     }
     t->has_ctrl = true;
     return INTP_OK;
@@ -483,25 +482,6 @@ bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv,
     return true;
 }
 
-int auto_refine_steps(const TableModel& m) {
-    // The FP32 solve's relative error is about e0 = 6e-8 * sum_d kappa_d
-    // (kappa ~ 3 per axis for cubic collocation, tens for periodic order
-    // >= 6). Each double-float residual step multiplies the error by about
-    // e0, with the control points kept as double-floats (no FP32 storage
-    // floor). One step always: a derivative multiplies the control points'
-    // error by about the axis length per order, so the FP32 solve alone
-    // leaves derivatives above 1e-6. Further steps until about 1e-12, enough
-    // for second derivatives of a 512-point axis.
-    const double e0 = fp32_solve_error_estimate(m);
-    double e = e0 * e0;
-    int steps = 1;
-    while (e > 1e-12 && steps < 4) {
-        e *= e0;
-        ++steps;
-    }
-    return steps;
-}
-
 intp_status create_table(const intp_table_desc* desc, bool stream_ordered, cudaStream_t stream, intp_table** out) {
     if (!desc || !out) return fail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
@@ -562,9 +542,10 @@ size_t table_device_bytes(const intp_table* t) {
 size_t table_build_scratch_bytes(const intp_table_desc* desc) {
     int64_t total = 1;
     for (int d = 0; d < desc->dim && d < INTP_GPU_MAX_DIM; ++d) total *= desc->size[d];
-    // values staging (FP64) plus, in the mixed form, the refinement buffers
+    // values staging (FP64) plus, in the mixed form, the double-word solve's
+    // working array
     size_t b = static_cast<size_t>(total) * 8;
-    if (desc->precision == INTP_PRECISION_MIXED) b += static_cast<size_t>(total) * (8 * 3 + 4);
+    if (desc->precision == INTP_PRECISION_MIXED) b += static_cast<size_t>(total) * sizeof(DW);
     return b;
 }
 
@@ -618,16 +599,11 @@ void pack_table(const TableModel& m, Arena& ar, PackedTable& pt) {
         o.dinvf = ar.put(to_f32(f.dinv));
         o.bottomf = ar.put(to_f32(f.bottom));
         o.rightf = ar.put(to_f32(f.right));
-        // collocation rows as a band stencil of double-float values (row i,
-        // tap d: column i - band + d, cyclic on a periodic axis)
-        const RowStencil& st = ax.stencil;
-        std::vector<float2> val2(st.val.size());
-        for (size_t k = 0; k < val2.size(); ++k) {
-            const double v = st.val[k];
-            const float h = static_cast<float>(v);
-            val2[k] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
-        }
-        o.sval = ar.put(val2);
+        o.lowerw = ar.put(to_dw(f.lower));
+        o.upperw = ar.put(to_dw(f.upper));
+        o.dinvw = ar.put(to_dw(f.dinv));
+        o.bottomw = ar.put(to_dw(f.bottom));
+        o.rightw = ar.put(to_dw(f.right));
     }
 }
 
@@ -690,8 +666,11 @@ void bind_table(const TableModel& m, const double* lo_user, const PackedTable& p
         fd.dinvf = reinterpret_cast<const float*>(base + o.dinvf);
         fd.bottomf = reinterpret_cast<const float*>(base + o.bottomf);
         fd.rightf = reinterpret_cast<const float*>(base + o.rightf);
-        fd.sval = reinterpret_cast<const float2*>(base + o.sval);
-        fd.band = (ax.stencil.width - 1) / 2;
+        fd.lowerw = reinterpret_cast<const DW*>(base + o.lowerw);
+        fd.upperw = reinterpret_cast<const DW*>(base + o.upperw);
+        fd.dinvw = reinterpret_cast<const DW*>(base + o.dinvw);
+        fd.bottomw = reinterpret_cast<const DW*>(base + o.bottomw);
+        fd.rightw = reinterpret_cast<const DW*>(base + o.rightw);
         fd.clo = ax.factor.const_lo;
         fd.chi = ax.factor.const_hi;
         fd.clo32 = ax.factor.const_lo32;
@@ -1206,9 +1185,8 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     const int64_t m = bins ? g.nbuckets * kNoAllocSortBlocks : 0;
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     const size_t fixed = up(static_cast<size_t>(m) * 4) * 2 + up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    // per query: two records (in input order and in bucket order) and its
-    // rank within its (bucket, sort CTA) pair
-    const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D)) * 2 + 4;
+    // per query: its record (in bucket order)
+    const size_t per_rec = static_cast<size_t>(4 * bin_record_words(D));
     if (bins && fixed + 1024 * per_rec + 512 > kNoAllocScratchBytes)
         return fail(INTP_ERR_INVALID_ARGUMENT,
                     "table has too many buckets (" + std::to_string(g.nbuckets) +
@@ -1229,15 +1207,10 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
     p += up(static_cast<size_t>(m) * 4);
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += up(static_cast<size_t>((m + 4095) / 4096) * 4);
-    const size_t rec_bytes = static_cast<size_t>(cap) * 4 * bin_record_words(D);
-    uint32_t* in_rec = reinterpret_cast<uint32_t*>(p);
-    p += up(rec_bytes);
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
-    p += up(rec_bytes);
-    uint32_t* rank = reinterpret_cast<uint32_t*>(p);
     // every word the kernels read is written earlier in the same chunk (counts
-    // by the locate kernel, offsets by the scan, records by locate and
-    // permute), so nothing in the area has to be cleared between calls
+    // by the count kernel, offsets by the scan, records by the scatter), so
+    // nothing in the area has to be cleared between calls
     int sms = 1;
     INTP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     const size_t ob = out_f32 ? 4 : 8;
@@ -1245,7 +1218,7 @@ intp_status intp_eval_noalloc(const intp_table* t, const double* coords, int64_t
         const int64_t n = std::min(cap, npts - p0);
         int64_t slice = 0;
         INTP_CUDA(bin_sort_chunk(t->dev, g, coords + p0 * D, n, kNoAllocSortBlocks, blkcount, blkoffset, tile_sum,
-                                 in_rec, rank, rec, &slice, s),
+                                 rec, &slice, s),
                   "binned sort");
         void* o = static_cast<unsigned char*>(out) + static_cast<size_t>(p0) * plan.k * ob;
         const CUtensorMap* tm = t->has_tile_map ? t->tile_map : nullptr;

@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "device_common.cuh"
+#include "dw.cuh"
 
 namespace intp_gb300 {
 
@@ -33,14 +34,13 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
                             int64_t npts, const DerivPlan& plan, void* out, bool out_f32, int64_t chunk,
                             cudaStream_t s);
 // One chunk's counting sort by bucket into caller-provided scratch: blkcount
-// and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096);
-// in_rec and rec hold n records of bin_record_words(D) words each (queries
-// in input order, then in bucket order), rank n words (each query's rank
-// within its (bucket, sort CTA) pair). Needs n <= nblk * 2^20. Returns the
-// slice of input queries each sort CTA took (for the evaluation).
+// and blkoffset hold nbuckets * nblk entries, tile_sum ceil(that / 4096); rec
+// holds n records of bin_record_words(D) words each, in bucket order. Needs
+// n <= nblk * 2^20. Returns the slice of input queries each sort CTA took
+// (for the evaluation).
 cudaError_t bin_sort_chunk(const TableDev& t, const BinGeom& g, const double* coords, int64_t n, int nblk,
-                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* in_rec,
-                           uint32_t* rank, uint32_t* rec, int64_t* slice, cudaStream_t s);
+                           uint32_t* blkcount, uint32_t* blkoffset, uint32_t* tile_sum, uint32_t* rec, int64_t* slice,
+                           cudaStream_t s);
 int bin_record_words(int dim);
 // (launch_bin_eval_*: `grid` is the SM count; the launchers place as many
 // evaluation CTAs per SM as fit.)
@@ -95,21 +95,21 @@ cudaError_t launch_proxy_build(const TableDev& t, bool mixed, const double* coor
 cudaError_t launch_proxy_eval(const TableDev* tables, int ntables, int dim, int order, bool mixed, int64_t npts,
                               const int64_t* cells, const void* xr, const void* base, const DerivPlan& plan, void* out,
                               int out_f32, cudaStream_t s);
+// The mixed form's double-word line solve (same substitution as the FP32 and
+// FP64 solves, R = DW), its right-hand side (the shifted values split into
+// double-words) and the split of its solution into the table's two FP32
+// arrays.
+cudaError_t launch_line_solve_dw(DW* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                 const DW* lower, const DW* upper, const DW* dinv, const DW* bottom, const DW* right,
+                                 cudaStream_t s, int64_t clo = 0, int64_t chi = 0, int64_t zside = INT64_MAX);
+cudaError_t launch_shift_copy_f64_dw(const double* src, DW* dst, const ShiftDesc& sd, cudaStream_t s);
+cudaError_t launch_dw_unpack(const DW* w, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s);
 // FP32 copy; with dst_lo the double-float split (dst + dst_lo = the value),
 // the high part written to dst2 as well.
 cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_lo, float* dst2, const ShiftDesc& sd,
                                       cudaStream_t s);
-// One double-float residual pass along an axis (n points, stride S) over N
-// values with the axis' band stencil (band half-width `band`, values val):
-// out = A in, or r = rhs - A in (FP32) when rhs_hi is given. in_lo may be
-// null (plain FP32 input).
-cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
-                                 const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
-                                 int band, bool periodic, const float2* val, cudaStream_t s);
-// (c, lo) += corr in double-float (lo read as 0 unless has_lo).
-cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s);
 // Reads and clears the device error flag set by a kernel whose bounded wait
 // ran out (0 = none).
 int take_device_error(cudaStream_t s);

@@ -23,7 +23,7 @@
 
 #include "basis32.cuh"
 #include "device_common.cuh"
-#include "refine_df.cuh"
+#include "dot2.cuh"
 
 namespace intp_gb300 {
 
@@ -128,7 +128,7 @@ __device__ __forceinline__ void mixed_point_outputs(const TableDev& t, const Der
 //    double-float, (c_hi - ref_hi) + (c_lo - ref_lo), so their rounding
 //    scales with the variation across the stencil, not across a tile;
 //  - derivative weights from the basis recursion (axis_weights32_precise);
-//  - compensated accumulation (Dot2, refine_df.cuh) of every partial sum
+//  - compensated accumulation (Dot2, dot2.cuh) of every partial sum
 //    of the separable contraction, carried as double-floats between axes.
 // fetch(idx) returns the FP32 operand of control point (c_d - O + idx_d)_d;
 // ref = ref_hi + ref_lo is the central control point, added back to values.

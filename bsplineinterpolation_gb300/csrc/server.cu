@@ -18,9 +18,7 @@
 // when there are two or more) take small requests only (evaluations of up to
 // kSmallPoints points, builds of up to kSmallValues values) and run on
 // high-priority streams, so that small requests neither queue behind large
-// ones for a slot nor wait for their kernels on the device; and at most
-// kMaxLargeInflight large units run at once, so that the host-to-device copy
-// queue, which serves every stream in order, stays short.
+// ones for a slot nor wait for their kernels on the device.
 //
 // Memory: resident tables plus the transient bytes of the work in flight stay
 // within the configured budget. At creation the server reserves
@@ -65,9 +63,9 @@ constexpr int kMaxSlots = 64;
 constexpr uint64_t kDefaultBudget = uint64_t{150} << 30;
 constexpr int64_t kDefaultMaxBatchPoints = int64_t{1} << 24;
 // transient bytes of the binned evaluation (batches of at least
-// kBinnedPoints queries): per query two 16-byte sort records and a 4-byte
-// rank, plus an allowance for the per-bucket bookkeeping
-constexpr size_t kEvalScratchPerPoint = 36;
+// kBinnedPoints queries): per query its 16-byte sort record, plus an
+// allowance for the per-bucket bookkeeping
+constexpr size_t kEvalScratchPerPoint = 16;
 constexpr size_t kEvalScratchFixed = size_t{16} << 20;
 constexpr int64_t kBinnedPoints = int64_t{1} << 18;
 // work-unit bounds: the largest evaluation unit (larger requests are split),
@@ -75,11 +73,6 @@ constexpr int64_t kBinnedPoints = int64_t{1} << 18;
 constexpr int64_t kPiecePoints = int64_t{1} << 21;
 constexpr int64_t kSmallPoints = int64_t{1} << 16;
 constexpr int64_t kSmallValues = int64_t{1} << 18;
-// large units (evaluation pieces above kSmallPoints, builds above
-// kSmallValues) in flight at once: their host-to-device copies share the copy
-// engines first come first served, so more of them in flight only lengthens
-// the copy queue that a small request's copy waits behind
-constexpr int kMaxLargeInflight = 3;
 // device memory reserved in the stream-ordered pool at creation (at most the
 // budget): tables and work units are carved from it, so an admission does not
 // wait for the driver to map new memory while requests queue behind it
@@ -135,7 +128,6 @@ struct Part {
 
 struct Unit {
     bool build = false;
-    bool large = false;  // counted against kMaxLargeInflight
     std::vector<Part> parts;
     int64_t table = 0;
     size_t reserve = 0;  // transient device bytes counted while in flight
@@ -198,7 +190,6 @@ struct intp_server {
     uint64_t lru_clock = 0;
     uint64_t resident_bytes = 0;
     uint64_t inflight_bytes = 0;
-    int large_inflight = 0;
 
     // statistics since the last reset
     std::vector<double> lat_build, lat_eval;
@@ -297,7 +288,6 @@ void intp_server::finish_slot(Slot& s, cudaError_t e) {
     const Clock::time_point now = Clock::now();
     Unit& u = s.unit;
     inflight_bytes -= u.reserve;
-    if (u.large) --large_inflight;
     if (u.build) {
         Request* r = u.parts[0].r;
         Table& tb = tables[u.table];
@@ -341,8 +331,6 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         // a reserved slot takes small requests only
         if (s.small_only && (r->build ? build_values(r->desc) > kSmallValues : r->npts - r->admitted > kSmallPoints))
             continue;
-        const bool large = r->build ? build_values(r->desc) > kSmallValues : r->npts - r->admitted > kSmallPoints;
-        if (large && large_inflight >= kMaxLargeInflight) continue;
         if (r->build) {
             const size_t need = table_build_scratch_bytes(&r->desc) +
                                 [&] {
@@ -360,7 +348,6 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
             pending.erase(it);
             Unit u;
             u.build = true;
-            u.large = large;
             u.parts.push_back(Part{r, 0, 0});
             r->t_admit = Clock::now();
             r->admitted_once = true;
@@ -381,7 +368,6 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
                 return true;
             }
             inflight_bytes += need;
-            if (u.large) ++large_inflight;
             cudaEventRecord(s.done, s.stream);
             s.unit = std::move(u);
             s.busy = true;
@@ -404,9 +390,7 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         const int K = r->derivs.empty() ? 1 : r->nderiv;
         const size_t ob = r->out_dtype == INTP_F32 ? 4 : 8;
         const size_t per_pt = static_cast<size_t>(tb.dim) * 8 + static_cast<size_t>(K) * ob + kEvalScratchPerPoint;
-        // a reserved slot, or the large-unit cap reached: the unit stays small
-        const bool small_unit = s.small_only || large_inflight >= kMaxLargeInflight;
-        const int64_t cap = std::min(max_batch_points, small_unit ? kSmallPoints : kPiecePoints);
+        const int64_t cap = std::min(max_batch_points, s.small_only ? kSmallPoints : kPiecePoints);
         u.parts.push_back(Part{r, r->admitted, std::min(r->npts - r->admitted, cap)});
         u.npts = u.parts[0].n;
         if (r->admitted + u.npts == r->npts) {
@@ -503,8 +487,6 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         }
         tb.last_use = ++lru_clock;
         inflight_bytes += u.reserve;
-        u.large = u.npts > kSmallPoints;
-        if (u.large) ++large_inflight;
         cudaEventRecord(s.done, st);
         s.unit = std::move(u);
         s.busy = true;

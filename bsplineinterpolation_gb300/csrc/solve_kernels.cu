@@ -1,6 +1,6 @@
 // Control-point solve: per-axis band / cyclic-band substitution over every
 // mesh line (InterpolationTemplate.hpp:448-580, BandLU.hpp:120-143 and
-// :215-259), plus the double-float residual of mixed-precision refinement.
+// :215-259), in FP64, FP32 and double-word arithmetic (the mixed form).
 //
 // A mesh of shape N_0 x ... x N_{D-1} is processed one axis at a time. Along
 // axis a the lines are indexed by (outer o, inner t): element k of a line is
@@ -21,7 +21,6 @@
 
 #include "async_copy.cuh"
 #include "launch.hpp"
-#include "refine_df.cuh"
 #include "solve_line.cuh"
 
 namespace intp_gb300 {
@@ -208,19 +207,39 @@ __global__ void __launch_bounds__(256) shift_copy_kernel(const double* __restric
             }
         }
         const double v = src[j];
-        if constexpr (sizeof(To) == 4) {
-            if (dlo) {
-                // integer split (no FP64 instructions): dst + dlo = v to
-                // about 2^-46 relative
-                float h, l;
-                split_double(v, h, l);
-                dst[o] = h;
-                dst2[o] = h;
-                dlo[o] = l;
-                continue;
+        if constexpr (std::is_same<To, DW>::value) {
+            // the double-word right-hand side of the mixed solve: the
+            // integer split below, hi + lo = v to about 2^-46 relative
+            float h, l;
+            split_double(v, h, l);
+            dst[o] = DW(h, l);
+        } else {
+            if constexpr (sizeof(To) == 4) {
+                if (dlo) {
+                    // integer split (no FP64 instructions): dst + dlo = v to
+                    // about 2^-46 relative
+                    float h, l;
+                    split_double(v, h, l);
+                    dst[o] = h;
+                    dst2[o] = h;
+                    dlo[o] = l;
+                    continue;
+                }
             }
+            dst[o] = static_cast<To>(v);
         }
-        dst[o] = static_cast<To>(v);
+    }
+}
+
+// The mixed solve's double-word solution as the table's two FP32 arrays:
+// control point = hi + lo.
+__global__ void __launch_bounds__(256) dw_unpack_kernel(const DW* __restrict__ w, float* __restrict__ hi,
+                                                        float* __restrict__ lo, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const DW v = w[i];
+        hi[i] = v.hi;
+        lo[i] = v.lo;
     }
 }
 
@@ -242,166 +261,6 @@ struct AxisPos {
     }
     __device__ __forceinline__ int64_t operator()(int64_t e) const { return (e / S64) % n64; }
 };
-
-// One residual pass of the mixed form's refinement along an axis of n points
-// and stride S, over all N values (channel blocks included), with Dot2
-// accumulation over the axis' band stencil (dot2_band_row, the operations of
-// the batched residual): out = A_axis in as a double-float, or on the last
-// pass (FINAL) r = rhs - A_axis in rounded to FP32 -- the correction solve's
-// right-hand side. HAS_LO: the input is double-float (else plain FP32). One
-// thread per output element, kResidualIlp elements per loop trip (independent loads
-// in flight); the columns are computed, not loaded, and on a strided axis
-// the warp's coefficient loads are broadcasts.
-constexpr int kResidualIlp = 4;
-
-// One element pair of a residual pass: elements e0, e1 (e1 >= N: a dummy
-// lane with zero coefficients and operands, never stored) as the two lanes
-// of the packed accumulator. Each lane applies dot2_band_row_t's taps in its
-// order; a tap that is zero in one lane only adds an exact zero there (the
-// running sum and error term keep their values), so each lane's result is
-// that of the scalar pass.
-template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
-__device__ __forceinline__ void residual_pair(const float* __restrict__ in_hi, const float* __restrict__ in_lo,
-                                              float* __restrict__ out_hi, float* __restrict__ out_lo,
-                                              const float* __restrict__ rhs_hi, const float* __restrict__ rhs_lo,
-                                              float* __restrict__ r, const AxisPos& pos, I S, I N, int n,
-                                              const float2* __restrict__ val, I e0, I e1) {
-    constexpr int W = 2 * BAND + 1;
-    const bool v1 = e1 < N;
-    const I i0 = pos(e0), i1 = v1 ? pos(e1) : I(0);
-    const I b0 = e0 - i0 * S, b1 = v1 ? e1 - i1 * S : I(0);
-    Dot2x2 acc{make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
-    if (FINAL) {
-        acc.s = make_float2(rhs_hi[e0], v1 ? rhs_hi[e1] : 0.0f);
-        acc.c = make_float2(rhs_lo[e0], v1 ? rhs_lo[e1] : 0.0f);
-    }
-    const float2* __restrict__ row0 = val + static_cast<int64_t>(i0) * W;
-    const float2* __restrict__ row1 = val + static_cast<int64_t>(i1) * W;
-#pragma unroll
-    for (int d = 0; d < W; ++d) {
-        float2 a0 = __ldg(row0 + d);
-        float2 a1 = v1 ? __ldg(row1 + d) : make_float2(0.0f, 0.0f);
-        const bool z0 = a0.x == 0.0f, z1 = a1.x == 0.0f;
-        if (z0 && z1) continue;
-        if (FINAL) {
-            a0.x = -a0.x;
-            a0.y = -a0.y;
-            a1.x = -a1.x;
-            a1.y = -a1.y;
-        }
-        float2 xh = make_float2(0.0f, 0.0f), xl = make_float2(0.0f, 0.0f);
-        if (!z0) {
-            int c = static_cast<int>(i0) - BAND + d;
-            if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
-            const I j = b0 + static_cast<I>(c) * S;
-            xh.x = __ldg(in_hi + j);
-            if (HAS_LO) xl.x = __ldg(in_lo + j);
-        }
-        if (!z1) {
-            int c = static_cast<int>(i1) - BAND + d;
-            if (PERIODIC) c = c < 0 ? c + n : (c >= n ? c - n : c);
-            const I j = b1 + static_cast<I>(c) * S;
-            xh.y = __ldg(in_hi + j);
-            if (HAS_LO) xl.y = __ldg(in_lo + j);
-        }
-        dot2_add2<HAS_LO>(acc, make_float2(a0.x, a1.x), make_float2(a0.y, a1.y), xh, xl);
-    }
-    if (FINAL) {
-        const float2 v = __fadd2_rn(acc.s, acc.c);
-        r[e0] = v.x;
-        if (v1) r[e1] = v.y;
-    } else {
-        float2 h, l;
-        df_two_sum2(acc.s, acc.c, h, l);
-        out_hi[e0] = h.x;
-        out_lo[e0] = l.x;
-        if (v1) {
-            out_hi[e1] = h.y;
-            out_lo[e1] = l.y;
-        }
-    }
-}
-
-template <class I, int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
-__global__ void __launch_bounds__(256) residual_pass_kernel(const float* __restrict__ in_hi,
-                                                            const float* __restrict__ in_lo, float* __restrict__ out_hi,
-                                                            float* __restrict__ out_lo,
-                                                            const float* __restrict__ rhs_hi,
-                                                            const float* __restrict__ rhs_lo, float* __restrict__ r,
-                                                            AxisPos pos, I S, I N, int n,
-                                                            const float2* __restrict__ val) {
-    const I stride = static_cast<I>(gridDim.x) * blockDim.x;
-    for (I e0 = blockIdx.x * static_cast<I>(blockDim.x) + threadIdx.x; e0 < N; e0 += kResidualIlp * stride) {
-#pragma unroll
-        for (int u = 0; u < kResidualIlp; u += 2) {
-            const I e = e0 + u * stride;
-            if (e < N)
-                residual_pair<I, BAND, PERIODIC, HAS_LO, FINAL>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, S,
-                                                                N, n, val, e, e + stride);
-        }
-    }
-}
-
-template <int BAND, bool PERIODIC, bool HAS_LO, bool FINAL>
-void launch_residual_t(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
-                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, const float2* val,
-                       cudaStream_t s) {
-    AxisPos pos{};
-    pos.S64 = S;
-    pos.n64 = n;
-    const int grid = grid_for((N + kResidualIlp - 1) / kResidualIlp, 256, 152 * 16);
-    if (N <= kIndex32Max) {
-        pos.byS = FastDiv::make(static_cast<uint32_t>(S));
-        pos.byN = FastDiv::make(static_cast<uint32_t>(n));
-        residual_pass_kernel<uint32_t, BAND, PERIODIC, HAS_LO, FINAL><<<grid, 256, 0, s>>>(
-            in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, static_cast<uint32_t>(S), static_cast<uint32_t>(N),
-            static_cast<int>(n), val);
-    } else {
-        residual_pass_kernel<int64_t, BAND, PERIODIC, HAS_LO, FINAL><<<grid, 256, 0, s>>>(
-            in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, pos, S, N, static_cast<int>(n), val);
-    }
-}
-
-template <int BAND, bool PERIODIC>
-void launch_residual_bp(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
-                        const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, const float2* val,
-                        cudaStream_t s) {
-    const bool lo = in_lo != nullptr, fin = rhs_hi != nullptr;
-    if (lo && fin)
-        launch_residual_t<BAND, PERIODIC, true, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
-    else if (lo)
-        launch_residual_t<BAND, PERIODIC, true, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
-                                                       s);
-    else if (fin)
-        launch_residual_t<BAND, PERIODIC, false, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
-                                                       s);
-    else
-        launch_residual_t<BAND, PERIODIC, false, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val,
-                                                        s);
-}
-
-template <int BAND>
-void launch_residual_b(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo, const float* rhs_hi,
-                       const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N, bool periodic,
-                       const float2* val, cudaStream_t s) {
-    if (periodic)
-        launch_residual_bp<BAND, true>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
-    else
-        launch_residual_bp<BAND, false>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, val, s);
-}
-
-// (c, lo) += corr, element-wise in double-float (lo taken as 0 when has_lo
-// is 0: the first refinement step).
-__global__ void __launch_bounds__(256) correct_kernel(float* __restrict__ c, float* __restrict__ lo,
-                                                      const float* __restrict__ corr, int64_t n, int has_lo) {
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        float h = c[i], l = has_lo ? lo[i] : 0.0f;
-        df_correct(h, l, corr[i], has_lo != 0);
-        c[i] = h;
-        lo[i] = l;
-    }
-}
 
 }  // namespace
 
@@ -432,6 +291,13 @@ cudaError_t launch_line_solve_f32(float* x, int64_t n, int64_t S, int64_t nlines
     return launch_solve_r<float>(x, n, S, nlines, p, q, cyclic, f, s);
 }
 
+cudaError_t launch_line_solve_dw(DW* x, int64_t n, int64_t S, int64_t nlines, int p, int q, bool cyclic,
+                                 const DW* lower, const DW* upper, const DW* dinv, const DW* bottom, const DW* right,
+                                 cudaStream_t s, int64_t clo, int64_t chi, int64_t zside) {
+    FactorView<DW> f{n, lower, upper, dinv, bottom, right, clo, chi, zside};
+    return launch_solve_r<DW>(x, n, S, nlines, p, q, cyclic, f, s);
+}
+
 cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const ShiftDesc& sd,
                                       cudaStream_t s) {
     const int64_t N = sd.total * sd.channels;
@@ -441,6 +307,24 @@ cudaError_t launch_shift_copy_f64_f64(const double* src, double* dst, const Shif
         shift_copy_kernel<double, uint32_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
     else
         shift_copy_kernel<double, int64_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_copy_f64_dw(const double* src, DW* dst, const ShiftDesc& sd, cudaStream_t s) {
+    const int64_t N = sd.total * sd.channels;
+    const int grid = grid_for(N, 256, 152 * 16);
+    const int id = shift_identity(sd) ? 1 : 0;
+    if (N <= kIndex32Max)
+        shift_copy_kernel<DW, uint32_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
+    else
+        shift_copy_kernel<DW, int64_t><<<grid, 256, 0, s>>>(src, dst, nullptr, nullptr, sd, id);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dw_unpack(const DW* w, float* hi, float* lo, int64_t n, cudaStream_t s) {
+    dw_unpack_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(w, hi, lo, n);
     note_launch();
     return cudaGetLastError();
 }
@@ -458,30 +342,5 @@ cudaError_t launch_shift_copy_f64_f32(const double* src, float* dst, float* dst_
     return cudaGetLastError();
 }
 
-cudaError_t launch_residual_pass(const float* in_hi, const float* in_lo, float* out_hi, float* out_lo,
-                                 const float* rhs_hi, const float* rhs_lo, float* r, int64_t n, int64_t S, int64_t N,
-                                 int band, bool periodic, const float2* val, cudaStream_t s) {
-#define INTP_RESIDUAL_CASE(B) \
-    case B: launch_residual_b<B>(in_hi, in_lo, out_hi, out_lo, rhs_hi, rhs_lo, r, n, S, N, periodic, val, s); break;
-    switch (band) {
-        INTP_RESIDUAL_CASE(0)
-        INTP_RESIDUAL_CASE(1)
-        INTP_RESIDUAL_CASE(2)
-        INTP_RESIDUAL_CASE(3)
-        INTP_RESIDUAL_CASE(4)
-        INTP_RESIDUAL_CASE(5)
-        INTP_RESIDUAL_CASE(6)
-        default: return cudaErrorInvalidValue;
-    }
-#undef INTP_RESIDUAL_CASE
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_correct(float* c, float* lo, const float* corr, int64_t n, bool has_lo, cudaStream_t s) {
-    correct_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(c, lo, corr, n, has_lo ? 1 : 0);
-    note_launch();
-    return cudaGetLastError();
-}
 
 }  // namespace intp_gb300

@@ -16,6 +16,8 @@
 #include <climits>
 #include <type_traits>
 
+#include "dw.cuh"
+
 namespace intp_gb300 {
 
 template <class R>
@@ -381,7 +383,9 @@ static __device__ int g_warm_rows_cap = -1;
 
 template <class R>
 __device__ __forceinline__ bool bits_equal(R a, R b) {
-    if constexpr (sizeof(R) == 4)
+    if constexpr (std::is_same<R, DW>::value)
+        return __float_as_uint(a.hi) == __float_as_uint(b.hi) && __float_as_uint(a.lo) == __float_as_uint(b.lo);
+    else if constexpr (sizeof(R) == 4)
         return __float_as_uint(a) == __float_as_uint(b);
     else
         return __double_as_longlong(a) == __double_as_longlong(b);

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "dw.cuh"
 #include "spline_model.hpp"
 
 namespace intp_gb300 {
@@ -32,16 +33,12 @@ struct Arena {
     }
 };
 
-// Device pointers of one axis's LU factor (FP64 and FP32 copies) and of its
-// collocation rows as a band stencil (double-float residuals of the mixed
-// form): sval[i * (2 * band + 1) + d] = A(i, i - band + d) as a (hi, lo)
-// float pair, the column taken cyclically on a periodic axis and the value
-// 0 where a non-periodic column falls outside the axis.
+// Device pointers of one axis's LU factor: FP64 (the FP64 form), FP32 (the
+// mixed form's plain FP32 solve) and double-word (its default solve) copies.
 struct AxisFactorDev {
     const double *lower, *upper, *dinv, *bottom, *right;
     const float *lowerf, *upperf, *dinvf, *bottomf, *rightf;
-    const float2* sval;
-    int band;
+    const DW *lowerw, *upperw, *dinvw, *bottomw, *rightw;
     int64_t clo, chi;      // FP64 rows identical to row clo (LineFactor::const_lo/const_hi)
     int64_t clo32, chi32;  // the same for the FP32 rows (LineFactor::const_lo32/const_hi32)
     int64_t zside, zside32;  // cyclic side-band sums: zero entries from here (LineFactor::zside/zside32)
@@ -51,7 +48,8 @@ struct AxisFactorDev {
 struct PackedTable {
     struct Axis {
         size_t knots, keys, rinv, rinvf, kdf, khi, klo;
-        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf, sval;
+        size_t lower, upper, dinv, bottom, right, lowerf, upperf, dinvf, bottomf, rightf;
+        size_t lowerw, upperw, dinvw, bottomw, rightw;
     } ax[kMaxDim];
 };
 
@@ -75,9 +73,5 @@ bool build_deriv_plan(int dim, int order, const int32_t* derivs, int32_t nderiv,
 // Sets the message intp_last_error() returns on the calling thread.
 void set_last_error(const std::string& msg);
 
-// Refinement steps of a mixed-precision solve of this table (1..4): enough
-// to bring the double-float control points to about 1e-12 relative error,
-// from the per-axis condition estimates.
-int auto_refine_steps(const TableModel& m);
 
 }  // namespace intp_gb300

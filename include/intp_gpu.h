@@ -40,7 +40,7 @@ typedef enum intp_status {
 
 typedef enum intp_precision {
     INTP_PRECISION_FP64 = 0,  /* FP64 end to end (parity form) */
-    INTP_PRECISION_MIXED = 1  /* FP32 solve + double-float refinement, FP32 basis/contraction */
+    INTP_PRECISION_MIXED = 1  /* double-word (FP32-pair) solve, FP32 basis/contraction */
 } intp_precision;
 
 typedef enum intp_dtype { INTP_F64 = 0, INTP_F32 = 1 } intp_dtype;
@@ -53,7 +53,9 @@ typedef struct intp_table_desc {
     int32_t dim;           /* 1..INTP_GPU_MAX_DIM */
     int32_t order;         /* 0..INTP_GPU_MAX_ORDER */
     int32_t precision;     /* intp_precision */
-    int32_t refine_steps;  /* mixed only: -1 = automatic (at least 1), else 0..4 */
+    int32_t refine_steps;  /* mixed only: 0 = plain FP32 solve (FP32 control points); any other
+                              value (default -1) = double-word solve (control points as FP32 pairs,
+                              about 48 bits) */
     int32_t periodic[INTP_GPU_MAX_DIM];
     int64_t size[INTP_GPU_MAX_DIM];     /* samples per axis (mesh dim sizes) */
     double range_lo[INTP_GPU_MAX_DIM];  /* uniform axis: x_min */
@@ -93,10 +95,9 @@ intp_status intp_table_interpolate(intp_table* table, const double* values,
                                    int32_t values_on_device, void* stream);
 
 /* Loads / reads control points (row-major, prod(size) doubles, host memory).
- * A mixed-precision table that refines its solve keeps every control point
- * as a double-float (an FP32 value plus its FP32 remainder, about 48
- * significant bits); a mixed table built without refinement keeps the FP32
- * value alone.
+ * A mixed-precision table keeps every control point as a double-word (an
+ * FP32 value plus its FP32 remainder, about 48 significant bits); one built
+ * with refine_steps = 0 keeps the FP32 value alone.
  * Replaces: BSpline::load_ctrlPts (src/include/BSpline.hpp:230-242) and
  * BSpline::control_points (BSpline.hpp:575-577, plain layout). */
 intp_status intp_table_set_control_points(intp_table* table, const double* ctrl_host);

@@ -7,8 +7,8 @@ random centres), 1e6 of them; outputs value and d/dx.
 
 - FP64 form: within 1e-12 of the oracle (relative to each output's max
   magnitude), spans bit-exact.
-- Mixed form (FP32 solve + double-float refinement, binned FP32
-  evaluation): within 1e-6 of the oracle, and the binned path's spans
+- Mixed form (double-word solve, binned FP32 evaluation): within 1e-6 of
+  the oracle, and the binned path's spans
   bit-exact against the oracle's get_knot_iter (BSpline.hpp:125-157).
 """
 import os

@@ -127,7 +127,8 @@ def test_reference_outputs_mixed(meta):
                          ids=lambda m: m["name"])
 def test_mixed_workload_shapes_within_1e6(meta):
     """The workload-shaped tables (smooth data, uniform grids) meet 1e-6 on
-    values with and without refinement of the FP32 solve."""
+    values with the plain FP32 solve (refine_steps = 0) and with the
+    double-word solve (the default)."""
     name = meta["name"]
     pts_np = Z[name + "/points"]
     inside = _in_domain(meta, pts_np)

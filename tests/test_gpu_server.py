@@ -141,14 +141,15 @@ def test_served_table_matches_oracle_and_direct_table():
 
 
 def test_budget_and_lru_eviction():
-    """2D 1024^2 mixed tables hold 8 MiB each (FP32 control points and
-    their FP32 remainders); a build needs ~44 MiB in flight (the table and
-    36 bytes of scratch per value). Under an 80 MiB budget five tables fit
-    with a build in flight and the sixth build evicts the least recently
-    used idle table; an evaluation of an evicted table reports ERR_STATE and
-    a request that could never fit reports ERR_BUDGET."""
+    """2D 1024^2 mixed tables hold 8 MiB each (their control points as two
+    FP32 arrays); a build needs ~25 MiB in flight (the table and 16 bytes of
+    scratch per value: the staged values and the double-word solve's working
+    array). Under a 60 MiB budget five tables fit with a build in flight
+    and the sixth build evicts the least recently used idle table; an
+    evaluation of an evicted table reports ERR_STATE and a request that
+    could never fit reports ERR_BUDGET."""
     rng = np.random.default_rng(5)
-    srv = bi.Server(memory_budget=80 << 20, slots=1)
+    srv = bi.Server(memory_budget=60 << 20, slots=1)
     try:
         vals = [_pinned(_smooth(rng, [1024, 1024])) for _ in range(7)]
         tids = []
@@ -171,7 +172,7 @@ def test_budget_and_lru_eviction():
         big = _pinned(_smooth(rng, [2048, 2048]))
         _, rid = srv.submit_build(3, [False, False], big, (0.0, 1.0), (0.0, 1.0))
         assert srv.wait(rid, WAIT_S) == ERR_BUDGET
-        assert srv.stats()["resident_bytes"] <= 80 << 20
+        assert srv.stats()["resident_bytes"] <= 60 << 20
     finally:
         srv.close()
 

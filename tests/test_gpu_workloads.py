@@ -6,12 +6,12 @@ of the reference, pinned bit-exact to the reference's build).
   matches the reference to 1e-12 (relative to max |f|), spans bit-exact.
 - Periodic high order: 2D, order 7, periodic in both axes, 512 x 512 of a
   sum of 16 random sinusoids (integer wavenumbers 1..20). Value, first and
-  second derivatives: the FP64 form to 1e-12; the mixed form (FP32 cyclic
-  solve with a double-float residual refinement, FP32 weights, the precise
-  contraction for second derivatives) to 1e-6 on every output.
+  second derivatives: the FP64 form to 1e-12; the mixed form (cyclic solve
+  in double-word arithmetic, FP32 weights, the precise contraction for
+  second derivatives) to 1e-6 on every output.
 - 3D cubic (the headline workload at 64^3): FP64 to 1e-12; the mixed form's
-  value and d/dx within 1e-6 of max |.|, its control points (double-floats
-  after refinement) within 1e-11 of the FP64 form's.
+  value and d/dx within 1e-6 of max |.|, its control points (double-words
+  from the double-word solve) within 1e-11 of the FP64 form's.
 """
 import numpy as np
 import pytest
@@ -77,9 +77,9 @@ def test_periodic_order7_fp64_matches_reference(periodic_o7):
 
 
 def test_periodic_order7_mixed_within_stated_error(periodic_o7):
-    """Mixed form on the periodic order-7 table: the automatic refinement
-    policy refines the FP32 cyclic solve with double-float residuals until the
-    control points are near 1e-12. A request with second derivatives takes
+    """Mixed form on the periodic order-7 table: the cyclic solve runs in
+    double-word arithmetic (control points near 1e-13 of the FP64 form's). A
+    request with second derivatives takes
     the precise contraction (operands relative to each query's central
     control point in double-float, recursion-based derivative weights,
     compensated sums). Every output, values through second derivatives,
