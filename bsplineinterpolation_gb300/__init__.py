@@ -587,10 +587,10 @@ class TableBatch:
             _lib.check(lib.intp_batch_build(self._h, v.ctypes.data, 0, _stream_ptr(stream)))
             _lib.check(lib.intp_stream_synchronize(_stream_ptr(stream)))
 
-    def set_schedule(self, persistent=False, stage_kb=16, strided_rows=32):
+    def set_schedule(self, persistent=False, contig_rows=32, strided_rows=32):
         """Schedule of the line solves (intp_batch_set_schedule); results do
         not depend on it."""
-        sc = _lib.BatchSchedule(int(bool(persistent)), int(stage_kb), int(strided_rows), 0, 0.0)
+        sc = _lib.BatchSchedule(int(bool(persistent)), int(contig_rows), int(strided_rows), 0, 0.0)
         _lib.check(_lib.load().intp_batch_set_schedule(self._h, C.byref(sc)))
 
     def schedule(self):

@@ -68,11 +68,11 @@ class ServerStats(C.Structure):
 
 class BatchSchedule(C.Structure):
     """intp_batch_schedule."""
-    _fields_ = [("persistent", C.c_int32), ("stage_kb", C.c_int32), ("strided_rows", C.c_int32),
+    _fields_ = [("persistent", C.c_int32), ("contig_rows", C.c_int32), ("strided_rows", C.c_int32),
                 ("pad_", C.c_int32), ("build_ms", C.c_double)]
 
     def as_dict(self):
-        return {"persistent": self.persistent, "stage_kb": self.stage_kb, "strided_rows": self.strided_rows,
+        return {"persistent": self.persistent, "contig_rows": self.contig_rows, "strided_rows": self.strided_rows,
                 "build_ms": self.build_ms}
 
 

@@ -36,11 +36,11 @@ using namespace intp_gb300;
 
 namespace {
 
-constexpr int kBatchMaxDim = 3;
 constexpr int32_t kChunkElems = 8192;
 constexpr int64_t kEvalRun = 2048;           // query points per evaluation CTA
-constexpr size_t kStageMaxBytes = 200 * 1024;  // longest contiguous line staged
-constexpr int kMaxLaunches = 64;               // work counters of one build (persistent passes)
+// work counters of one build's persistent launches: a pass per axis, a
+// launch per band class, and a mixed batch's FP32 and double-word solves
+constexpr int kMaxLaunches = 2 * kBatchMaxDim * kBatchClasses;
 
 intp_status bfail(intp_status s, const std::string& msg);
 
@@ -66,23 +66,19 @@ struct intp_batch {
     const AxisFactorDev* d_fac = nullptr;  // [ntables * kBatchMaxDim]
     const int64_t* d_off = nullptr;
     const int32_t* d_refine = nullptr;
-    const int2* d_bands = nullptr;  // (band width, cyclic) per (table, axis)
     const ChunkItem* d_chunks = nullptr;
     int64_t nchunks = 0;
-    // One axis pass: its work items in two launches, those whose staged
-    // lines fit the schedule's per-warp budget, then the rest (longer staged
-    // lines, launched with their own shared-memory size).
+    // One axis pass: its work items in one list per band class, a launch
+    // each, in the order of `order` (most values first).
     struct Pass {
-        const SolveItem* items = nullptr;
-        int64_t nitems = 0;
-        size_t smem_elems = 0;     // staging elements per warp
-        const SolveItem* long_items = nullptr;
-        int64_t nlong = 0;
-        size_t smem_long = 0;
+        const SolveItem* items[kBatchClasses] = {};
+        int64_t nitems[kBatchClasses] = {};
+        int order[kBatchClasses] = {};
+        int nclasses = 0;
     } pass[kBatchMaxDim];
     int npasses = 0;
     bool has_ctrl = false;
-    intp_batch_schedule sched{0, 16, 32, 0, 0.0};
+    intp_batch_schedule sched{0, 32, 32, 0, 0.0};
     void* work = nullptr;                // the schedule's work lists (device)
     unsigned int* counters = nullptr;    // work counters of the persistent passes (device)
 
@@ -120,168 +116,18 @@ intp_status bcuda(cudaError_t e, const char* what) {
 // kernels
 // ---------------------------------------------------------------------------
 
-template <class R>
-__device__ __forceinline__ FactorView<R> factor_view(const AxisFactorDev& f, int64_t n);
-
-template <>
-__device__ __forceinline__ FactorView<float> factor_view<float>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<float>{n, f.lowerf, f.upperf, f.dinvf, f.bottomf, f.rightf, f.clo32, f.chi32, f.zside32};
-}
-
-template <>
-__device__ __forceinline__ FactorView<double> factor_view<double>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<double>{n, f.lower, f.upper, f.dinv, f.bottom, f.right, f.clo, f.chi, f.zside};
-}
-
-template <>
-__device__ __forceinline__ FactorView<DW> factor_view<DW>(const AxisFactorDev& f, int64_t n) {
-    return FactorView<DW>{n, f.lowerw, f.upperw, f.dinvw, f.bottomw, f.rightw, f.clo, f.chi, f.zside};
-}
-
-// Tables a pass works on (mixed batches): every table, the tables solved in
-// FP32 (refine = 0), or the ones solved in double-word arithmetic (refine > 0).
-constexpr int kSelAll = -1, kSelPlain = -2, kSelDW = -3;
-__device__ __forceinline__ bool selected(int sel, int refine) {
-    return sel == kSelAll || (sel == kSelPlain ? refine == 0 : refine > 0);
-}
-
-// Lines are walked in chunks of this many elements (registers per lane).
-constexpr int kBatchChunk = 16;
-
-template <class R, class Line>
-__device__ __forceinline__ void solve_dispatch(int p, bool cyc, const FactorView<R>& fv, const Line& line) {
-    constexpr int K = kBatchChunk;
-    if (cyc) {
-        switch (p) {
-            case 0: solve_line_chunked<R, 0, 0, true, K, Line>(fv, line); return;
-            case 1: solve_line_chunked<R, 1, 1, true, K, Line>(fv, line); return;
-            case 2: solve_line_chunked<R, 2, 2, true, K, Line>(fv, line); return;
-            case 3: solve_line_chunked<R, 3, 3, true, K, Line>(fv, line); return;
-        }
-        return;
-    }
-    switch (p) {
-        case 0: solve_line_chunked<R, 0, 0, false, K, Line>(fv, line); return;
-        case 1: solve_line_chunked<R, 1, 1, false, K, Line>(fv, line); return;
-        case 2: solve_line_chunked<R, 2, 2, false, K, Line>(fv, line); return;
-        case 3: solve_line_chunked<R, 3, 3, false, K, Line>(fv, line); return;
-        case 4: solve_line_chunked<R, 4, 4, false, K, Line>(fv, line); return;
-        case 5: solve_line_chunked<R, 5, 5, false, K, Line>(fv, line); return;
-        case 6: solve_line_chunked<R, 6, 6, false, K, Line>(fv, line); return;
-    }
-}
-
-// A line of at least this many elements that is a warp's only line is solved
-// by the whole warp (solve_line_warp).
-constexpr int64_t kWarpLineMin = 128;
-
-// Warm-up rows of the warp-segmented substitution: enough for the zero
-// state's error to fall below the last bit in FP32 / FP64.
-template <class R>
-constexpr int warm_rows() {
-    return sizeof(R) == 4 ? 64 : 128;
-}
-
 }  // namespace
 
 namespace intp_gb300 {
-INTP_DEFINE_WARM_CAP_SETTER(set_warm_cap_batch)
+cudaError_t set_warm_cap_batch(int rows) {
+    cudaError_t e = set_warm_cap_batch_f32(rows);
+    if (e == cudaSuccess) e = set_warm_cap_batch_dw(rows);
+    if (e == cudaSuccess) e = set_warm_cap_batch_f64(rows);
+    return e;
+}
 }  // namespace intp_gb300
 
 namespace {
-
-template <class R>
-__device__ __forceinline__ void solve_dispatch_warp(int p, bool cyc, const FactorView<R>& fv, const LineRef<R>& line,
-                                                    int lane) {
-    constexpr int W = warm_rows<R>();
-    if (cyc) {
-        switch (p) {
-            case 0: solve_line_warp<R, 0, 0, true, W, true>(fv, line, lane); return;
-            case 1: solve_line_warp<R, 1, 1, true, W, true>(fv, line, lane); return;
-            case 2: solve_line_warp<R, 2, 2, true, W, true>(fv, line, lane); return;
-            case 3: solve_line_warp<R, 3, 3, true, W, true>(fv, line, lane); return;
-        }
-        return;
-    }
-    switch (p) {
-        case 0: solve_line_warp<R, 0, 0, false, W, true>(fv, line, lane); return;
-        case 1: solve_line_warp<R, 1, 1, false, W, true>(fv, line, lane); return;
-        case 2: solve_line_warp<R, 2, 2, false, W, true>(fv, line, lane); return;
-        case 3: solve_line_warp<R, 3, 3, false, W, true>(fv, line, lane); return;
-        case 4: solve_line_warp<R, 4, 4, false, W, true>(fv, line, lane); return;
-        case 5: solve_line_warp<R, 5, 5, false, W, true>(fv, line, lane); return;
-        case 6: solve_line_warp<R, 6, 6, false, W, true>(fv, line, lane); return;
-    }
-}
-
-// The work of one item (up to 32 lines of one table and axis) for one warp.
-// `bands` holds the band width and cyclic flag of every (table, axis).
-// `sel` picks the tables of a mixed batch: -1 every table, kSelPlain the
-// tables solved in FP32 (refine = 0), kSelDW the ones solved in double-word
-// arithmetic (refine > 0).
-template <class R>
-__device__ __forceinline__ void batch_solve_item(R* __restrict__ data, const SolveItem& it, R* tile,
-                                                 const TableDev* __restrict__ tables,
-                                                 const AxisFactorDev* __restrict__ fac,
-                                                 const int64_t* __restrict__ off,
-                                                 const int32_t* __restrict__ refine, int sel,
-                                                 const int2* __restrict__ bands) {
-    if (!selected(sel, refine[it.table])) return;
-    const int lane = threadIdx.x;
-    const TableDev& t = tables[it.table];
-    const AxisDev& ax = t.ax[it.axis];
-    const int64_t n = ax.n, S = ax.stride;
-    const int2 band = bands[it.table * kBatchMaxDim + it.axis];
-    const FactorView<R> fv = factor_view<R>(fac[it.table * kBatchMaxDim + it.axis], n);
-    R* base = data + off[it.table];
-    if (it.staged) {
-        // S == 1: lines line0 .. line0+rows-1 are one contiguous run of rows*n
-        const int ni = static_cast<int>(n), pitch = ni + 1;
-        R* src = base + it.line0 * n;
-        for (int r = 0; r < it.rows; ++r)
-            for (int k = lane; k < ni; k += 32) tile[r * pitch + k] = src[static_cast<int64_t>(r) * ni + k];
-        __syncwarp();
-        if (it.rows == 1 && n >= kWarpLineMin)
-            solve_dispatch_warp<R>(band.x, band.y != 0, fv, LineRef<R>{tile, 1}, lane);
-        else if (lane < it.rows)
-            solve_dispatch<R>(band.x, band.y != 0, fv, SmemChunks<R>{tile + lane * pitch});
-        __syncwarp();
-        for (int r = 0; r < it.rows; ++r)
-            for (int k = lane; k < ni; k += 32) src[static_cast<int64_t>(r) * ni + k] = tile[r * pitch + k];
-        return;
-    }
-    if (lane < it.rows) {
-        const int64_t l = it.line0 + lane;
-        const int64_t o = l / S, tt = l - o * S;
-        solve_dispatch<R>(band.x, band.y != 0, fv, StridedChunks<R>{base + o * n * S + tt, S});
-    }
-}
-
-// One warp per CTA. PERSIST: a grid of a few warps per SM drains the list
-// through an atomic counter (longest lines first), else one CTA per item.
-template <class R, bool PERSIST>
-__global__ void __launch_bounds__(32) batch_solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
-                                                         int64_t nitems, unsigned int* __restrict__ counter,
-                                                         const TableDev* __restrict__ tables,
-                                                         const AxisFactorDev* __restrict__ fac,
-                                                         const int64_t* __restrict__ off,
-                                                         const int32_t* __restrict__ refine, int sel,
-                                                         const int2* __restrict__ bands) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* tile = reinterpret_cast<R*>(smem_raw);
-    if constexpr (!PERSIST) {
-        batch_solve_item<R>(data, items[blockIdx.x], tile, tables, fac, off, refine, sel, bands);
-    } else {
-        for (;;) {
-            unsigned int idx = 0;
-            if (threadIdx.x == 0) idx = atomicAdd(counter, 1u);
-            idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
-            if (static_cast<int64_t>(idx) >= nitems) return;
-            batch_solve_item<R>(data, items[idx], tile, tables, fac, off, refine, sel, bands);
-            __syncwarp();
-        }
-    }
-}
 
 // Element-wise passes over chunk items:
 //  op 0: dst[shift(i)] = (R) src[i]; in a mixed batch, for the tables solved
@@ -346,32 +192,14 @@ __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const do
 
 size_t up256(size_t v) { return (v + 255) & ~size_t(255); }
 
-int sm_count_batch() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
-    }
-    return n;
-}
-
-// Work lists of the axis passes under a schedule (lines per strided item,
-// shared memory per warp for staged contiguous lines) and the value chunks
-// of the element-wise kernels. Per pass: the items that fit the staging
-// budget, then (in their own list) the staged lines longer than it.
-struct PassLists {
-    std::vector<SolveItem> items, long_items;
-    size_t smem = 0, smem_long = 0;
-};
-
-void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<PassLists>& passes,
-                std::vector<ChunkItem>& chunks) {
-    // staging bytes per element: 8 for FP64 and for the double-word solve of
-    // mixed batches (an FP32 pass then stages at most half its budget)
-    const size_t esz = b.mixed() ? sizeof(DW) : sizeof(double);
-    const size_t stage = static_cast<size_t>(sc.stage_kb) * 1024;
-    passes.assign(kBatchMaxDim, {});
+// Work lists of the axis passes under a schedule (lines per item on the
+// contiguous and on the strided axes), one list per (pass, band class) at
+// index pass * kBatchClasses + class, with the values each list covers, and
+// the value chunks of the element-wise kernels.
+void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<std::vector<SolveItem>>& passes,
+                std::vector<int64_t>& values, std::vector<ChunkItem>& chunks) {
+    passes.assign(static_cast<size_t>(kBatchMaxDim) * kBatchClasses, {});
+    values.assign(passes.size(), 0);
     chunks.clear();
     for (int64_t i = 0; i < b.ntables; ++i) {
         const TableModel& m = b.models[i];
@@ -380,34 +208,18 @@ void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<
             const int64_t n = m.axis[a].n;
             const int64_t nlines = m.total / n;
             const bool contig = (a == m.dim - 1);
-            int64_t rows_max = sc.strided_rows;
-            bool staged = false;
-            size_t line_bytes = 0;
-            if (contig) {
-                rows_max = 32;
-                line_bytes = static_cast<size_t>(n + 1) * esz;
-                if (line_bytes <= kStageMaxBytes) {
-                    staged = true;
-                    rows_max = std::max<int64_t>(1, std::min<int64_t>(32, static_cast<int64_t>(stage / line_bytes)));
-                }
-            }
-            const bool is_long = staged && line_bytes > stage;
-            PassLists& pl = passes[j];
+            const int64_t rows_max = contig ? sc.contig_rows : sc.strided_rows;
+            const LineFactor& f = m.axis[a].factor;
+            const size_t list = static_cast<size_t>(j) * kBatchClasses + batch_band_class(f.p, f.cyclic);
+            values[list] += m.total;
             for (int64_t l0 = 0; l0 < nlines; l0 += rows_max) {
                 SolveItem it{};
                 it.table = static_cast<int32_t>(i);
                 it.axis = static_cast<int16_t>(a);
-                it.staged = staged ? 1 : 0;
+                it.contig = contig ? 1 : 0;
                 it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
                 it.line0 = l0;
-                const size_t need = staged ? static_cast<size_t>(it.rows) * static_cast<size_t>(n + 1) : 0;
-                if (is_long) {
-                    pl.long_items.push_back(it);
-                    pl.smem_long = std::max(pl.smem_long, need);
-                } else {
-                    pl.items.push_back(it);
-                    pl.smem = std::max(pl.smem, need);
-                }
+                passes[list].push_back(it);
             }
         }
         for (int64_t s = 0; s < m.total; s += kChunkElems) {
@@ -422,25 +234,20 @@ void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<
     auto longest_first = [&](const SolveItem& x, const SolveItem& y) {
         return b.models[x.table].axis[x.axis].n > b.models[y.table].axis[y.axis].n;
     };
-    for (auto& p : passes) {
-        std::stable_sort(p.items.begin(), p.items.end(), longest_first);
-        std::stable_sort(p.long_items.begin(), p.long_items.end(), longest_first);
-    }
+    for (auto& p : passes) std::stable_sort(p.begin(), p.end(), longest_first);
 }
 
 // Builds and uploads the work lists of schedule sc (replacing the batch's).
 intp_status apply_schedule(intp_batch* b, const intp_batch_schedule& sc) {
-    if (sc.stage_kb < 1 || sc.stage_kb > 200 || sc.strided_rows < 1 || sc.strided_rows > 32)
-        return bfail(INTP_ERR_INVALID_ARGUMENT, "schedule: stage_kb in [1, 200], strided_rows in [1, 32]");
-    std::vector<PassLists> passes;
+    if (sc.contig_rows < 1 || sc.contig_rows > 32 || sc.strided_rows < 1 || sc.strided_rows > 32)
+        return bfail(INTP_ERR_INVALID_ARGUMENT, "schedule: contig_rows and strided_rows in [1, 32]");
+    std::vector<std::vector<SolveItem>> passes;
+    std::vector<int64_t> values;
     std::vector<ChunkItem> chunks;
-    build_work(*b, sc, passes, chunks);
+    build_work(*b, sc, passes, values, chunks);
     Arena ar;
-    size_t o_items[kBatchMaxDim], o_long[kBatchMaxDim];
-    for (int j = 0; j < kBatchMaxDim; ++j) {
-        o_items[j] = ar.put(passes[j].items);
-        o_long[j] = ar.put(passes[j].long_items);
-    }
+    std::vector<size_t> o_items(passes.size());
+    for (size_t j = 0; j < passes.size(); ++j) o_items[j] = ar.put(passes[j]);
     if (b->work) cudaFree(b->work);
     b->work = nullptr;
     BATCH_CUDA(cudaMalloc(&b->work, std::max<size_t>(ar.host.size(), 16)), "cudaMalloc(batch work lists)");
@@ -449,13 +256,18 @@ intp_status apply_schedule(intp_batch* b, const intp_batch_schedule& sc) {
     b->npasses = 0;
     for (int j = 0; j < kBatchMaxDim; ++j) {
         intp_batch::Pass& p = b->pass[j];
-        p.items = reinterpret_cast<const SolveItem*>(base + o_items[j]);
-        p.nitems = static_cast<int64_t>(passes[j].items.size());
-        p.smem_elems = passes[j].smem;
-        p.long_items = reinterpret_cast<const SolveItem*>(base + o_long[j]);
-        p.nlong = static_cast<int64_t>(passes[j].long_items.size());
-        p.smem_long = passes[j].smem_long;
-        if (p.nitems + p.nlong > 0) b->npasses = j + 1;
+        p.nclasses = 0;
+        for (int c = 0; c < kBatchClasses; ++c) {
+            const size_t list = static_cast<size_t>(j) * kBatchClasses + c;
+            p.items[c] = reinterpret_cast<const SolveItem*>(base + o_items[list]);
+            p.nitems[c] = static_cast<int64_t>(passes[list].size());
+            if (p.nitems[c] > 0) p.order[p.nclasses++] = c;
+        }
+        // the classes with the most values first
+        std::stable_sort(p.order, p.order + p.nclasses, [&](int x, int y) {
+            return values[static_cast<size_t>(j) * kBatchClasses + x] > values[static_cast<size_t>(j) * kBatchClasses + y];
+        });
+        if (p.nclasses > 0) b->npasses = j + 1;
     }
     b->sched = sc;
     b->sched.build_ms = 0.0;
@@ -472,46 +284,27 @@ int batch_sm_count() {
     return n;
 }
 
-template <class R, bool PERSIST>
-cudaError_t launch_items(intp_batch* b, R* data, const SolveItem* items, int64_t nitems, size_t smem_elems,
-                         unsigned int* counter, int sel, const int2* bands, cudaStream_t s) {
-    if (nitems == 0) return cudaSuccess;
-    const size_t smem = smem_elems * sizeof(R);
-    auto k = batch_solve_kernel<R, PERSIST>;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-    }
-    int64_t grid = nitems;
-    if (PERSIST) {
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32, smem) != cudaSuccess || per_sm < 1)
-            per_sm = 1;
-        grid = std::min<int64_t>(nitems, static_cast<int64_t>(per_sm) * batch_sm_count());
-    }
-    k<<<static_cast<unsigned>(grid), 32, smem, s>>>(data, items, nitems, counter, b->d_tables, b->d_fac, b->d_off,
-                                                    b->d_refine, sel, bands);
-    note_launch();
-    return cudaGetLastError();
-}
-
-// One solve of every table: the axis passes in order, each as its regular
-// and its long-line launch. `launch` numbers the persistent launches of the
+// One solve of every table: the axis passes in order, a launch per band
+// class present in the pass. `launch` numbers the persistent launches of the
 // build (their work counters were cleared when the build started).
 template <class R>
-cudaError_t run_passes(intp_batch* b, R* data, int sel, const int2* bands, int& launch, cudaStream_t s) {
+cudaError_t run_passes(intp_batch* b, R* data, int sel, int& launch, cudaStream_t s) {
     for (int j = 0; j < b->npasses; ++j) {
         const intp_batch::Pass& p = b->pass[j];
-        for (int part = 0; part < 2; ++part) {
-            const SolveItem* items = part == 0 ? p.items : p.long_items;
-            const int64_t nitems = part == 0 ? p.nitems : p.nlong;
-            const size_t smem = part == 0 ? p.smem_elems : p.smem_long;
-            if (nitems == 0) continue;
-            cudaError_t e;
-            if (b->sched.persistent && launch < kMaxLaunches)
-                e = launch_items<R, true>(b, data, items, nitems, smem, b->counters + launch++, sel, bands, s);
-            else
-                e = launch_items<R, false>(b, data, items, nitems, smem, nullptr, sel, bands, s);
+        for (int k = 0; k < p.nclasses; ++k) {
+            const int c = p.order[k];
+            BatchSolveLaunch a{};
+            a.items = p.items[c];
+            a.nitems = p.nitems[c];
+            a.persistent = b->sched.persistent && launch < kMaxLaunches;
+            a.counter = a.persistent ? b->counters + launch++ : nullptr;
+            a.tables = b->d_tables;
+            a.fac = b->d_fac;
+            a.off = b->d_off;
+            a.refine = b->d_refine;
+            a.sel = sel;
+            a.sm_count = batch_sm_count();
+            const cudaError_t e = launch_batch_solve(data, c, a, s);
             if (e != cudaSuccess) return e;
         }
     }
@@ -523,7 +316,6 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
     int launch = 0;
     if (b->sched.persistent)
         BATCH_CUDA(cudaMemsetAsync(b->counters, 0, sizeof(unsigned int) * kMaxLaunches, s), "cudaMemsetAsync(counters)");
-    const int2* bands = b->d_bands;
     const unsigned nch = static_cast<unsigned>(b->nchunks);
     if (!b->mixed()) {
         double* c = static_cast<double*>(b->ctrl);
@@ -531,7 +323,7 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
                                                              b->d_off, b->d_refine);
         note_launch();
         BATCH_CUDA(cudaGetLastError(), "batch shift copy");
-        BATCH_CUDA(run_passes<double>(b, c, kSelAll, bands, launch, s), "batch line solve (fp64)");
+        BATCH_CUDA(run_passes<double>(b, c, kBatchSelAll, launch, s), "batch line solve (fp64)");
         b->has_ctrl = true;
         return INTP_OK;
     }
@@ -556,9 +348,9 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
     note_launch();
     BATCH_CUDA(cudaGetLastError(), "batch shift copy");
     if (b->min_refine == 0)
-        BATCH_CUDA(run_passes<float>(b, c, kSelPlain, bands, launch, s), "batch line solve (fp32)");
+        BATCH_CUDA(run_passes<float>(b, c, kBatchSelPlain, launch, s), "batch line solve (fp32)");
     if (w) {
-        BATCH_CUDA(run_passes<DW>(b, w, kSelDW, bands, launch, s), "batch line solve (double-word)");
+        BATCH_CUDA(run_passes<DW>(b, w, kBatchSelDW, launch, s), "batch line solve (double-word)");
         batch_elementwise_kernel<float><<<nch, 256, 0, s>>>(1, nullptr, c, w, b->ctrl_lo, b->d_chunks, b->d_tables,
                                                             b->d_off, b->d_refine);
         note_launch();
@@ -625,6 +417,13 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
                 delete b;
                 return bfail(INTP_ERR_INVALID_ARGUMENT, where + err);
             }
+            for (int a = 0; a < d.dim; ++a) {
+                const LineFactor& f = b->models[i].axis[a].factor;
+                if (f.p != f.q || f.p > (f.cyclic ? kBatchMaxCyclicBand : kBatchMaxBand)) {
+                    delete b;
+                    return bfail(INTP_ERR_UNSUPPORTED, where + "band outside the batched solve's classes");
+                }
+            }
             if (b->models[i].total >= (int64_t{1} << 31)) {
                 delete b;
                 return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables hold fewer than 2^31 values each");
@@ -646,21 +445,15 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     Arena ar;
     std::vector<PackedTable> packed(static_cast<size_t>(ntables));
     for (int64_t i = 0; i < ntables; ++i) pack_table(b->models[i], ar, packed[i]);
-    std::vector<PassLists> passes;
+    std::vector<std::vector<SolveItem>> passes;
+    std::vector<int64_t> pass_values;
     std::vector<ChunkItem> chunks;
-    build_work(*b, b->sched, passes, chunks);
-    std::vector<int2> bands(static_cast<size_t>(ntables) * kBatchMaxDim, int2{0, 0});
-    for (int64_t i = 0; i < ntables; ++i)
-        for (int a = 0; a < b->models[i].dim; ++a) {
-            const LineFactor& f = b->models[i].axis[a].factor;
-            bands[i * kBatchMaxDim + a] = int2{f.p, f.cyclic ? 1 : 0};
-        }
+    build_work(*b, b->sched, passes, pass_values, chunks);
     std::vector<int32_t> refine32(b->refine.begin(), b->refine.end());
     const size_t o_tables = ar.add(sizeof(TableDev) * static_cast<size_t>(ntables));
     const size_t o_fac = ar.add(sizeof(AxisFactorDev) * static_cast<size_t>(ntables) * kBatchMaxDim);
     const size_t o_off = ar.put(b->off);
     const size_t o_ref = ar.put(refine32);
-    const size_t o_bands = ar.put(bands);
     const size_t o_chunks = ar.put(chunks);
     cudaError_t e = cudaMalloc(&b->arena, ar.host.size());
     if (e != cudaSuccess) {
@@ -698,7 +491,6 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     b->d_fac = reinterpret_cast<const AxisFactorDev*>(base + o_fac);
     b->d_off = reinterpret_cast<const int64_t*>(base + o_off);
     b->d_refine = reinterpret_cast<const int32_t*>(base + o_ref);
-    b->d_bands = reinterpret_cast<const int2*>(base + o_bands);
     b->d_chunks = reinterpret_cast<const ChunkItem*>(base + o_chunks);
     b->nchunks = static_cast<int64_t>(chunks.size());
     e = cudaMalloc(reinterpret_cast<void**>(&b->counters), sizeof(unsigned int) * kMaxLaunches);
@@ -775,13 +567,13 @@ intp_status intp_batch_autotune(intp_batch* b, const double* values, int32_t val
         st = bfail(INTP_ERR_CUDA, "cudaEventCreate");
     intp_batch_schedule best{};
     double best_ms = 0.0;
-    const int32_t stage_kb[] = {8, 16, 32};
+    const int32_t crows[] = {16, 32};
     const int32_t rows[] = {16, 32};
     for (int pers = 0; pers < 2 && st == INTP_OK; ++pers)
-        for (int32_t kb : stage_kb)
+        for (int32_t cr : crows)
             for (int32_t r : rows) {
                 if (st != INTP_OK) break;
-                intp_batch_schedule sc{pers, kb, r, 0, 0.0};
+                intp_batch_schedule sc{pers, cr, r, 0, 0.0};
                 st = apply_schedule(b, sc);
                 if (st == INTP_OK) st = batch_interpolate(b, v, s);  // warm-up
                 if (st != INTP_OK) break;

@@ -7,19 +7,38 @@
 #include <cstdint>
 
 #include "device_common.cuh"
+#include "dw.cuh"
 
 namespace intp_gb300 {
+
+struct AxisFactorDev;
+
+constexpr int kBatchMaxDim = 3;
+
+// Band classes of the line solves: non-cyclic bands p = q = 0..kBatchMaxBand
+// are classes 0..kBatchMaxBand, cyclic bands p = q = 0..kBatchMaxCyclicBand
+// follow them. Each class has its own kernel instance.
+constexpr int kBatchMaxBand = 6, kBatchMaxCyclicBand = 3;
+constexpr int kBatchClasses = kBatchMaxBand + 1 + kBatchMaxCyclicBand + 1;
+inline int batch_band_class(int p, bool cyclic) { return cyclic ? kBatchMaxBand + 1 + p : p; }
+
+// Tables a solve launch works on (mixed batches): every table, the tables
+// solved in FP32 (refine = 0), or the ones solved in double-word arithmetic.
+constexpr int kBatchSelAll = -1, kBatchSelPlain = -2, kBatchSelDW = -3;
+
+// the per-warp chunk transpose of contiguous lines (WarpContigChunks)
+constexpr int kBatchTransposeElems = 32 * 33;
 
 // Up to 32 lines of one table along one axis, solved by one warp (lane l
 // takes line line0 + l). Line l of axis a starts at element o*n*S + t with
 // o = l / S, t = l % S, where S is the axis stride; consecutive lines of a
 // strided axis (S > 1) are adjacent in memory, so the warp's accesses
-// coalesce. Lines of the contiguous axis (S = 1) are staged in shared memory
-// when `staged` is set.
+// coalesce. Lines of the contiguous axis (S = 1, `contig` set) move chunk by
+// chunk through a per-warp shared-memory transpose.
 struct SolveItem {
     int32_t table;
     int16_t axis;
-    int8_t staged;
+    int8_t contig;
     int8_t pad8;
     int32_t rows;
     int32_t pad;
@@ -40,6 +59,32 @@ struct EvalItem {
     int64_t coord_off;  // first coordinate (in doubles) of the run
     int64_t out_pt;     // global index of the run's first point
 };
+
+// One launch of the batched line solves: the work items of one pass and one
+// band class, and the batch's device arrays.
+struct BatchSolveLaunch {
+    const SolveItem* items;
+    int64_t nitems;
+    unsigned int* counter;  // work counter (persistent launches)
+    const TableDev* tables;
+    const AxisFactorDev* fac;  // [table * kBatchMaxDim + axis]
+    const int64_t* off;        // control-point offset of each table
+    const int32_t* refine;     // per table: 0 FP32 solve, > 0 double-word solve
+    int sel;                   // kBatchSel*
+    bool persistent;           // a grid of a few warps per SM drains an atomic work queue
+    int sm_count;
+};
+
+// Solves the items of one band class in place (batch_solve_{f32,dw,f64}.cu).
+cudaError_t launch_batch_solve(float* data, int cls, const BatchSolveLaunch& a, cudaStream_t s);
+cudaError_t launch_batch_solve(DW* data, int cls, const BatchSolveLaunch& a, cudaStream_t s);
+cudaError_t launch_batch_solve(double* data, int cls, const BatchSolveLaunch& a, cudaStream_t s);
+
+// Test hook: caps the warm-up rows of the warp-segmented substitution in
+// each of those translation units (< 0 restores the default).
+cudaError_t set_warm_cap_batch_f32(int rows);
+cudaError_t set_warm_cap_batch_dw(int rows);
+cudaError_t set_warm_cap_batch_f64(int rows);
 
 // Evaluates the items of one (dim, order) class: tables[] are the batch's
 // device descriptors (control points bound).

@@ -294,14 +294,14 @@ intp_status intp_batch_build(intp_batch* batch, const double* values, int32_t va
 typedef struct intp_batch_schedule {
     int32_t persistent;    /* 1: each axis pass is a grid of a few warps per SM draining an atomic work
                               queue (longest lines first); 0: one CTA per work item */
-    int32_t stage_kb;      /* shared memory per warp for contiguous lines, KB (1..200); staged lines
-                              above it run in a launch of their own */
+    int32_t contig_rows;   /* lines per work item on the contiguous axis (1..32); each chunk of them
+                              moves through a per-warp shared-memory transpose */
     int32_t strided_rows;  /* lines per work item on strided axes (1..32) */
     int32_t pad_;
     double build_ms;       /* build time measured by intp_batch_autotune (0 when set by hand) */
 } intp_batch_schedule;
 
-/* Sets / reads the schedule (the default: one CTA per item, 16 KB, 32 lines). */
+/* Sets / reads the schedule (the default: one CTA per item, 32 lines per item on every axis). */
 intp_status intp_batch_set_schedule(intp_batch* batch, const intp_batch_schedule* schedule);
 intp_status intp_batch_get_schedule(const intp_batch* batch, intp_batch_schedule* schedule);
 /* Times a build of the batch from `values` (as intp_batch_build) under each

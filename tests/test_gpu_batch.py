@@ -195,19 +195,20 @@ def test_batch_rejects_bad_requests():
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_schedules_give_identical_control_points(precision):
     """The line solves' schedule (persistent work queue or one CTA per item,
-    staging budget, lines per item) never changes a line's arithmetic: every
-    schedule, and the one intp_batch_autotune picks, gives the same control
-    points bit for bit (and those of the tables built alone)."""
+    lines per item on the contiguous and the strided axes) never changes a
+    line's arithmetic: every schedule, and the one intp_batch_autotune picks,
+    gives the same control points bit for bit (and those of the tables built
+    alone)."""
     b = _golden_batch(precision)
     want = [b.control_points(i) for i in range(len(BATCHABLE))]
     values = np.concatenate([Z[m["name"] + "/values"] for m in BATCHABLE])
-    for persistent, kb, rows in ((False, 16, 32), (True, 1, 8), (True, 64, 1), (False, 4, 16)):
-        b.set_schedule(persistent, kb, rows)
-        assert b.schedule()["stage_kb"] == kb
+    for persistent, crows, rows in ((False, 32, 32), (True, 1, 8), (True, 7, 1), (False, 16, 16)):
+        b.set_schedule(persistent, crows, rows)
+        assert b.schedule()["contig_rows"] == crows
         b.build(values)
         for i in range(len(BATCHABLE)):
-            assert np.array_equal(b.control_points(i), want[i]), (persistent, kb, rows, BATCHABLE[i]["name"])
+            assert np.array_equal(b.control_points(i), want[i]), (persistent, crows, rows, BATCHABLE[i]["name"])
     chosen = b.autotune(values)
-    assert chosen["build_ms"] > 0 and chosen["stage_kb"] in (8, 16, 32)
+    assert chosen["build_ms"] > 0 and chosen["contig_rows"] in (16, 32)
     for i in range(len(BATCHABLE)):
         assert np.array_equal(b.control_points(i), want[i])
