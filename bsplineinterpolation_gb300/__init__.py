@@ -531,7 +531,9 @@ class TableBatch:
 
     `tables` is a sequence of (order, periodicity, mesh_dims, x_ranges)
     tuples, one per table, with the meaning of InterpolationFunctionTemplate's
-    arguments (dimension 1..3). Every table of a batch has one precision.
+    arguments (dimension 1..3), optionally with a fifth entry C > 1 for a
+    vector-valued table of C components (its values hold the C components of
+    each mesh point consecutively). Every table of a batch has one precision.
     The reference builds such tables one InterpolationFunction at a time
     (InterpolationTemplate.hpp:60-143); here one launch per axis pass solves
     all of them, and one launch per (dimension, order) class evaluates them.
@@ -544,20 +546,23 @@ class TableBatch:
         self._keep = []
         self.dims = []
         self.orders = []
+        self.channels = []
         for i, t in enumerate(tables):
-            order, periodicity, mesh_dims, x_ranges = t
+            order, periodicity, mesh_dims, x_ranges = t[:4]
+            ch = int(t[4]) if len(t) > 4 else 1
             desc, keep, dims, _ = _make_desc(order, periodicity, mesh_dims, list(x_ranges), precision,
-                                             refine_steps)
+                                             refine_steps, ch)
             descs[i] = desc
             self._keep.extend(keep)
             self.dims.append(dims)
             self.orders.append(int(order))
+            self.channels.append(max(1, ch))
         h = C.c_void_p()
         _lib.check(lib.intp_batch_create(descs, n, C.byref(h)))
         self._h = h
         self.ntables = n
         self.precision = precision
-        self.sizes = [int(np.prod(d)) for d in self.dims]
+        self.sizes = [int(np.prod(d)) * c for d, c in zip(self.dims, self.channels)]
         self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
 
     def __del__(self):
@@ -616,14 +621,17 @@ class TableBatch:
     def control_points(self, i):
         out = np.zeros(self.sizes[i])
         _lib.check(_lib.load().intp_batch_get_control_points(self._h, i, out.ctypes.data))
-        return out.reshape(self.dims[i])
+        shape = list(self.dims[i]) + ([self.channels[i]] if self.channels[i] > 1 else [])
+        return out.reshape(shape)
 
     def evaluate(self, coords, point_offsets, derivs=None, out=None, out_dtype=None, stream=None):
         """Evaluates table i at its points point_offsets[i] .. point_offsets[i+1]-1.
         `coords`: CUDA tensor of every table's points in table order (dim_i
         doubles per point). `derivs`: K rows of up to 4 derivative orders (a
         table of dimension D uses the first D). Returns a (points x K) CUDA
-        tensor."""
+        tensor; a batch with vector-valued tables returns one flat tensor in
+        which table i's outputs (its points x K x C_i) follow those of the
+        tables before it (`output_views` splits it)."""
         torch = _torch()
         lib = _lib.load()
         po = np.ascontiguousarray(np.asarray(point_offsets, np.int64))
@@ -644,11 +652,28 @@ class TableBatch:
         x = coords.to(torch.float64).contiguous().reshape(-1)
         npts = int(po[-1])
         if out is None:
-            out = torch.empty((npts, K), dtype=torch.float32 if od == _lib.F32 else torch.float64,
-                              device=x.device)
+            dt = torch.float32 if od == _lib.F32 else torch.float64
+            if max(self.channels) == 1:
+                out = torch.empty((npts, K), dtype=dt, device=x.device)
+            else:
+                n = np.diff(po)
+                out = torch.empty(int(np.sum(n * K * np.asarray(self.channels))), dtype=dt, device=x.device)
         _lib.check(lib.intp_batch_eval(self._h, C.c_void_p(x.data_ptr()), po.ctypes.data, kp, K,
                                        C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
         return out
+
+    def output_views(self, out, point_offsets, K=1):
+        """Table i's outputs as a (points x K) view, or (points x K x C) for a
+        vector-valued table, of an `evaluate` result."""
+        po = np.asarray(point_offsets, np.int64)
+        flat = out.reshape(-1)
+        views, e = [], 0
+        for i in range(self.ntables):
+            n, c = int(po[i + 1] - po[i]), self.channels[i]
+            v = flat[e:e + n * K * c]
+            views.append(v.reshape(n, K) if c == 1 else v.reshape(n, K, c))
+            e += n * K * c
+        return views
 
 
 class Server:
@@ -691,11 +716,18 @@ class Server:
             return C.c_void_p(x.data_ptr())
         return C.c_void_p(x.ctypes.data)
 
-    def submit_build(self, order, periodicity, values, *x_ranges, precision="mixed", refine_steps=-1):
+    def submit_build(self, order, periodicity, values, *x_ranges, precision="mixed", refine_steps=-1,
+                     vector=False):
         """Queues a table build from `values` (mesh, host array or tensor);
-        returns (table_id, request_id)."""
+        returns (table_id, request_id). vector=True: the last axis of `values`
+        holds the C components of a vector-valued table, whose evaluations
+        return C values per output (N x K x C)."""
         dims = list(values.shape)
-        desc, keep, _, _ = _make_desc(order, periodicity, dims, x_ranges, precision, refine_steps)
+        channels = 1
+        if vector:
+            channels = dims[-1]
+            dims = dims[:-1]
+        desc, keep, _, _ = _make_desc(order, periodicity, dims, x_ranges, precision, refine_steps, channels)
         tid, rid = C.c_int64(), C.c_int64()
         _lib.check(_lib.load().intp_server_submit_build(self._h, C.byref(desc), self._ptr(values),
                                                        C.byref(tid), C.byref(rid)))
@@ -703,8 +735,8 @@ class Server:
         return tid.value, rid.value
 
     def submit_eval(self, table_id, points, out, derivs=None, out_dtype="f32"):
-        """Queues an evaluation of `points` (N x D) into `out` (N x K);
-        returns the request id."""
+        """Queues an evaluation of `points` (N x D) into `out` (N x K, or
+        N x K x C for a C-channel table); returns the request id."""
         od = _lib.F32 if out_dtype == "f32" else _lib.F64
         if derivs is None:
             kp, K, karr = None, 1, None

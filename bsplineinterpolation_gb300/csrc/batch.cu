@@ -51,7 +51,8 @@ struct intp_batch {
     int device = 0;
     int64_t ntables = 0;
     std::vector<TableModel> models;
-    std::vector<int64_t> off;      // ntables + 1 element offsets
+    std::vector<int64_t> off;      // ntables + 1 element offsets (every channel)
+    std::vector<int> channels;     // values per mesh point of each table (vector-valued tables)
     // mixed: per table 0 (FP32 solve) or > 0 (double-word solve, control
     // points kept as ctrl + ctrl_lo); the largest and the smallest value
     std::vector<int> refine;
@@ -81,8 +82,20 @@ struct intp_batch {
     intp_batch_schedule sched{0, 32, 32, 0, 0.0};
     void* work = nullptr;                // the schedule's work lists (device)
     unsigned int* counters = nullptr;    // work counters of the persistent passes (device)
+    // The band classes of one pass run concurrently: class order[0] on the
+    // caller's stream, the others on these streams, forked from and joined
+    // back to the caller's stream by events (created on first need).
+    cudaStream_t side[kBatchClasses - 1] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kBatchClasses - 1] = {};
+    int nside = 0;
 
     ~intp_batch() {
+        for (int k = 0; k < nside; ++k) {
+            cudaStreamDestroy(side[k]);
+            cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
         if (work) cudaFree(work);
         if (counters) cudaFree(counters);
         if (arena) cudaFree(arena);
@@ -148,40 +161,72 @@ __global__ void __launch_bounds__(256) batch_elementwise_kernel(int op, const do
     const bool dw = w && refine[c.table] > 0;
     if (op != 0 && !dw) return;
     const int64_t o0 = off[c.table];
+    // each thread moves kU elements per step, their loads issued together
+    constexpr int kU = 4;
+    const int step = kU * blockDim.x;
     if (op == 0) {
         const TableDev& t = tables[c.table];
-        // batched tables hold fewer than 2^31 values each: 32-bit index math
-        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
-            const int64_t i = c.start + e;
-            int r = static_cast<int>(i), o = 0;
-            for (int d = t.dim - 1; d >= 0; --d) {
-                const AxisDev& a = t.ax[d];
-                const int na = static_cast<int>(a.n);
-                const int q = r / na;
-                int idx = r - q * na;
-                r = q;
-                if (a.periodic) {
-                    idx += (t.order / 2) % na;
-                    if (idx >= na) idx -= na;
-                }
-                o += idx * static_cast<int>(a.stride);
+        // vector-valued tables: input element j is point j / C, channel
+        // j % C (channel fastest); channel ch's mesh starts at ch * chan_stride
+        const int C = t.channels;
+        bool shifted = C > 1;
+        for (int d = 0; d < t.dim; ++d) shifted = shifted || (t.ax[d].periodic && (t.order / 2) % t.ax[d].n != 0);
+        for (int e0 = threadIdx.x; e0 < c.len; e0 += step) {
+            double v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int e = e0 + u * blockDim.x;
+                v[u] = e < c.len ? src[o0 + c.start + e] : 0.0;
             }
-            const double v = src[o0 + i];
-            if (dw) {
-                float h, l;
-                split_double(v, h, l);
-                w[o0 + o] = DW(h, l);
-            } else {
-                dst[o0 + o] = static_cast<R>(v);
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int e = e0 + u * blockDim.x;
+                if (e >= c.len) break;
+                // batched tables hold fewer than 2^31 values each: 32-bit
+                // index math
+                int o = static_cast<int>(c.start + e);
+                if (shifted) {
+                    const int pt = o / C, ch = o - pt * C;
+                    int r = pt;
+                    o = ch * static_cast<int>(t.chan_stride);
+                    for (int d = t.dim - 1; d >= 0; --d) {
+                        const AxisDev& a = t.ax[d];
+                        const int na = static_cast<int>(a.n);
+                        const int q = r / na;
+                        int idx = r - q * na;
+                        r = q;
+                        if (a.periodic) {
+                            idx += (t.order / 2) % na;
+                            if (idx >= na) idx -= na;
+                        }
+                        o += idx * static_cast<int>(a.stride);
+                    }
+                }
+                if (dw) {
+                    float h, l;
+                    split_double(v[u], h, l);
+                    w[o0 + o] = DW(h, l);
+                } else {
+                    dst[o0 + o] = static_cast<R>(v[u]);
+                }
             }
         }
     } else {
         float* x = reinterpret_cast<float*>(dst);
-        for (int e = threadIdx.x; e < c.len; e += blockDim.x) {
-            const int64_t i = o0 + c.start + e;
-            const DW v = w[i];
-            x[i] = v.hi;
-            ctrl_lo[i] = v.lo;
+        for (int e0 = threadIdx.x; e0 < c.len; e0 += step) {
+            DW v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int e = e0 + u * blockDim.x;
+                v[u] = e < c.len ? w[o0 + c.start + e] : DW(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int e = e0 + u * blockDim.x;
+                if (e >= c.len) break;
+                x[o0 + c.start + e] = v[u].hi;
+                ctrl_lo[o0 + c.start + e] = v[u].lo;
+            }
         }
     }
 }
@@ -203,6 +248,7 @@ void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<
     chunks.clear();
     for (int64_t i = 0; i < b.ntables; ++i) {
         const TableModel& m = b.models[i];
+        const int C = b.channels[i];
         for (int j = 0; j < m.dim; ++j) {
             const int a = m.dim - 1 - j;
             const int64_t n = m.axis[a].n;
@@ -211,22 +257,24 @@ void build_work(const intp_batch& b, const intp_batch_schedule& sc, std::vector<
             const int64_t rows_max = contig ? sc.contig_rows : sc.strided_rows;
             const LineFactor& f = m.axis[a].factor;
             const size_t list = static_cast<size_t>(j) * kBatchClasses + batch_band_class(f.p, f.cyclic);
-            values[list] += m.total;
-            for (int64_t l0 = 0; l0 < nlines; l0 += rows_max) {
-                SolveItem it{};
-                it.table = static_cast<int32_t>(i);
-                it.axis = static_cast<int16_t>(a);
-                it.contig = contig ? 1 : 0;
-                it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
-                it.line0 = l0;
-                passes[list].push_back(it);
-            }
+            values[list] += m.total * C;
+            for (int ch = 0; ch < C; ++ch)
+                for (int64_t l0 = 0; l0 < nlines; l0 += rows_max) {
+                    SolveItem it{};
+                    it.table = static_cast<int32_t>(i);
+                    it.axis = static_cast<int16_t>(a);
+                    it.contig = contig ? 1 : 0;
+                    it.rows = static_cast<int32_t>(std::min<int64_t>(rows_max, nlines - l0));
+                    it.chan = ch;
+                    it.line0 = l0;
+                    passes[list].push_back(it);
+                }
         }
-        for (int64_t s = 0; s < m.total; s += kChunkElems) {
+        for (int64_t s = 0; s < m.total * C; s += kChunkElems) {
             ChunkItem c{};
             c.table = static_cast<int32_t>(i);
             c.start = s;
-            c.len = static_cast<int32_t>(std::min<int64_t>(kChunkElems, m.total - s));
+            c.len = static_cast<int32_t>(std::min<int64_t>(kChunkElems, m.total * C - s));
             chunks.push_back(c);
         }
     }
@@ -284,15 +332,52 @@ int batch_sm_count() {
     return n;
 }
 
-// One solve of every table: the axis passes in order, a launch per band
-// class present in the pass. `launch` numbers the persistent launches of the
-// build (their work counters were cleared when the build started).
+// Streams and events for `need` concurrent side launches.
+cudaError_t ensure_side_streams(intp_batch* b, int need) {
+    if (need > 0 && !b->fork) {
+        cudaError_t e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    while (b->nside < need) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(st);
+            return e;
+        }
+        b->side[b->nside] = st;
+        b->join[b->nside] = ev;
+        ++b->nside;
+    }
+    return cudaSuccess;
+}
+
+// One solve of every table: the axis passes in order; within a pass a launch
+// per band class present, the classes concurrently (they touch disjoint
+// tables) and joined before the next pass. `launch` numbers the persistent
+// launches of the build (their work counters were cleared when the build
+// started).
 template <class R>
 cudaError_t run_passes(intp_batch* b, R* data, int sel, int& launch, cudaStream_t s) {
     for (int j = 0; j < b->npasses; ++j) {
         const intp_batch::Pass& p = b->pass[j];
+        if (p.nclasses == 0) continue;
+        cudaError_t e = ensure_side_streams(b, p.nclasses - 1);
+        if (e != cudaSuccess) return e;
+        if (p.nclasses > 1) {
+            e = cudaEventRecord(b->fork, s);
+            if (e != cudaSuccess) return e;
+        }
         for (int k = 0; k < p.nclasses; ++k) {
             const int c = p.order[k];
+            cudaStream_t sk = k == 0 ? s : b->side[k - 1];
+            if (k > 0) {
+                e = cudaStreamWaitEvent(sk, b->fork, 0);
+                if (e != cudaSuccess) return e;
+            }
             BatchSolveLaunch a{};
             a.items = p.items[c];
             a.nitems = p.nitems[c];
@@ -304,8 +389,13 @@ cudaError_t run_passes(intp_batch* b, R* data, int sel, int& launch, cudaStream_
             a.refine = b->d_refine;
             a.sel = sel;
             a.sm_count = batch_sm_count();
-            const cudaError_t e = launch_batch_solve(data, c, a, s);
+            e = launch_batch_solve(data, c, a, sk);
             if (e != cudaSuccess) return e;
+            if (k > 0) {
+                e = cudaEventRecord(b->join[k - 1], sk);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->join[k - 1], 0);
+                if (e != cudaSuccess) return e;
+            }
         }
     }
     return cudaSuccess;
@@ -379,6 +469,7 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
     b->refine.assign(static_cast<size_t>(ntables), 0);
     try {
         b->models.resize(static_cast<size_t>(ntables));
+        b->channels.assign(static_cast<size_t>(ntables), 1);
         for (int64_t i = 0; i < ntables; ++i) {
             const intp_table_desc& d = descs[i];
             const std::string where = "table " + std::to_string(i) + ": ";
@@ -390,9 +481,9 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
                 delete b;
                 return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables have dimension 1..3");
             }
-            if (d.channels > 1) {
+            if (d.channels < 0 || d.channels > INTP_GPU_MAX_CHANNELS) {
                 delete b;
-                return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables are scalar (channels <= 1)");
+                return bfail(INTP_ERR_INVALID_ARGUMENT, where + "channels must be in [0, 64]");
             }
             if (d.order < 0 || d.order > INTP_GPU_MAX_ORDER) {
                 delete b;
@@ -424,11 +515,12 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
                     return bfail(INTP_ERR_UNSUPPORTED, where + "band outside the batched solve's classes");
                 }
             }
-            if (b->models[i].total >= (int64_t{1} << 31)) {
+            b->channels[i] = d.channels > 1 ? d.channels : 1;
+            if (b->models[i].total * b->channels[i] >= (int64_t{1} << 31)) {
                 delete b;
                 return bfail(INTP_ERR_UNSUPPORTED, where + "batched tables hold fewer than 2^31 values each");
             }
-            b->off[i + 1] = b->off[i] + b->models[i].total;
+            b->off[i + 1] = b->off[i] + b->models[i].total * b->channels[i];
             if (b->mixed()) {
                 b->refine[i] = d.refine_steps == 0 ? 0 : 1;
                 b->max_refine = std::max(b->max_refine, b->refine[i]);
@@ -477,6 +569,7 @@ intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, int
         TableDev& dv = b->h_tables[i];
         std::memset(&dv, 0, sizeof dv);
         bind_table(b->models[i], lo_user, packed[i], base, dv, &fac[i * kBatchMaxDim]);
+        dv.channels = b->channels[i];
         dv.ctrl = static_cast<const unsigned char*>(b->ctrl) + static_cast<size_t>(b->off[i]) * b->elem();
         dv.ctrl_lo = b->refine[i] > 0 ? b->ctrl_lo + b->off[i] : nullptr;
     }
@@ -623,6 +716,15 @@ intp_status intp_batch_get_control_points(const intp_batch* b, int64_t table, do
     } else {
         BATCH_CUDA(cudaMemcpy(out, src, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToHost), "cudaMemcpy(ctrl)");
     }
+    // vector-valued tables: from one mesh per channel to channel fastest,
+    // as intp_table_get_control_points gives them
+    const int64_t C = b->channels[table];
+    if (C > 1) {
+        const int64_t P = n / C;
+        std::vector<double> planar(out, out + n);
+        for (int64_t i = 0; i < P; ++i)
+            for (int64_t c = 0; c < C; ++c) out[i * C + c] = planar[c * P + i];
+    }
     return INTP_OK;
 }
 
@@ -634,9 +736,11 @@ intp_status intp_batch_eval(const intp_batch* b, const double* coords, const int
     if (point_offsets[0] != 0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets[0] must be 0");
     if (derivs && (nderiv < 1 || nderiv > INTP_GPU_MAX_DERIV))
         return bfail(INTP_ERR_INVALID_ARGUMENT, "nderiv must be in [1, 16]");
-    // runs of queries per (dim, order) class
+    // runs of queries per (dim, order) class; table i's outputs follow those
+    // of the tables before it, (points x K x channels) each
     std::vector<EvalItem> items[kBatchMaxDim + 1][INTP_GPU_MAX_ORDER + 1];
-    int64_t coff = 0;
+    const int64_t K = derivs ? nderiv : 1;
+    int64_t coff = 0, ooff = 0;
     for (int64_t i = 0; i < b->ntables; ++i) {
         const int64_t p0 = point_offsets[i], p1 = point_offsets[i + 1];
         if (p1 < p0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets must not decrease");
@@ -646,10 +750,11 @@ intp_status intp_batch_eval(const intp_batch* b, const double* coords, const int
             it.table = static_cast<int32_t>(i);
             it.count = static_cast<int32_t>(std::min<int64_t>(kEvalRun, p1 - p));
             it.coord_off = coff + (p - p0) * m.dim;
-            it.out_pt = p;
+            it.out_elem = ooff + (p - p0) * K * b->channels[i];
             items[m.dim][m.order].push_back(it);
         }
         coff += (p1 - p0) * m.dim;
+        ooff += (p1 - p0) * K * b->channels[i];
     }
     const int64_t npts = point_offsets[b->ntables];
     if (npts == 0) return INTP_OK;

@@ -34,14 +34,16 @@ constexpr int kBatchTransposeElems = 32 * 33;
 // o = l / S, t = l % S, where S is the axis stride; consecutive lines of a
 // strided axis (S > 1) are adjacent in memory, so the warp's accesses
 // coalesce. Lines of the contiguous axis (S = 1, `contig` set) move chunk by
-// chunk through a per-warp shared-memory transpose.
+// chunk through a per-warp shared-memory transpose. A vector-valued table
+// stores each channel's control points as one mesh (channel ch at
+// ch * chan_stride); an item covers lines of one channel.
 struct SolveItem {
     int32_t table;
     int16_t axis;
     int8_t contig;
     int8_t pad8;
     int32_t rows;
-    int32_t pad;
+    int32_t chan;
     int64_t line0;
 };
 
@@ -52,12 +54,13 @@ struct ChunkItem {
     int64_t start;  // element index within the table
 };
 
-// A run of query points of one table, evaluated by one CTA.
+// A run of query points of one table, evaluated by one CTA. Point i of the
+// run writes its K outputs of every channel ch at out_elem + (i*K + k)*C + ch.
 struct EvalItem {
     int32_t table;
     int32_t count;
     int64_t coord_off;  // first coordinate (in doubles) of the run
-    int64_t out_pt;     // global index of the run's first point
+    int64_t out_elem;   // first output element of the run
 };
 
 // One launch of the batched line solves: the work items of one pass and one

@@ -29,9 +29,11 @@ __global__ void __launch_bounds__(kBatchEvalThreads) batch_eval_kernel(const Tab
         }
         __syncthreads();
         const double* xs = coords + it.coord_off;
+        void* o = out_f32 ? static_cast<void*>(static_cast<float*>(out) + it.out_elem)
+                          : static_cast<void*>(static_cast<double*>(out) + it.out_elem);
         for (int i = threadIdx.x; i < it.count; i += blockDim.x)
-            eval_detail::eval_point<D, O, MIXED>(sh_t, xs + static_cast<int64_t>(i) * D, plan, out, out_f32,
-                                                 (it.out_pt + i) * plan.k);
+            eval_detail::eval_point<D, O, MIXED>(sh_t, xs + static_cast<int64_t>(i) * D, plan, o, out_f32,
+                                                 static_cast<int64_t>(i) * plan.k);
     }
 }
 

@@ -68,7 +68,7 @@ __device__ __forceinline__ void solve_item(R* __restrict__ data, const SolveItem
     const AxisDev& ax = t.ax[it.axis];
     const int64_t n = ax.n, S = ax.stride;
     const FactorView<R> fv = factor_view<R>(fac[it.table * kBatchMaxDim + it.axis], n);
-    R* base = data + off[it.table];
+    R* base = data + off[it.table] + it.chan * t.chan_stride;
     if (it.contig) {
         // S == 1: lines line0 .. line0+rows-1 are one contiguous run of
         // rows*n; each chunk moves through the warp's [32][33] transpose (all

@@ -540,10 +540,10 @@ size_t table_device_bytes(const intp_table* t) {
 }
 
 size_t table_build_scratch_bytes(const intp_table_desc* desc) {
-    int64_t total = 1;
+    int64_t total = desc->channels > 1 ? desc->channels : 1;
     for (int d = 0; d < desc->dim && d < INTP_GPU_MAX_DIM; ++d) total *= desc->size[d];
     // values staging (FP64) plus, in the mixed form, the double-word solve's
-    // working array
+    // working array (every channel)
     size_t b = static_cast<size_t>(total) * 8;
     if (desc->precision == INTP_PRECISION_MIXED) b += static_cast<size_t>(total) * sizeof(DW);
     return b;

@@ -114,6 +114,7 @@ struct Table {
     intp_table* t = nullptr;
     int32_t state = kQueued;
     int dim = 0;
+    int channels = 1;       // values per mesh point (vector-valued tables)
     int refs = 0;           // queued or running requests that use the table
     bool release = false;   // drop once refs reaches 0
     size_t bytes = 0;       // device bytes while resident
@@ -143,7 +144,7 @@ struct Slot {
 };
 
 int64_t build_values(const intp_table_desc& d) {
-    int64_t n = 1;
+    int64_t n = d.channels > 1 ? d.channels : 1;
     for (int k = 0; k < d.dim; ++k) n *= d.size[k];
     return n;
 }
@@ -334,7 +335,7 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         if (r->build) {
             const size_t need = table_build_scratch_bytes(&r->desc) +
                                 [&] {
-                                    int64_t n = 1;
+                                    int64_t n = std::max(r->desc.channels, 1);
                                     for (int d = 0; d < r->desc.dim; ++d) n *= r->desc.size[d];
                                     return static_cast<size_t>(n) * 8 + (size_t{1} << 20);
                                 }();
@@ -387,7 +388,8 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         // order
         Unit u;
         u.table = r->table;
-        const int K = r->derivs.empty() ? 1 : r->nderiv;
+        // output values per point: one per derivative and channel
+        const int K = (r->derivs.empty() ? 1 : r->nderiv) * tb.channels;
         const size_t ob = r->out_dtype == INTP_F32 ? 4 : 8;
         const size_t per_pt = static_cast<size_t>(tb.dim) * 8 + static_cast<size_t>(K) * ob + kEvalScratchPerPoint;
         const int64_t cap = std::min(max_batch_points, s.small_only ? kSmallPoints : kPiecePoints);
@@ -628,7 +630,8 @@ intp_status intp_server_submit_build(intp_server* s, const intp_table_desc* desc
                                      int64_t* table_id, int64_t* request_id) {
     if (!s || !desc || !values || !table_id || !request_id) return sfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     if (desc->dim < 1 || desc->dim > INTP_GPU_MAX_DIM) return sfail(INTP_ERR_UNSUPPORTED, "dimension must be in [1, 4]");
-    if (desc->channels > 1) return sfail(INTP_ERR_UNSUPPORTED, "served tables are scalar (channels <= 1)");
+    if (desc->channels < 0 || desc->channels > INTP_GPU_MAX_CHANNELS)
+        return sfail(INTP_ERR_INVALID_ARGUMENT, "channels must be in [0, 64]");
     Request* r = new (std::nothrow) Request();
     if (!r) return sfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
     r->build = true;
@@ -648,6 +651,7 @@ intp_status intp_server_submit_build(intp_server* s, const intp_table_desc* desc
         Table& tb = s->tables[r->table];
         tb.state = kQueued;
         tb.dim = desc->dim;
+        tb.channels = desc->channels > 1 ? desc->channels : 1;
         s->requests[r->id] = r;
         s->pending.push_back(r);
         *table_id = r->table;

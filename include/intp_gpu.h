@@ -68,7 +68,9 @@ typedef struct intp_table_desc {
      * type T, Interpolation.hpp:17-507). Values and control points are then
      * prod(size) x C, channel fastest, and every evaluation output is C
      * values. All channels share the knots, the factors and, per query, the
-     * basis weights. Single tables only (not batches or the serving loop). */
+     * basis weights. Single tables, batches and the serving loop take them;
+     * they evaluate with the direct kernel (the binned path stages one
+     * channel's tiles). */
     int32_t channels;
     int32_t reserved_;
 } intp_table_desc;
@@ -278,12 +280,12 @@ typedef struct intp_batch intp_batch;
  * constructions (InterpolationTemplate.hpp:60-79). */
 intp_status intp_batch_create(const intp_table_desc* descs, int64_t ntables, intp_batch** out);
 intp_status intp_batch_destroy(intp_batch* batch);
-/* Number of tables and total number of mesh values (sum of prod(size)). */
+/* Number of tables and total number of mesh values (sum of prod(size) x C). */
 intp_status intp_batch_info(const intp_batch* batch, int64_t* ntables, int64_t* total_values);
 
 /* Solves the control points of every table. `values` holds each table's
  * row-major value mesh, in table order (total_values doubles, host or device
- * memory). Replaces InterpolationFunctionTemplate::interpolate
+ * memory; a C-channel table's C values per mesh point consecutive). Replaces InterpolationFunctionTemplate::interpolate
  * (InterpolationTemplate.hpp:118-143) once per table. */
 intp_status intp_batch_build(intp_batch* batch, const double* values, int32_t values_on_device, void* stream);
 
@@ -310,7 +312,8 @@ intp_status intp_batch_get_schedule(const intp_batch* batch, intp_batch_schedule
 intp_status intp_batch_autotune(intp_batch* batch, const double* values, int32_t values_on_device,
                                 void* stream, intp_batch_schedule* chosen);
 
-/* Control points of one table (prod(size) doubles, host memory).
+/* Control points of one table (prod(size) x C doubles, channel fastest, host
+ * memory).
  * Replaces BSpline::control_points (BSpline.hpp:575-577). */
 intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table, double* ctrl_host);
 
@@ -320,7 +323,9 @@ intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table
  * those points table after table, dim_i doubles per point. derivs (host
  * memory): nderiv rows of INTP_GPU_MAX_DIM orders, of which a table of
  * dimension D uses the first D, or NULL for the value only. out (device
- * memory): point_offsets[ntables] x nderiv values of out_dtype.
+ * memory): table after table, each table's points x nderiv x C values of
+ * out_dtype (C = 1 for scalar tables: point_offsets[ntables] x nderiv in
+ * all for a scalar batch).
  * Replaces InterpolationFunction::operator() / derivative
  * (Interpolation.hpp:132-146, :177-205) per table and point. */
 intp_status intp_batch_eval(const intp_batch* batch, const double* coords, const int64_t* point_offsets,

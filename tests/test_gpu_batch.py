@@ -212,3 +212,59 @@ def test_schedules_give_identical_control_points(precision):
     assert chosen["build_ms"] > 0 and chosen["contig_rows"] in (16, 32)
     for i in range(len(BATCHABLE)):
         assert np.array_equal(b.control_points(i), want[i])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_vector_valued_tables_in_a_batch(precision):
+    """Vector-valued tables (the reference's InterpolationFunction with a
+    vector T, interpolation-test.cpp:672-703) mixed with scalar ones in one
+    batch: each table's control points and outputs equal those of the same
+    table built and evaluated alone, bit for bit, and every channel agrees
+    with the oracle's scalar table of that channel."""
+    rng = np.random.default_rng(41)
+    tables = [  # (order, periodicity, dims, channels)
+        (3, [False, False], [40, 36], 3),
+        (5, [True], [300], 1),
+        (3, [True, False], [33, 130], 2),
+        (4, [False], [2000], 4),
+        (5, [False, True, False], [12, 14, 16], 2),
+        (3, [False, False], [20, 24], 1),
+    ]
+    specs, vals, per_table = [], [], []
+    for order, per, dims, C in tables:
+        v = rng.normal(size=list(dims) + ([C] if C > 1 else []))
+        axes = np.meshgrid(*[np.linspace(0.0, 1.0, n) for n in dims], indexing="ij")
+        smooth = np.cos(3.0 * axes[0]) * np.sin(2.0 * axes[-1] + 0.5)
+        v = 1e-3 * v + (smooth[..., None] if C > 1 else smooth)
+        ranges = [(0.0, 1.0)] * len(dims)
+        specs.append((order, per, dims, ranges, C))
+        vals.append(v.ravel())
+        per_table.append(v)
+    b = bi.TableBatch(specs, precision=precision)
+    b.build(np.concatenate(vals))
+    counts = [int(rng.integers(0, 3000)) for _ in tables]
+    counts[1] = 0  # a table without points
+    po = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    pts = [rng.uniform(0.0, 1.0, (n, len(t[2]))) for n, t in zip(counts, tables)]
+    coords = torch.tensor(np.concatenate([p.ravel() for p in pts]), device="cuda")
+    derivs = np.array([[0, 0, 0], [1, 0, 0]], np.int32)
+    out = b.evaluate(coords, po, derivs=derivs, out_dtype="f64")
+    views = b.output_views(out, po, K=2)
+    for i, (order, per, dims, C) in enumerate(tables):
+        ranges = [(0.0, 1.0)] * len(dims)
+        f = bi.InterpolationFunction(order, per, per_table[i], *ranges, precision=precision, vector=C > 1)
+        assert np.array_equal(b.control_points(i), f.control_points()), i
+        if counts[i] == 0:
+            assert views[i].shape[0] == 0
+            continue
+        want = f.evaluate(torch.tensor(pts[i], device="cuda"), derivs=derivs[:, :len(dims)],
+                          out_dtype="f64").cpu().numpy()
+        got = views[i].cpu().numpy()
+        assert got.shape == want.shape, i
+        assert np.array_equal(got, want), i
+        tol = 1e-12 if precision == "fp64" else 1e-6
+        for c in range(C):
+            chan = per_table[i][..., c] if C > 1 else per_table[i]
+            ref = oracle.Spline(len(dims), order, per, dims, [0.0] * len(dims), [1.0] * len(dims)).interpolate(chan)
+            g = got[:, 0, c] if C > 1 else got[:, 0]
+            assert norm_rel_err(g, ref.eval(pts[i])) < tol, (i, c)
