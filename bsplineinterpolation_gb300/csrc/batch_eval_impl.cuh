@@ -11,7 +11,10 @@ namespace batch_detail {
 
 constexpr int kBatchEvalThreads = 128;
 
-template <int D, int O, bool MIXED>
+// LO: the plan has derivative outputs (mixed tables then contract with the
+// control points' remainders); value-only plans run an instance without that
+// code, with fewer registers.
+template <int D, int O, bool MIXED, bool LO>
 __global__ void __launch_bounds__(kBatchEvalThreads) batch_eval_kernel(const TableDev* __restrict__ tables,
                                                                        const EvalItem* __restrict__ items,
                                                                        int64_t nitems, const double* __restrict__ coords,
@@ -32,7 +35,7 @@ __global__ void __launch_bounds__(kBatchEvalThreads) batch_eval_kernel(const Tab
         void* o = out_f32 ? static_cast<void*>(static_cast<float*>(out) + it.out_elem)
                           : static_cast<void*>(static_cast<double*>(out) + it.out_elem);
         for (int i = threadIdx.x; i < it.count; i += blockDim.x)
-            eval_detail::eval_point<D, O, MIXED>(sh_t, xs + static_cast<int64_t>(i) * D, plan, o, out_f32,
+            eval_detail::eval_point<D, O, MIXED, LO>(sh_t, xs + static_cast<int64_t>(i) * D, plan, o, out_f32,
                                                  static_cast<int64_t>(i) * plan.k);
     }
 }
@@ -41,8 +44,12 @@ template <int D, int O, bool MIXED>
 cudaError_t launch_one(const TableDev* tables, const EvalItem* items, int64_t nitems, const double* coords,
                        const DerivPlan& plan, void* out, bool out_f32, cudaStream_t s) {
     const int64_t grid = nitems < 152 * 64 ? nitems : 152 * 64;
-    batch_eval_kernel<D, O, MIXED><<<static_cast<unsigned>(grid), kBatchEvalThreads, 0, s>>>(
-        tables, items, nitems, coords, plan, out, out_f32 ? 1 : 0);
+    if (MIXED && plan.has_deriv)
+        batch_eval_kernel<D, O, MIXED, true><<<static_cast<unsigned>(grid), kBatchEvalThreads, 0, s>>>(
+            tables, items, nitems, coords, plan, out, out_f32 ? 1 : 0);
+    else
+        batch_eval_kernel<D, O, MIXED, false><<<static_cast<unsigned>(grid), kBatchEvalThreads, 0, s>>>(
+            tables, items, nitems, coords, plan, out, out_f32 ? 1 : 0);
     note_launch();
     return cudaGetLastError();
 }

@@ -171,7 +171,9 @@ __device__ __forceinline__ void mixed_channel(const TableDev& t, const DerivPlan
 
 // All outputs of one query point: xp holds its D coordinates, output k goes
 // to out[o0 + k]. Shared by the direct kernel and the batched-table kernel.
-template <int D, int O, bool MIXED>
+// LO = false: a caller whose plan has no derivative output (the control
+// points' remainders are never read) drops that contraction's code.
+template <int D, int O, bool MIXED, bool LO = true>
 __device__ __forceinline__ void eval_point(const TableDev& t, const double* __restrict__ xp, const DerivPlan& plan,
                                            void* __restrict__ out, int out_f32, int64_t o0) {
     using R = typename std::conditional<MIXED, float, double>::type;
@@ -214,7 +216,7 @@ __device__ __forceinline__ void eval_point(const TableDev& t, const double* __re
             // the remainders matter for derivatives only (a value is within
             // FP32 rounding of the stored control points either way); 4D
             // tables contract the stored FP32 control points
-            if constexpr (D <= 3) {
+            if constexpr (D <= 3 && LO) {
                 if (t.ctrl_lo && plan.has_deriv) {
                     mixed_channel<D, O, true>(t, plan, cell, xr, base, off, cpc, t.ctrl_lo + ch * t.chan_stride, out,
                                               out_f32, o0, C, ch);
