@@ -26,8 +26,6 @@ inline int batch_band_class(int p, bool cyclic) { return cyclic ? kBatchMaxBand 
 // solved in FP32 (refine = 0), or the ones solved in double-word arithmetic.
 constexpr int kBatchSelAll = -1, kBatchSelPlain = -2, kBatchSelDW = -3;
 
-// the per-warp chunk transpose of contiguous lines (WarpContigChunks)
-constexpr int kBatchTransposeElems = 32 * 33;
 
 // Up to 32 lines of one table along one axis, solved by one warp (lane l
 // takes line line0 + l). Line l of axis a starts at element o*n*S + t with

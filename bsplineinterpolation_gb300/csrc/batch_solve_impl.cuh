@@ -41,8 +41,12 @@ __device__ __forceinline__ bool selected(int sel, int refine) {
     return sel == kBatchSelAll || (sel == kBatchSelPlain ? refine == 0 : refine > 0);
 }
 
-// Lines are walked in chunks of this many elements (registers per lane).
-constexpr int kChunk = 16;
+// Lines are walked in chunks of this many elements (registers per lane; the
+// next chunk's strided loads are held in registers too).
+template <class R>
+constexpr int chunk_of() {
+    return sizeof(R) == 4 ? 16 : 8;
+}
 
 // A line of at least this many elements that is a warp's only line is solved
 // by the whole warp (solve_line_warp).
@@ -54,6 +58,11 @@ template <class R>
 constexpr int warm_rows() {
     return sizeof(R) == 4 ? 64 : 128;
 }
+
+// Contiguous lines: chunks through a double per-warp stage, the next
+// chunk's rows in flight while one is solved.
+template <class R>
+using ContigIo = WarpContigChunksPF<R, chunk_of<R>()>;
 
 // The work of one item (up to 32 lines of one table and axis, band P = Q,
 // cyclic or not) for one warp. `sel` picks the tables of a mixed batch.
@@ -71,32 +80,32 @@ __device__ __forceinline__ void solve_item(R* __restrict__ data, const SolveItem
     R* base = data + off[it.table] + it.chan * t.chan_stride;
     if (it.contig) {
         // S == 1: lines line0 .. line0+rows-1 are one contiguous run of
-        // rows*n; each chunk moves through the warp's [32][33] transpose (all
-        // lanes take part, lane l owning line line0 + l)
+        // rows*n; each chunk moves through the warp's [32][chunk+1] stages
+        // (all lanes take part, lane l owning line line0 + l)
         R* x = base + it.line0 * n;
         if (it.rows == 1 && n >= kWarpLineMin)
             solve_line_warp<R, P, P, CYC, warm_rows<R>(), true>(fv, LineRef<R>{x, 1}, lane);
         else
-            solve_line_chunked<R, P, P, CYC, kChunk>(fv, WarpContigChunks<R>{x, n, it.rows, tile, lane});
+            solve_line_chunked<R, P, P, CYC, chunk_of<R>()>(fv, ContigIo<R>{x, n, it.rows, tile, lane});
         return;
     }
     if (lane < it.rows) {
         const int64_t l = it.line0 + lane;
         const int64_t o = l / S, tt = l - o * S;
-        solve_line_chunked<R, P, P, CYC, kChunk>(fv, StridedChunks<R>{base + o * n * S + tt, S});
+        solve_line_chunked<R, P, P, CYC, chunk_of<R>()>(fv, StridedChunks<R>{base + o * n * S + tt, S});
     }
 }
 
 // One warp per CTA. PERSIST: a grid of a few warps per SM drains the list
 // through an atomic counter (longest lines first), else one CTA per item.
 template <class R, bool PERSIST, int P, bool CYC>
-__global__ void __launch_bounds__(32) solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
+__global__ void __launch_bounds__(32, 16) solve_kernel(R* __restrict__ data, const SolveItem* __restrict__ items,
                                                    int64_t nitems, unsigned int* __restrict__ counter,
                                                    const TableDev* __restrict__ tables,
                                                    const AxisFactorDev* __restrict__ fac,
                                                    const int64_t* __restrict__ off,
                                                    const int32_t* __restrict__ refine, int sel) {
-    __shared__ __align__(16) R tile[kBatchTransposeElems];
+    __shared__ __align__(16) R tile[ContigIo<R>::kStageElems];
     if constexpr (!PERSIST) {
         solve_item<R, P, CYC>(data, items[blockIdx.x], tile, tables, fac, off, refine, sel);
     } else {

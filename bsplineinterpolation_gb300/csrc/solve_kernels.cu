@@ -62,7 +62,7 @@ constexpr int warm_rows() {
 // lines (adjacent t), so every chunk load and store of a warp is a run of
 // contiguous elements. No shared memory: occupancy is set by registers only.
 template <class R, int P, int Q, bool CYC>
-__global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R* __restrict__ x, int64_t n,
+__global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_strided_kernel(R* __restrict__ x, int64_t n,
                                                                               int64_t S, int64_t nlines,
                                                                               FactorView<R> f) {
     for (int64_t l = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; l < nlines;
@@ -72,18 +72,20 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_warp_strided_kernel(R*
     }
 }
 
-// Contiguous axis (S = 1): one warp per 32 consecutive lines.
+// Contiguous axis (S = 1): one warp per 32 consecutive lines, each chunk's
+// rows copied into a shared-memory stage while the previous chunk is solved.
 template <class R, int P, int Q, bool CYC>
 __global__ void __launch_bounds__(kSolveWarps * 32, 4) solve_warp_contig_kernel(R* __restrict__ x, int64_t n,
                                                                              int64_t nlines, FactorView<R> f) {
-    __shared__ R stage[kSolveWarps][32 * 33];
+    using Io = WarpContigChunksPF<R, line_chunk<R>()>;
+    __shared__ __align__(16) R stage[kSolveWarps][Io::kStageElems];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t ngroups = (nlines + 31) / 32;
     for (int64_t g = blockIdx.x * static_cast<int64_t>(kSolveWarps) + warp; g < ngroups;
          g += static_cast<int64_t>(gridDim.x) * kSolveWarps) {
         const int64_t l0 = g * 32;
         const int rows = static_cast<int>(nlines - l0 < 32 ? nlines - l0 : 32);
-        WarpContigChunks<R> io{x + l0 * n, n, rows, stage[warp], lane};
+        Io io{x + l0 * n, n, rows, stage[warp], lane};
         solve_line_chunked<R, P, Q, CYC, line_chunk<R>()>(f, io);
     }
 }

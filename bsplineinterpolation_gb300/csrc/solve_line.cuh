@@ -42,12 +42,23 @@ __device__ __forceinline__ double fma_r(double a, double b, double c) { return _
 
 // Chunk accessors of one line: load(i0, cnt, buf) fills buf[0 .. cnt-1] with
 // elements i0 .. i0+cnt-1 of the line, store(i0, cnt, buf) writes them back.
+// An accessor with kPrefetch also moves chunks in two steps, so that the
+// next chunk's loads are in flight while the current one is computed:
+// fetch(i0, cnt, pend, slot) issues the loads, take(i0, cnt, pend, slot, buf)
+// completes them into buf, and store(i0, cnt, buf, slot) writes back a chunk
+// taken from `slot` (slots alternate between consecutive chunks).
 
 // Element k at base[k*S] (global memory; each lane its own line).
+// Prefetch: the next chunk's loads land in registers (Pending).
 template <class R>
 struct StridedChunks {
     R* base;
     int64_t S;
+    static constexpr bool kPrefetch = true;
+    template <int K>
+    struct Pending {
+        R v[K];
+    };
     template <int K>
     __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
 #pragma unroll
@@ -59,6 +70,20 @@ struct StridedChunks {
 #pragma unroll
         for (int k = 0; k < K; ++k)
             if (k < cnt) base[(i0 + k) * S] = buf[k];
+    }
+    template <int K>
+    __device__ __forceinline__ void fetch(int64_t i0, int cnt, Pending<K>& p, int) const {
+        load(i0, cnt, p.v);
+    }
+    template <int K>
+    __device__ __forceinline__ void take(int64_t, int cnt, Pending<K>& p, int, R (&buf)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = p.v[k];
+    }
+    template <int K>
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K], int) const {
+        store(i0, cnt, buf);
     }
 };
 
@@ -130,6 +155,72 @@ struct WarpContigChunks {
                 if (r < rows) x[r * n + i0 + lane] = stage[r * 33 + lane];
         }
     }
+};
+
+// One asynchronous global -> shared copy of BYTES (4 or 8) bytes.
+template <int BYTES>
+__device__ __forceinline__ void line_cp_async(void* dst_smem, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem))),
+                 "l"(src), "n"(BYTES)
+                 : "memory");
+}
+
+// WarpContigChunks with prefetch: two per-warp stages of [32][K+1] elements
+// (`stage` holds both, 2 * 32 * (K+1)); a chunk's rows move into its slot's
+// stage by cp.async (8- or 4-byte copies, lane j taking element i0 + j of
+// every line), so they are in flight while the previous chunk is computed.
+// The arithmetic is that of WarpContigChunks: only the data movement
+// differs. Warp-collective, like WarpContigChunks.
+template <class R, int K>
+struct WarpContigChunksPF {
+    R* x;
+    int64_t n;
+    int rows;
+    R* stage;
+    int lane;
+    static constexpr bool kPrefetch = true;
+    static constexpr int kPitch = K + 1;
+    static constexpr int kStageElems = 2 * 32 * kPitch;
+    template <int KK>
+    struct Pending {};
+    __device__ __forceinline__ R* slot_stage(int slot) const { return stage + slot * 32 * kPitch; }
+    __device__ __forceinline__ void fetch(int64_t i0, int cnt, Pending<K>&, int slot) const {
+        static_assert(sizeof(R) == 4 || sizeof(R) == 8, "4- or 8-byte elements");
+        __syncwarp();  // the slot's previous chunk has been read out by every lane
+        R* st = slot_stage(slot);
+        if (lane < cnt) {
+            const R* src = x + i0 + lane;
+            for (int r = 0; r < rows; ++r) line_cp_async<sizeof(R)>(st + r * kPitch + lane, src + r * n);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    __device__ __forceinline__ void take(int64_t, int cnt, Pending<K>&, int slot, R (&buf)[K]) const {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncwarp();
+        const R* st = slot_stage(slot);
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) buf[k] = st[lane * kPitch + k];
+    }
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K], int slot) const {
+        R* st = slot_stage(slot);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < cnt) st[lane * kPitch + k] = buf[k];
+        __syncwarp();
+        if (lane < cnt) {
+            for (int r = 0; r < rows; ++r) x[r * n + i0 + lane] = st[r * kPitch + lane];
+        }
+    }
+    // one-off chunks (the cyclic corner rows), through slot 0
+    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
+        Pending<K> p;
+        fetch(i0, cnt, p, 0);
+        take(i0, cnt, p, 0, buf);
+    }
+    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const { store(i0, cnt, buf, 0); }
 };
 
 // WarpContigChunks for FP32 lines whose length is a multiple of 4 (every line
@@ -225,6 +316,11 @@ struct WarpContigChunksV4 {
 // chi) from registers. It pays where one lane walks a long line alone (the
 // factor loads of each chunk would wait on L2); where a warp's lanes share
 // the factor row, the loads are broadcasts and the registers cost occupancy.
+template <class Io, class = void>
+struct chunks_prefetch : std::false_type {};
+template <class Io>
+struct chunks_prefetch<Io, std::void_t<decltype(Io::kPrefetch)>> : std::integral_constant<bool, Io::kPrefetch> {};
+
 template <class R, int P, int Q, bool CYC, int K, class Io, bool CONST_ROWS = false>
 __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const Io& io) {
     const int64_t n = f.n;
@@ -278,19 +374,38 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
             }
         }
     };
-    for (int64_t i0 = 0; i0 < n; i0 += K) {
-        const int cnt = static_cast<int>(n - i0 < K ? n - i0 : K);
-        R buf[K];
-        io.load(i0, cnt, buf);
-        if constexpr (CONST_ROWS) {
-            if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
-                forward(std::true_type{}, i0, cnt, buf);
-                io.store(i0, cnt, buf);
-                continue;
-            }
+    if constexpr (chunks_prefetch<Io>::value && !CONST_ROWS) {
+        // the next chunk's loads are issued before this chunk is computed
+        typename Io::template Pending<K> pend;
+        int slot = 0;
+        int cnt = static_cast<int>(n < K ? n : K);
+        if (n > 0) io.fetch(0, cnt, pend, slot);
+        for (int64_t i0 = 0; i0 < n; i0 += K) {
+            R buf[K];
+            io.take(i0, cnt, pend, slot, buf);
+            const int64_t j0 = i0 + K;
+            const int ncnt = static_cast<int>(j0 < n ? (n - j0 < K ? n - j0 : K) : 0);
+            if (ncnt > 0) io.fetch(j0, ncnt, pend, slot ^ 1);
+            forward(std::false_type{}, i0, cnt, buf);
+            io.store(i0, cnt, buf, slot);
+            slot ^= 1;
+            cnt = ncnt;
         }
-        forward(std::false_type{}, i0, cnt, buf);
-        io.store(i0, cnt, buf);
+    } else {
+        for (int64_t i0 = 0; i0 < n; i0 += K) {
+            const int cnt = static_cast<int>(n - i0 < K ? n - i0 : K);
+            R buf[K];
+            io.load(i0, cnt, buf);
+            if constexpr (CONST_ROWS) {
+                if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
+                    forward(std::true_type{}, i0, cnt, buf);
+                    io.store(i0, cnt, buf);
+                    continue;
+                }
+            }
+            forward(std::false_type{}, i0, cnt, buf);
+            io.store(i0, cnt, buf);
+        }
     }
     // ---- back: x = U^{-1} y ----
     R zw[Q > 0 ? Q : 1];  // z_{i+1} .. z_{i+Q}
@@ -327,20 +442,41 @@ __device__ __forceinline__ void solve_line_chunked(const FactorView<R>& f, const
             }
         }
     };
-    for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
-        const int cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
-        const int64_t i0 = i1 - cnt + 1;
-        R buf[K];
-        io.load(i0, cnt, buf);
-        if constexpr (CONST_ROWS) {
-            if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
-                back(std::true_type{}, i0, cnt, buf);
-                io.store(i0, cnt, buf);
-                continue;
-            }
+    if constexpr (chunks_prefetch<Io>::value && !CONST_ROWS) {
+        // the forward sweep's stores (other lanes' too) before the first
+        // asynchronous read of this sweep
+        __threadfence_block();
+        typename Io::template Pending<K> pend;
+        int slot = 0;
+        int cnt = static_cast<int>(n < K ? n : K);
+        if (n > 0) io.fetch(n - cnt, cnt, pend, slot);
+        for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
+            const int64_t i0 = i1 - cnt + 1;
+            R buf[K];
+            io.take(i0, cnt, pend, slot, buf);
+            const int ncnt = static_cast<int>(i0 < K ? i0 : K);
+            if (ncnt > 0) io.fetch(i0 - ncnt, ncnt, pend, slot ^ 1);
+            back(std::false_type{}, i0, cnt, buf);
+            io.store(i0, cnt, buf, slot);
+            slot ^= 1;
+            cnt = ncnt;
         }
-        back(std::false_type{}, i0, cnt, buf);
-        io.store(i0, cnt, buf);
+    } else {
+        for (int64_t i1 = n - 1; i1 >= 0; i1 -= K) {
+            const int cnt = static_cast<int>(i1 + 1 < K ? i1 + 1 : K);
+            const int64_t i0 = i1 - cnt + 1;
+            R buf[K];
+            io.load(i0, cnt, buf);
+            if constexpr (CONST_ROWS) {
+                if (has_const && i0 >= f.clo && i0 + cnt <= f.chi) {
+                    back(std::true_type{}, i0, cnt, buf);
+                    io.store(i0, cnt, buf);
+                    continue;
+                }
+            }
+            back(std::false_type{}, i0, cnt, buf);
+            io.store(i0, cnt, buf);
+        }
     }
 }
 
