@@ -87,76 +87,6 @@ struct StridedChunks {
     }
 };
 
-// A line held contiguously (in shared memory).
-template <class R>
-struct SmemChunks {
-    R* base;
-    template <int K>
-    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) buf[k] = base[i0 + k];
-    }
-    template <int K>
-    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) base[i0 + k] = buf[k];
-    }
-};
-
-// 32 consecutive contiguous lines, lane l owning line l0 + l (x = line l0's
-// first element, `rows` lines present), each chunk moved through a per-warp
-// [32][33] shared-memory transpose: the global accesses are runs of one
-// line's elements (lane j touches element i0 + j of every line, all 32
-// loads in flight), and lane l reading element k of its line touches bank
-// (l + k) mod 32. Chunks are at most 32 elements. Warp-collective: every
-// lane calls with the same chunk; lanes past `rows` compute on stale values
-// that are never written back.
-template <class R>
-struct WarpContigChunks {
-    R* x;
-    int64_t n;
-    int rows;
-    R* stage;
-    int lane;
-    template <int K>
-    __device__ __forceinline__ void load(int64_t i0, int cnt, R (&buf)[K]) const {
-        static_assert(K <= 32, "chunks of at most 32 elements");
-        __syncwarp();
-        if (lane < cnt) {
-            // rows in groups (32 FP32 / 16 FP64 loads in flight per lane)
-            constexpr int G = sizeof(R) == 4 ? 32 : 16;
-#pragma unroll
-            for (int g = 0; g < 32; g += G) {
-                R v[G];
-#pragma unroll
-                for (int r = 0; r < G; ++r)
-                    if (g + r < rows) v[r] = x[(g + r) * n + i0 + lane];
-#pragma unroll
-                for (int r = 0; r < G; ++r) stage[(g + r) * 33 + lane] = v[r];
-            }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) buf[k] = stage[lane * 33 + k];
-    }
-    template <int K>
-    __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const {
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (k < cnt) stage[lane * 33 + k] = buf[k];
-        __syncwarp();
-        if (lane < cnt) {
-#pragma unroll
-            for (int r = 0; r < 32; ++r)
-                if (r < rows) x[r * n + i0 + lane] = stage[r * 33 + lane];
-        }
-    }
-};
-
 // One asynchronous global -> shared copy of BYTES (4 or 8) bytes.
 template <int BYTES>
 __device__ __forceinline__ void line_cp_async(void* dst_smem, const void* src) {
@@ -166,12 +96,16 @@ __device__ __forceinline__ void line_cp_async(void* dst_smem, const void* src) {
                  : "memory");
 }
 
-// WarpContigChunks with prefetch: two per-warp stages of [32][K+1] elements
-// (`stage` holds both, 2 * 32 * (K+1)); a chunk's rows move into its slot's
-// stage by cp.async (8- or 4-byte copies, lane j taking element i0 + j of
-// every line), so they are in flight while the previous chunk is computed.
-// The arithmetic is that of WarpContigChunks: only the data movement
-// differs. Warp-collective, like WarpContigChunks.
+// 32 consecutive contiguous lines, lane l owning line l0 + l (x = line l0's
+// first element, `rows` lines present), each chunk moved through a per-warp
+// shared-memory stage of [32][K+1] elements: the global accesses are runs of
+// one line's elements (lane j touches element i0 + j of every line), and
+// lane l reading element k of its line touches word l * (K+1) + k, distinct
+// banks across the warp. Two stages (`stage` holds both, 2 * 32 * (K+1))
+// alternate between consecutive chunks: a chunk's rows move into its slot's
+// stage by cp.async (8- or 4-byte copies), in flight while the previous
+// chunk is computed. Warp-collective: every lane calls with the same chunk;
+// lanes past `rows` compute on stale values that are never written back.
 template <class R, int K>
 struct WarpContigChunksPF {
     R* x;
@@ -223,14 +157,14 @@ struct WarpContigChunksPF {
     __device__ __forceinline__ void store(int64_t i0, int cnt, const R (&buf)[K]) const { store(i0, cnt, buf, 0); }
 };
 
-// WarpContigChunks for FP32 lines whose length is a multiple of 4 (every line
+// Contiguous FP32 lines whose length is a multiple of 4 (every line
 // starts 16-byte aligned): chunks of 16 elements move as float4 vectors
 // through a per-warp [32][20] stage. Lane l = 4 * row_sub + q loads column
 // group q (elements 4q .. 4q+3 of the chunk) of rows row_sub, +8, +16, +24;
 // lane l then reads its own row as four float4 (16-byte units 5l + j: the
 // eight lanes of a phase hit distinct bank groups). A chunk that does not
 // start on a multiple of 4 (the cyclic corner read) takes per-element
-// copies. Only data moves: results equal those of WarpContigChunks.
+// copies. Only data moves: results equal those of WarpContigChunksPF.
 struct WarpContigChunksV4 {
     float* x;  // first element of line l0
     int64_t n;
