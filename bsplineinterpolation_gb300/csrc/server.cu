@@ -104,6 +104,7 @@ struct Request {
     // result
     Clock::time_point t_submit;
     Clock::time_point t_admit;  // its first work unit was issued
+    double device_ms = 0.0;     // tracing: device time of its work units (sum)
     bool admitted_once = false;
     intp_status status = INTP_OK;
     std::string error;
@@ -138,6 +139,7 @@ struct Unit {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr;  // tracing: recorded when a unit is issued (timing events)
     bool busy = false;
     bool small_only = false;  // reserved for small requests (high-priority stream)
     Unit unit;
@@ -195,9 +197,13 @@ struct intp_server {
     // statistics since the last reset
     std::vector<double> lat_build, lat_eval;
     // request trace (INTP_GB300_SERVER_TRACE=<file>): one line per completed
-    // request, written when the server is destroyed
+    // request, written when the server is destroyed; its device_ms column
+    // sums the device time of the request's work units
     std::string trace_path;
     std::vector<std::string> trace;
+    // tracing: worker-loop iterations that began more than 5 ms after the
+    // previous one (start ms, gap ms), written to <trace file>.gaps
+    std::vector<std::pair<double, double>> loop_gaps;
     double points = 0;
     int64_t failed = 0, evictions = 0, merged_units = 0;
     Clock::time_point t_reset = Clock::now(), t_last = Clock::now();
@@ -224,9 +230,9 @@ void intp_server::complete(Request* r, intp_status st, const std::string& msg, C
     if (!trace_path.empty()) {
         char line[256];
         const Clock::time_point ta = r->admitted_once ? r->t_admit : now;
-        std::snprintf(line, sizeof line, "%lld,%d,%lld,%.3f,%.3f,%.3f,%d\n", static_cast<long long>(r->id),
+        std::snprintf(line, sizeof line, "%lld,%d,%lld,%.3f,%.3f,%.3f,%.3f,%d\n", static_cast<long long>(r->id),
                       r->build ? 1 : 0, static_cast<long long>(r->build ? build_values(r->desc) : r->npts),
-                      ms_since(t_reset, r->t_submit), ms_since(r->t_submit, ta), ms_since(ta, now),
+                      ms_since(t_reset, r->t_submit), ms_since(r->t_submit, ta), ms_since(ta, now), r->device_ms,
                       static_cast<int>(st));
         trace.emplace_back(line);
     }
@@ -289,6 +295,11 @@ void intp_server::finish_slot(Slot& s, cudaError_t e) {
     const Clock::time_point now = Clock::now();
     Unit& u = s.unit;
     inflight_bytes -= u.reserve;
+    if (s.start && e == cudaSuccess) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, s.start, s.done) == cudaSuccess)
+            for (const Part& pt : u.parts) pt.r->device_ms += ms;
+    }
     if (u.build) {
         Request* r = u.parts[0].r;
         Table& tb = tables[u.table];
@@ -355,6 +366,7 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
             u.table = r->table;
             u.reserve = need;
             intp_table* t = nullptr;
+            if (s.start) cudaEventRecord(s.start, s.stream);
             intp_status st = create_table(&r->desc, true, s.stream, &t);
             if (st == INTP_OK) {
                 tables[r->table].t = t;
@@ -432,6 +444,7 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
         }
         const int D = tb.dim;
         cudaStream_t st = s.stream;
+        if (s.start) cudaEventRecord(s.start, st);
         double* dc = nullptr;
         void* dout = nullptr;
         cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dc), static_cast<size_t>(u.npts) * D * 8 + 16, st);
@@ -500,7 +513,14 @@ bool intp_server::admit(Slot& s, std::unique_lock<std::mutex>& lock) {
 void intp_server::run() {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lock(mu);
+    Clock::time_point t_prev = Clock::now();
     for (;;) {
+        if (!trace_path.empty()) {
+            const Clock::time_point t_it = Clock::now();
+            const double gap = ms_since(t_prev, t_it);
+            if (gap > 5.0) loop_gaps.emplace_back(ms_since(t_reset, t_it), gap);
+            t_prev = t_it;
+        }
         bool any_busy = false;
         for (Slot& s : slots) {
             if (!s.busy) continue;
@@ -553,13 +573,19 @@ intp_server::~intp_server() {
     for (Slot& s : slots) {
         if (s.stream) cudaStreamSynchronize(s.stream);
         if (s.done) cudaEventDestroy(s.done);
+        if (s.start) cudaEventDestroy(s.start);
         if (s.stream) cudaStreamDestroy(s.stream);
     }
     for (auto& kv : requests) delete kv.second;  // includes any never waited on
     if (!trace_path.empty()) {
         if (FILE* f = std::fopen(trace_path.c_str(), "w")) {
-            std::fputs("id,build,size,submit_ms,queue_ms,service_ms,status\n", f);
+            std::fputs("id,build,size,submit_ms,queue_ms,service_ms,device_ms,status\n", f);
             for (const std::string& l : trace) std::fputs(l.c_str(), f);
+            std::fclose(f);
+        }
+        if (FILE* f = std::fopen((trace_path + ".gaps").c_str(), "w")) {
+            std::fputs("at_ms,gap_ms\n", f);
+            for (const auto& g : loop_gaps) std::fprintf(f, "%.3f,%.3f\n", g.first, g.second);
             std::fclose(f);
         }
     }
@@ -597,7 +623,10 @@ intp_status intp_server_create(const intp_server_config* cfg, intp_server** out)
         Slot& sl = s->slots[static_cast<size_t>(i)];
         sl.small_only = i < nsmall;
         cudaError_t e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.small_only ? greatest : least);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        // tracing times each unit on the device (timing events)
+        const unsigned ev_flags = s->trace_path.empty() ? cudaEventDisableTiming : cudaEventDefault;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, ev_flags);
+        if (e == cudaSuccess && !s->trace_path.empty()) e = cudaEventCreateWithFlags(&sl.start, cudaEventDefault);
         if (e != cudaSuccess) {
             delete s;
             return sfail(INTP_ERR_CUDA, std::string("server streams: ") + cudaGetErrorString(e));
