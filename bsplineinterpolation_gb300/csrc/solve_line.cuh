@@ -99,7 +99,8 @@ __device__ __forceinline__ void line_cp_async(void* dst_smem, const void* src) {
 // 32 consecutive contiguous lines, lane l owning line l0 + l (x = line l0's
 // first element, `rows` lines present), each chunk moved through a per-warp
 // shared-memory stage of [32][K+1] elements: the global accesses are runs of
-// one line's elements (lane j touches element i0 + j of every line), and
+// K elements of 32 / K lines per instruction (lane j touches element
+// i0 + j % K of lines j / K, j / K + 32 / K, ...), and
 // lane l reading element k of its line touches word l * (K+1) + k, distinct
 // banks across the warp. Two stages (`stage` holds both, 2 * 32 * (K+1))
 // alternate between consecutive chunks: a chunk's rows move into its slot's
@@ -123,9 +124,12 @@ struct WarpContigChunksPF {
         static_assert(sizeof(R) == 4 || sizeof(R) == 8, "4- or 8-byte elements");
         __syncwarp();  // the slot's previous chunk has been read out by every lane
         R* st = slot_stage(slot);
-        if (lane < cnt) {
-            const R* src = x + i0 + lane;
-            for (int r = 0; r < rows; ++r) line_cp_async<sizeof(R)>(st + r * kPitch + lane, src + r * n);
+        // all lanes copy: lane l takes element l % K of rows l / K, + 32 / K, ...
+        static_assert(32 % K == 0, "chunks of a power-of-two length up to 32");
+        const int e = lane % K;
+        if (e < cnt) {
+            const R* src = x + i0 + e;
+            for (int r = lane / K; r < rows; r += 32 / K) line_cp_async<sizeof(R)>(st + r * kPitch + e, src + r * n);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
@@ -144,8 +148,9 @@ struct WarpContigChunksPF {
         for (int k = 0; k < K; ++k)
             if (k < cnt) st[lane * kPitch + k] = buf[k];
         __syncwarp();
-        if (lane < cnt) {
-            for (int r = 0; r < rows; ++r) x[r * n + i0 + lane] = st[r * kPitch + lane];
+        const int e = lane % K;
+        if (e < cnt) {
+            for (int r = lane / K; r < rows; r += 32 / K) x[r * n + i0 + e] = st[r * kPitch + e];
         }
     }
     // one-off chunks (the cyclic corner rows), through slot 0
