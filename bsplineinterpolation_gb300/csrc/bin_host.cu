@@ -298,7 +298,7 @@ cudaError_t run_binned_eval(const TableDev& t, const BinGeom& g, const CUtensorM
     uint32_t* tile_sum = reinterpret_cast<uint32_t*>(p);
     p += b_t;
     uint32_t* rec = reinterpret_cast<uint32_t*>(p);
-    const int K = plan.k;
+    const int K = plan.k * (t.channels > 1 ? t.channels : 1);  // output values per query
     const size_t ob = out_f32 ? 4 : 8;
     const int grid_eval = sm_count();  // the launchers fill each SM
     for (int64_t p0 = 0; p0 < npts && e == cudaSuccess; p0 += cap) {

@@ -390,7 +390,7 @@ template <int D, int O, bool LEAN, class TS>
 __device__ __forceinline__ void eval_record(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
                                             const float* tile, const int (&org)[D], float cbase,
                                             const uint32_t (&w)[rec_words<D>()], uint32_t cell,
-                                            void* __restrict__ out, int out_f32) {
+                                            void* __restrict__ out, int out_f32, int C, int ch) {
     constexpr int RW = rec_words<D>();
     constexpr int W = O + 1;
     const int K = plan.k;
@@ -409,19 +409,20 @@ __device__ __forceinline__ void eval_record(const TableDev& t, const BinGeom& g,
     for (int d = 0; d < D; ++d) tref += ref_tap<O>() * TS::S(d);
     const float cref = tl[tref];
     const int64_t o0 = idx * K;
-    // value and one derivative (the common request) leave as one 8-byte store
+    // value and one derivative (the common request) leave as one 8-byte store;
+    // output k of channel ch of a vector-valued table goes to (o0 + k) * C + ch
     float first = 0.0f;
-    const bool pair = out_f32 == 3 && K == 2;
-    auto emit = [out, out_f32, o0, pair, &first](int k, float v) {
+    const bool pair = out_f32 == 3 && K == 2 && C == 1;
+    auto emit = [out, out_f32, o0, pair, C, ch, &first](int k, float v) {
         if (pair) {
             if (k == 0)
                 first = v;
             else
                 reinterpret_cast<float2*>(static_cast<float*>(out) + o0)[0] = make_float2(first, v);
         } else if (out_f32) {
-            static_cast<float*>(out)[o0 + k] = v;
+            static_cast<float*>(out)[(o0 + k) * C + ch] = v;
         } else {
-            static_cast<double*>(out)[o0 + k] = static_cast<double>(v);
+            static_cast<double*>(out)[(o0 + k) * C + ch] = static_cast<double>(v);
         }
     };
     if constexpr (LEAN) {
@@ -462,7 +463,7 @@ template <int D, int O, bool LEAN, class TS>
 __device__ __forceinline__ void eval_sorted(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
                                             const float* tile, const int (&org)[D], float cbase,
                                             const uint32_t* sbuf, const uint16_t* cellof, int n,
-                                            void* __restrict__ out, int out_f32) {
+                                            void* __restrict__ out, int out_f32, int C, int ch) {
     constexpr int RW = rec_words<D>();
     for (int q = threadIdx.x; q < n; q += kBinThreads) {
         uint32_t w[RW];
@@ -477,7 +478,7 @@ __device__ __forceinline__ void eval_sorted(const TableDev& t, const BinGeom& g,
             w[2] = v.z;
             w[3] = v.w;
         }
-        eval_record<D, O, LEAN, TS>(t, g, plan, tile, org, cbase, w, cellof[q], out, out_f32);
+        eval_record<D, O, LEAN, TS>(t, g, plan, tile, org, cbase, w, cellof[q], out, out_f32, C, ch);
     }
 }
 
@@ -488,8 +489,8 @@ template <int D, int O, class TS>
 __device__ __noinline__ void eval_sorted_general(const TableDev& t, const BinGeom& g, const DerivPlan& plan,
                                                  const float* tile, const int (&org)[D], float cbase,
                                                  const uint32_t* sbuf, const uint16_t* cellof, int n,
-                                                 void* __restrict__ out, int out_f32) {
-    eval_sorted<D, O, false, TS>(t, g, plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
+                                                 void* __restrict__ out, int out_f32, int C, int ch) {
+    eval_sorted<D, O, false, TS>(t, g, plan, tile, org, cbase, sbuf, cellof, n, out, out_f32, C, ch);
 }
 
 // Evaluation CTA. CTA j takes the j-th equal slice of the records in bucket
@@ -530,6 +531,7 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
     __shared__ uint32_t sh_seg[kMaxSortBlocks];                    // the bucket's per-sort-CTA first slots
     __shared__ uint32_t sh_warp[kBinThreads / 32];
     const float* __restrict__ cp = static_cast<const float*>(t.ctrl);
+    const int C = t.channels > 1 ? t.channels : 1;
     const int64_t r0 = nrec * blockIdx.x / gridDim.x, r1 = nrec * (blockIdx.x + 1) / gridDim.x;
     if (r0 >= r1) return;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -570,6 +572,12 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
                 rem /= g.nb[d];
             }
         }
+        // vector-valued tables: the bucket's records once per channel, each
+        // channel's tile staged by element copies (the TMA maps cover one
+        // channel)
+        for (int ch = 0; ch < C; ++ch) {
+        const float* __restrict__ cpc = cp + ch * t.chan_stride;
+        const float* __restrict__ clc = cl ? cl + ch * t.chan_stride : nullptr;
         __syncthreads();
         for (int j = tid; j < nblk; j += kBinThreads) sh_seg[j] = __ldg(blkoffset + b * nblk + j);
         if (tid == 0 && cl) {
@@ -580,10 +588,10 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 off += static_cast<int64_t>(tile_index(t.ax[d], org[d] + TS::P(d) / 2)) * t.ax[d].stride;
-            sh_cbase = __ldg(cp + off);
+            sh_cbase = __ldg(cpc + off);
         }
         // one TMA box unless the tile wraps around a periodic axis
-        bool tma = use_tma != 0;
+        bool tma = use_tma != 0 && C == 1;
 #pragma unroll
         for (int d = 0; d < D; ++d)
             if (t.ax[d].periodic && org[d] + TS::P(d) > t.ax[d].n) tma = false;
@@ -631,8 +639,8 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
                     rem /= TS::P(d);
                     off += sh_outer[d][i];
                 }
-                cp_async<4>(tile + e, cp + off);
-                if (cl) cp_async<4>(tile_lo + e, cl + off);
+                cp_async<4>(tile + e, cpc + off);
+                if (cl) cp_async<4>(tile_lo + e, clc + off);
             }
             cp_async_wait_all();
         }
@@ -720,11 +728,13 @@ __global__ void __launch_bounds__(kBinThreads, 3) eval_kernel(TableDev t, BinGeo
             }
             __syncthreads();
             if (sh_plan.simple)
-                eval_sorted<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
+                eval_sorted<D, O, true, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32, C, ch);
             else
-                eval_sorted_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32);
+                eval_sorted_general<D, O, TS>(sh_t, g, sh_plan, tile, org, cbase, sbuf, cellof, n, out, out_f32, C,
+                                              ch);
             __syncthreads();
         }
+        }  // channel
         r = end;
     }
 }

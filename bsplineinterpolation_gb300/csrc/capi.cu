@@ -275,11 +275,11 @@ intp_status upload_table(intp_table* t) {
     }
     t->dev.channels = t->channels;
     t->dev.chan_stride = m.total;
-    // the binned path stages one channel's tiles: vector-valued tables
-    // evaluate with the direct kernel
-    if (t->mixed() && m.dim <= 3 && t->channels == 1) {
+    // binned evaluation: a vector-valued table's channels are staged one
+    // after another by element copies (the TMA maps cover one channel)
+    if (t->mixed() && m.dim <= 3) {
         t->bins = make_bin_geom(t->dev);
-        if (t->bins.smem_buckets > 0)
+        if (t->bins.smem_buckets > 0 && t->channels == 1)
             t->has_tile_map = make_tile_map(t, t->ctrl, &t->tile_map[0]) &&
                               (!t->ctrl_lo || make_tile_map(t, t->ctrl_lo, &t->tile_map[1]));
     }

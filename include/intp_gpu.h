@@ -68,9 +68,9 @@ typedef struct intp_table_desc {
      * type T, Interpolation.hpp:17-507). Values and control points are then
      * prod(size) x C, channel fastest, and every evaluation output is C
      * values. All channels share the knots, the factors and, per query, the
-     * basis weights. Single tables, batches and the serving loop take them;
-     * they evaluate with the direct kernel (the binned path stages one
-     * channel's tiles). */
+     * basis weights. Single tables (direct and binned evaluation), batches
+     * and the serving loop take them; intp_eval_noalloc evaluates them with
+     * the direct kernel. */
     int32_t channels;
     int32_t reserved_;
 } intp_table_desc;
