@@ -701,6 +701,18 @@ def run_batched(args, torch, steps=5, warmup=3):
     build_ms = float(np.median([a.elapsed_time(c) for a, c, _ in ev]))
     eval_ms = float(np.median([c.elapsed_time(d) for _, c, d in ev]))
     total_ms = ev[0][0].elapsed_time(ev[-1][2]) / steps
+    # the same step replayed from a captured CUDA graph (intp_batch_graph_*)
+    g = b.graph(vals, coords, offsets, out=out)
+    for _ in range(warmup):
+        g.launch(torch.cuda.current_stream())
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(steps):
+        g.launch(torch.cuda.current_stream())
+    g1.record()
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / steps
+    g.close()
     # accuracy of a sample of tables against the FP64 form of the same batch
     b64 = bi.TableBatch(specs, precision="fp64")
     b64.build(vals)
@@ -709,6 +721,7 @@ def run_batched(args, torch, steps=5, warmup=3):
     return {"workload": "%d tables (half 1D N~U[16,4096], half 2D sides~U[16,256]; O in {3,5}; 30%% periodic),"
                         " %d queries" % (len(specs), npts),
             "points_per_s": npts / (total_ms / 1e3), "build_ms": build_ms, "eval_ms": eval_ms,
+            "graph_ms": graph_ms, "graph_points_per_s": npts / (graph_ms / 1e3),
             "eval_points_per_s": npts / (eval_ms / 1e3), "mesh_values": int(values.size),
             "max_rel_err_vs_fp64": err, "steps": steps, "warmup": warmup, "schedule": schedule}
 

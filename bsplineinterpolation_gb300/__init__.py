@@ -662,6 +662,43 @@ class TableBatch:
                                        C.c_void_p(out.data_ptr()), od, _stream_ptr(stream)))
         return out
 
+    def graph(self, values, coords, point_offsets, derivs=None, out=None, out_dtype=None):
+        """A CUDA graph of one build from `values` and one evaluation of
+        `coords` into `out` (CUDA tensors; intp_batch_graph_create). Returns a
+        BatchGraph whose launch() replays both, reading the tensors' contents
+        at each launch; `out` (allocated here when None) is its `out`."""
+        torch = _torch()
+        lib = _lib.load()
+        po = np.ascontiguousarray(np.asarray(point_offsets, np.int64))
+        if po.size != self.ntables + 1:
+            raise ValueError("point_offsets needs ntables + 1 entries")
+        if not (_is_cuda_tensor(values) and _is_cuda_tensor(coords)):
+            raise ValueError("graph buffers are CUDA tensors")
+        if values.dtype != torch.float64 or not values.is_contiguous() or values.numel() != int(self.offsets[-1]):
+            raise ValueError("values: %d contiguous float64 values" % int(self.offsets[-1]))
+        if coords.dtype != torch.float64 or not coords.is_contiguous():
+            raise ValueError("coords: contiguous float64")
+        if out_dtype is None:
+            out_dtype = "f32" if self.precision == "mixed" else "f64"
+        od = _lib.F32 if out_dtype == "f32" else _lib.F64
+        if derivs is None:
+            kp, K, karr = None, 1, None
+        else:
+            d = np.asarray(derivs, np.int32)
+            d = d.reshape(-1, d.shape[-1])
+            karr = np.zeros((d.shape[0], _lib.MAX_DIM), np.int32)
+            karr[:, :d.shape[1]] = d
+            K = karr.shape[0]
+            kp = karr.ctypes.data
+        if out is None:
+            dt = torch.float32 if od == _lib.F32 else torch.float64
+            n = np.diff(po)
+            out = torch.empty(int(np.sum(n * K * np.asarray(self.channels))), dtype=dt, device=coords.device)
+        h = C.c_void_p()
+        _lib.check(lib.intp_batch_graph_create(self._h, C.c_void_p(values.data_ptr()), C.c_void_p(coords.data_ptr()),
+                                               po.ctypes.data, kp, K, C.c_void_p(out.data_ptr()), od, C.byref(h)))
+        return BatchGraph(h, self, (values, coords, out))
+
     def output_views(self, out, point_offsets, K=1):
         """Table i's outputs as a (points x K) view, or (points x K x C) for a
         vector-valued table, of an `evaluate` result."""
@@ -674,6 +711,29 @@ class TableBatch:
             views.append(v.reshape(n, K) if c == 1 else v.reshape(n, K, c))
             e += n * K * c
         return views
+
+
+class BatchGraph:
+    """A captured build + evaluation of a TableBatch (TableBatch.graph)."""
+
+    def __init__(self, handle, batch, buffers):
+        self._h = handle
+        self._batch = batch  # the graph holds the batch's pointers
+        self._buffers = buffers
+        self.out = buffers[2]
+
+    def launch(self, stream=None):
+        _lib.check(_lib.load().intp_batch_graph_launch(self._h, _stream_ptr(stream)))
+        return self.out
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().intp_batch_graph_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 class Server:

@@ -129,6 +129,9 @@ SIGNATURES = {
     "intp_batch_get_schedule": (C.c_int, [_P, C.POINTER(BatchSchedule)]),
     "intp_batch_autotune": (C.c_int, [_P, _P, C.c_int32, _P, C.POINTER(BatchSchedule)]),
     "intp_batch_eval": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_batch_graph_create": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, _P, C.c_int32, _P]),
+    "intp_batch_graph_launch": (C.c_int, [_P, _P]),
+    "intp_batch_graph_destroy": (C.c_int, [_P]),
     "intp_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "intp_server_destroy": (C.c_int, [_P]),
     "intp_server_submit_build": (C.c_int, [_P, C.POINTER(TableDesc), _P, C.POINTER(C.c_int64),

@@ -450,6 +450,73 @@ intp_status batch_interpolate(intp_batch* b, const double* values, cudaStream_t 
     return INTP_OK;
 }
 
+// The evaluation's work list: runs of at most kEvalRun points of one table,
+// grouped by (dimension, order) class, with each class's plan.
+struct EvalWork {
+    std::vector<EvalItem> items;  // classes one after another
+    struct Class {
+        int D, O;
+        size_t pos, count;
+        DerivPlan plan;
+    };
+    std::vector<Class> classes;
+    int64_t npts = 0;
+    bool out_f32 = true;
+};
+
+intp_status make_eval_work(const intp_batch* b, const int64_t* point_offsets, const int32_t* derivs, int32_t nderiv,
+                           int32_t out_dtype, EvalWork& w) {
+    if (out_dtype != INTP_F64 && out_dtype != INTP_F32) return bfail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
+    if (point_offsets[0] != 0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets[0] must be 0");
+    if (derivs && (nderiv < 1 || nderiv > INTP_GPU_MAX_DERIV))
+        return bfail(INTP_ERR_INVALID_ARGUMENT, "nderiv must be in [1, 16]");
+    w.out_f32 = out_dtype == INTP_F32;
+    // runs of queries per (dim, order) class; table i's outputs follow those
+    // of the tables before it, (points x K x channels) each
+    std::vector<EvalItem> items[kBatchMaxDim + 1][INTP_GPU_MAX_ORDER + 1];
+    const int64_t K = derivs ? nderiv : 1;
+    int64_t coff = 0, ooff = 0;
+    for (int64_t i = 0; i < b->ntables; ++i) {
+        const int64_t p0 = point_offsets[i], p1 = point_offsets[i + 1];
+        if (p1 < p0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets must not decrease");
+        const TableModel& m = b->models[i];
+        for (int64_t p = p0; p < p1; p += kEvalRun) {
+            EvalItem it{};
+            it.table = static_cast<int32_t>(i);
+            it.count = static_cast<int32_t>(std::min<int64_t>(kEvalRun, p1 - p));
+            it.coord_off = coff + (p - p0) * m.dim;
+            it.out_elem = ooff + (p - p0) * K * b->channels[i];
+            items[m.dim][m.order].push_back(it);
+        }
+        coff += (p1 - p0) * m.dim;
+        ooff += (p1 - p0) * K * b->channels[i];
+    }
+    w.npts = point_offsets[b->ntables];
+    for (int D = 1; D <= kBatchMaxDim; ++D)
+        for (int O = 0; O <= INTP_GPU_MAX_ORDER; ++O) {
+            const std::vector<EvalItem>& v = items[D][O];
+            if (v.empty()) continue;
+            EvalWork::Class c{D, O, w.items.size(), v.size(), DerivPlan{}};
+            std::string err;
+            if (!build_deriv_plan(D, O, derivs, nderiv, INTP_GPU_MAX_DIM, c.plan, err))
+                return bfail(INTP_ERR_INVALID_ARGUMENT, err);
+            w.items.insert(w.items.end(), v.begin(), v.end());
+            w.classes.push_back(c);
+        }
+    return INTP_OK;
+}
+
+// One launch per class of the work list (d_items: its device copy).
+intp_status launch_eval_work(const intp_batch* b, const EvalWork& w, const EvalItem* d_items, const double* coords,
+                             void* out, cudaStream_t s) {
+    for (const EvalWork::Class& c : w.classes) {
+        const cudaError_t e = launch_batch_eval(c.D, c.O, b->mixed(), b->d_tables, d_items + c.pos,
+                                                static_cast<int64_t>(c.count), coords, c.plan, out, w.out_f32, s);
+        if (e != cudaSuccess) return bcuda(e, "batched evaluation");
+    }
+    return INTP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -732,65 +799,92 @@ intp_status intp_batch_eval(const intp_batch* b, const double* coords, const int
                             const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype, void* stream) {
     if (!b || !point_offsets) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
     if (!b->has_ctrl) return bfail(INTP_ERR_STATE, "batch has no control points yet");
-    if (out_dtype != INTP_F64 && out_dtype != INTP_F32) return bfail(INTP_ERR_INVALID_ARGUMENT, "unknown output dtype");
-    if (point_offsets[0] != 0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets[0] must be 0");
-    if (derivs && (nderiv < 1 || nderiv > INTP_GPU_MAX_DERIV))
-        return bfail(INTP_ERR_INVALID_ARGUMENT, "nderiv must be in [1, 16]");
-    // runs of queries per (dim, order) class; table i's outputs follow those
-    // of the tables before it, (points x K x channels) each
-    std::vector<EvalItem> items[kBatchMaxDim + 1][INTP_GPU_MAX_ORDER + 1];
-    const int64_t K = derivs ? nderiv : 1;
-    int64_t coff = 0, ooff = 0;
-    for (int64_t i = 0; i < b->ntables; ++i) {
-        const int64_t p0 = point_offsets[i], p1 = point_offsets[i + 1];
-        if (p1 < p0) return bfail(INTP_ERR_INVALID_ARGUMENT, "point_offsets must not decrease");
-        const TableModel& m = b->models[i];
-        for (int64_t p = p0; p < p1; p += kEvalRun) {
-            EvalItem it{};
-            it.table = static_cast<int32_t>(i);
-            it.count = static_cast<int32_t>(std::min<int64_t>(kEvalRun, p1 - p));
-            it.coord_off = coff + (p - p0) * m.dim;
-            it.out_elem = ooff + (p - p0) * K * b->channels[i];
-            items[m.dim][m.order].push_back(it);
-        }
-        coff += (p1 - p0) * m.dim;
-        ooff += (p1 - p0) * K * b->channels[i];
-    }
-    const int64_t npts = point_offsets[b->ntables];
-    if (npts == 0) return INTP_OK;
+    EvalWork w;
+    intp_status st = make_eval_work(b, point_offsets, derivs, nderiv, out_dtype, w);
+    if (st != INTP_OK || w.npts == 0) return st;
     if (!coords || !out) return bfail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
-    size_t nitems = 0;
-    for (auto& row : items)
-        for (auto& v : row) nitems += v.size();
-    std::vector<EvalItem> flat;
-    flat.reserve(nitems);
-    for (auto& row : items)
-        for (auto& v : row) flat.insert(flat.end(), v.begin(), v.end());
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     EvalItem* d_items = nullptr;
-    BATCH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_items), flat.size() * sizeof(EvalItem), s),
+    BATCH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_items), w.items.size() * sizeof(EvalItem), s),
                "cudaMallocAsync(batch work list)");
-    cudaError_t e = cudaMemcpyAsync(d_items, flat.data(), flat.size() * sizeof(EvalItem), cudaMemcpyHostToDevice, s);
-    size_t pos = 0;
-    intp_status st = INTP_OK;
+    cudaError_t e = cudaMemcpyAsync(d_items, w.items.data(), w.items.size() * sizeof(EvalItem), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) st = bcuda(e, "cudaMemcpyAsync(batch work list)");
-    for (int D = 1; D <= kBatchMaxDim && st == INTP_OK; ++D)
-        for (int O = 0; O <= INTP_GPU_MAX_ORDER && st == INTP_OK; ++O) {
-            const std::vector<EvalItem>& v = items[D][O];
-            if (v.empty()) continue;
-            DerivPlan plan;
-            std::string err;
-            if (!build_deriv_plan(D, O, derivs, nderiv, INTP_GPU_MAX_DIM, plan, err)) {
-                st = bfail(INTP_ERR_INVALID_ARGUMENT, err);
-                break;
-            }
-            e = launch_batch_eval(D, O, b->mixed(), b->d_tables, d_items + pos, static_cast<int64_t>(v.size()), coords,
-                                  plan, out, out_dtype == INTP_F32, s);
-            if (e != cudaSuccess) st = bcuda(e, "batched evaluation");
-            pos += v.size();
-        }
+    if (st == INTP_OK) st = launch_eval_work(b, w, d_items, coords, out, s);
     cudaFreeAsync(d_items, s);
     return st;
+}
+
+// A captured build + evaluation: the evaluation's work list uploaded once,
+// then one intp_batch_build and one intp_batch_eval recorded on a capturing
+// stream (the build's side streams join the capture through its events).
+struct intp_batch_graph {
+    intp_batch* b = nullptr;
+    void* items = nullptr;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~intp_batch_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+        if (items) cudaFree(items);
+    }
+};
+
+intp_status intp_batch_graph_create(intp_batch* b, const double* values, const double* coords,
+                                    const int64_t* point_offsets, const int32_t* derivs, int32_t nderiv, void* out,
+                                    int32_t out_dtype, intp_batch_graph** out_graph) {
+    if (!b || !values || !point_offsets || !out_graph) return bfail(INTP_ERR_INVALID_ARGUMENT, "null argument");
+    *out_graph = nullptr;
+    EvalWork w;
+    intp_status st = make_eval_work(b, point_offsets, derivs, nderiv, out_dtype, w);
+    if (st != INTP_OK) return st;
+    if (w.npts > 0 && (!coords || !out)) return bfail(INTP_ERR_INVALID_ARGUMENT, "null buffer");
+    intp_batch_graph* g = new (std::nothrow) intp_batch_graph();
+    if (!g) return bfail(INTP_ERR_OUT_OF_MEMORY, "out of host memory");
+    g->b = b;
+    auto gfail = [&](intp_status code) {
+        delete g;
+        return code;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return gfail(bcuda(e, "cudaStreamCreate(capture)"));
+    if (!w.items.empty()) {
+        e = cudaMalloc(&g->items, w.items.size() * sizeof(EvalItem));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(g->items, w.items.data(), w.items.size() * sizeof(EvalItem), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return gfail(bcuda(e, "batch graph work list"));
+    }
+    // one build outside the capture: it sets up the solve's working array and
+    // the side streams, which a capture may not create
+    st = batch_interpolate(b, values, g->cap);
+    if (st != INTP_OK) return gfail(st);
+    e = cudaStreamSynchronize(g->cap);
+    if (e != cudaSuccess) return gfail(bcuda(e, "batch graph warm-up build"));
+    e = cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return gfail(bcuda(e, "cudaStreamBeginCapture"));
+    st = batch_interpolate(b, values, g->cap);
+    if (st == INTP_OK && w.npts > 0)
+        st = launch_eval_work(b, w, static_cast<const EvalItem*>(g->items), coords, out, g->cap);
+    e = cudaStreamEndCapture(g->cap, &g->graph);
+    if (st != INTP_OK) return gfail(st);
+    if (e != cudaSuccess) return gfail(bcuda(e, "cudaStreamEndCapture"));
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) return gfail(bcuda(e, "cudaGraphInstantiate"));
+    *out_graph = g;
+    return INTP_OK;
+}
+
+intp_status intp_batch_graph_launch(intp_batch_graph* g, void* stream) {
+    if (!g) return bfail(INTP_ERR_INVALID_ARGUMENT, "null graph");
+    BATCH_CUDA(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch");
+    g->b->has_ctrl = true;
+    return INTP_OK;
+}
+
+intp_status intp_batch_graph_destroy(intp_batch_graph* g) {
+    delete g;
+    return INTP_OK;
 }
 
 }  // extern "C"

@@ -331,6 +331,22 @@ intp_status intp_batch_get_control_points(const intp_batch* batch, int64_t table
 intp_status intp_batch_eval(const intp_batch* batch, const double* coords, const int64_t* point_offsets,
                             const int32_t* derivs, int32_t nderiv, void* out, int32_t out_dtype, void* stream);
 
+/* A CUDA graph of one build and one evaluation of the batch: the arguments
+ * of intp_batch_build (device values) and intp_batch_eval, fixed at
+ * creation. Creation builds the batch once, uploads the evaluation's work
+ * list, then captures the build's launches (on side streams too) and the
+ * evaluation's launches. intp_batch_graph_launch replays them on `stream`,
+ * reading the values and coordinates then in those buffers; results equal
+ * those of intp_batch_build + intp_batch_eval on the same contents, bit for
+ * bit. The graph keeps pointers to the batch and the buffers: destroy it
+ * first. No counterpart in the reference. */
+typedef struct intp_batch_graph intp_batch_graph;
+intp_status intp_batch_graph_create(intp_batch* batch, const double* values, const double* coords,
+                                    const int64_t* point_offsets, const int32_t* derivs, int32_t nderiv, void* out,
+                                    int32_t out_dtype, intp_batch_graph** out_graph);
+intp_status intp_batch_graph_launch(intp_batch_graph* graph, void* stream);
+intp_status intp_batch_graph_destroy(intp_batch_graph* graph);
+
 /* ---- serving loop ----
  *
  * A worker thread that keeps built tables resident in device memory and

@@ -268,3 +268,33 @@ def test_vector_valued_tables_in_a_batch(precision):
             ref = oracle.Spline(len(dims), order, per, dims, [0.0] * len(dims), [1.0] * len(dims)).interpolate(chan)
             g = got[:, 0, c] if C > 1 else got[:, 0]
             assert norm_rel_err(g, ref.eval(pts[i])) < tol, (i, c)
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_captured_graph_equals_build_and_eval(persistent):
+    """A CUDA graph of one build and one evaluation (intp_batch_graph_*):
+    each replay gives what intp_batch_build + intp_batch_eval give on the
+    buffers' contents at that time, bit for bit, also after the values and
+    the coordinates are overwritten in place between replays."""
+    specs, values, pts = make_uneven_batch(40, 20261211)
+    b = bi.TableBatch(specs, precision="mixed")
+    b.set_schedule(persistent, 32, 32)
+    offsets = np.concatenate([[0], np.cumsum([p.shape[0] for p in pts])]).astype(np.int64)
+    vals = torch.tensor(np.concatenate([v.ravel() for v in values]), device="cuda")
+    coords = torch.tensor(np.concatenate([p.ravel() for p in pts]), device="cuda")
+    derivs = np.array([[0, 0], [1, 0]], np.int32)
+    g = b.graph(vals, coords, offsets, derivs=derivs)
+    try:
+        for step in range(3):
+            if step > 0:
+                vals.mul_(1.0 + 0.25 * step).add_(0.125)
+                coords.mul_(0.999)
+            out = g.launch()
+            torch.cuda.synchronize()
+            got = out.clone()
+            b.build(vals)
+            want = b.evaluate(coords, offsets, derivs=derivs)
+            torch.cuda.synchronize()
+            assert torch.equal(got.reshape(want.shape), want), step
+    finally:
+        g.close()
