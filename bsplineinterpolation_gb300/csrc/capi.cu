@@ -49,7 +49,6 @@ constexpr int64_t kDefaultChunk = int64_t{1} << 25;
 // nothing overlaps), and the device buffers of each kind in the ring
 constexpr int64_t kHostPipelineChunk = int64_t{1} << 25;
 constexpr int64_t kHostHeadChunk = int64_t{1} << 21;
-constexpr int64_t kHostTailChunk = int64_t{1} << 22;
 constexpr int kHostBuffers = 3;
 // the smallest batch worth binning
 constexpr int64_t kBinnedMinPoints = int64_t{1} << 18;
@@ -855,9 +854,12 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     // The copy-in stream allocates its own buffers and does not wait for work
     // queued earlier on the caller's stream, so the coordinates stream in
     // while that work (typically the table's solve) runs; every evaluation
-    // still runs after it. Chunks grow from kHostHeadChunk (the first
-    // evaluation starts early) and the last one is at most kHostTailChunk
-    // (little copy-out remains after the last evaluation).
+    // still runs after it. The copy-in bounds the pipeline (the link moves
+    // fewer points per second than the evaluation), so chunks grow from
+    // kHostHeadChunk (the first evaluation starts early) and then never take
+    // more than half of the points left: the last chunks shrink
+    // geometrically down to the head chunk, and little evaluation and
+    // copy-out remains after the last copy-in.
     constexpr int NB = kHostBuffers;
     cudaStream_t h2d = nullptr, d2h = nullptr;
     cudaEvent_t in_ready[NB] = {}, done[NB] = {}, freed[NB] = {};
@@ -879,8 +881,11 @@ intp_status intp_eval_host(const intp_table* t, const double* coords, int64_t np
     for (int64_t p0 = 0; p0 < npts && st == INTP_OK; ++i) {
         const int j = static_cast<int>(i % NB);
         const int64_t rem = npts - p0;
-        const int64_t tail = std::min(cur, kHostTailChunk);
-        const int64_t n = rem > cur + tail ? cur : (rem > tail ? rem - tail : rem);
+        const int64_t head = std::min(chunk, kHostHeadChunk);
+        // (what is left after a chunk is never below the head chunk, so every
+        // chunk of a batch takes the path one device call on it would take)
+        const int64_t n =
+            std::min(chunk, rem <= 2 * head ? rem : std::min(cur, std::max(head, (rem + 1) / 2)));
         cur = std::min(cur * 2, chunk);
         // buffer j's previous chunk: evaluated (input free) and copied out (output free)
         if (i >= NB) e = cudaStreamWaitEvent(h2d, done[j], 0);

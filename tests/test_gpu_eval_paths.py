@@ -144,9 +144,10 @@ def test_host_buffer_pipeline_equals_device_path(precision):
 
 def test_host_alloc_pipeline_with_growing_chunks():
     """intp_eval_host on page-locked buffers from intp_host_alloc, with a
-    batch large enough for the pipeline's growing chunks (2M, then 1M and a
-    4M tail for 7M points): every chunk takes the binned path and the results
-    equal one device-buffer evaluation bit for bit."""
+    batch large enough for the pipeline's chunks (2^21 points, then two of
+    about 2.45M for 7M points; no chunk below 2^21): every chunk takes the
+    binned path and the results equal one device-buffer evaluation bit for
+    bit."""
     import ctypes as C
     from bsplineinterpolation_gb300 import _lib
     lib = _lib.load()
