@@ -81,6 +81,7 @@ struct intp_batch {
     bool has_ctrl = false;
     intp_batch_schedule sched{0, 32, 32, 0, 0.0};
     void* work = nullptr;                // the schedule's work lists (device)
+    uint64_t work_version = 0;           // bumped whenever the work lists are replaced
     unsigned int* counters = nullptr;    // work counters of the persistent passes (device)
     // The band classes of one pass run concurrently: class order[0] on the
     // caller's stream, the others on these streams, forked from and joined
@@ -319,6 +320,7 @@ intp_status apply_schedule(intp_batch* b, const intp_batch_schedule& sc) {
     }
     b->sched = sc;
     b->sched.build_ms = 0.0;
+    ++b->work_version;
     return INTP_OK;
 }
 
@@ -819,6 +821,7 @@ intp_status intp_batch_eval(const intp_batch* b, const double* coords, const int
 // stream (the build's side streams join the capture through its events).
 struct intp_batch_graph {
     intp_batch* b = nullptr;
+    uint64_t work_version = 0;  // the batch's work lists the capture reads
     void* items = nullptr;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
@@ -871,12 +874,16 @@ intp_status intp_batch_graph_create(intp_batch* b, const double* values, const d
     if (e != cudaSuccess) return gfail(bcuda(e, "cudaStreamEndCapture"));
     e = cudaGraphInstantiate(&g->exec, g->graph, 0);
     if (e != cudaSuccess) return gfail(bcuda(e, "cudaGraphInstantiate"));
+    g->work_version = b->work_version;
     *out_graph = g;
     return INTP_OK;
 }
 
 intp_status intp_batch_graph_launch(intp_batch_graph* g, void* stream) {
     if (!g) return bfail(INTP_ERR_INVALID_ARGUMENT, "null graph");
+    // a new schedule replaced the work lists the capture reads
+    if (g->work_version != g->b->work_version)
+        return bfail(INTP_ERR_STATE, "the batch's schedule changed after the graph was captured");
     BATCH_CUDA(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch");
     g->b->has_ctrl = true;
     return INTP_OK;

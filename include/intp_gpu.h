@@ -339,7 +339,9 @@ intp_status intp_batch_eval(const intp_batch* batch, const double* coords, const
  * reading the values and coordinates then in those buffers; results equal
  * those of intp_batch_build + intp_batch_eval on the same contents, bit for
  * bit. The graph keeps pointers to the batch and the buffers: destroy it
- * first. No counterpart in the reference. */
+ * first. A new schedule (intp_batch_set_schedule, intp_batch_autotune)
+ * replaces the work lists the graph reads: its launches then fail with
+ * INTP_ERR_STATE. No counterpart in the reference. */
 typedef struct intp_batch_graph intp_batch_graph;
 intp_status intp_batch_graph_create(intp_batch* batch, const double* values, const double* coords,
                                     const int64_t* point_offsets, const int32_t* derivs, int32_t nderiv, void* out,

@@ -296,5 +296,9 @@ def test_captured_graph_equals_build_and_eval(persistent):
             want = b.evaluate(coords, offsets, derivs=derivs)
             torch.cuda.synchronize()
             assert torch.equal(got.reshape(want.shape), want), step
+        # a new schedule replaces the work lists the capture reads
+        b.set_schedule(not persistent, 16, 16)
+        with pytest.raises(bi.IntpError):
+            g.launch()
     finally:
         g.close()
