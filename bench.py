@@ -611,7 +611,10 @@ def e2e(args, f, vals, pts, lib, torch):
     for _ in range(max(1, min(args.warmup, 2))):
         step()
     torch.cuda.synchronize()
-    steps = max(1, min(args.steps, 3))
+    # at least 10 steps (about 0.15 s): the device slows down for tens of ms
+    # about every 0.5 s on these hosts, and a window of a few steps that
+    # meets one such slowdown misstates the rate by up to 3x
+    steps = max(10, args.steps)
     t0 = time.perf_counter()
     for _ in range(steps):
         step()

@@ -45,9 +45,12 @@ bool take_injected_alloc_failure() {
 constexpr int64_t kDefaultChunk = int64_t{1} << 25;
 // host-buffer evaluation (intp_eval_host): the largest chunk of its copy-in
 // / evaluate / copy-out pipeline, its first chunk (the copy-in that nothing
-// overlaps; chunks double from it), its last chunk (the copy-out that
-// nothing overlaps), and the device buffers of each kind in the ring
-constexpr int64_t kHostPipelineChunk = int64_t{1} << 25;
+// overlaps; chunks double from it), and the device buffers of each kind in
+// the ring. The host link bounds the pipeline, so small chunks cost little
+// evaluation rate and shorten the evaluation and copy-out left after the
+// last copy-in: 2^22 points measured best on the 3D cubic 256^3 workload
+// (1e8 points: 13.15 ms, against 13.35 at 2^23 and 13.97 at 2^25).
+constexpr int64_t kHostPipelineChunk = int64_t{1} << 22;
 constexpr int64_t kHostHeadChunk = int64_t{1} << 21;
 constexpr int kHostBuffers = 3;
 // the smallest batch worth binning
